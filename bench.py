@@ -1,0 +1,516 @@
+#!/usr/bin/env python
+"""Benchmark of the projection operators (one JSON line on rank 0).
+
+A step is one forward projection plus one backprojection of the workload
+(default: the 2D fan-beam n=2048 problem of the n-sweep: 2048 x 2048 image,
+2048 views over [0, 2 pi), 2897 cells of 1.5, source-isocentre 4096,
+isocentre-detector 2048, seeded 10-ellipse phantom).  ``value`` = operator
+calls per second over all ranks (2 per step), inputs resident in HBM;
+``e2e`` = the same through the public API with the volume copied in from
+pinned host memory and both results copied back every step.
+
+L2 is flushed (a 512 MiB write) between timed steps, outside the per-step
+CUDA events.  Multi-GPU runs are independent replicas (the operators do not
+exchange data), so scaling is weak.
+
+--impl reference     the reference has no CPU path; its operators restated
+                     by the FP64 oracle on the host cores (all threads), each
+                     step a bounded sample of views scaled to full operators
+--impl reference-gpu the reference's own CUDA operators (oracle/_ref shim),
+                     timed like its benchmark: wall clock with a device sync
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
+# the ncu captures summarised in profiles/; None where not captured.
+NCU_TRAFFIC = {
+    ("fan2048", "forward"): None,
+    ("fan2048", "backward"): None,
+}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference", "reference-gpu"])
+    p.add_argument("--workload", default="fan2048",
+                   help="fan<n> (n-sweep: n x n, n views) or cone256 / cone512")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=12.0,
+                   help="CPU work budget of the cpu_baseline sample")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------ workloads
+
+def workload(name: str):
+    from curadon_gb300.phantom import cone_config, fan_config, seed_for
+
+    if name.startswith("fan"):
+        n = int(name[3:])
+        g = fan_config(n)
+        return dict(kind="fan", name=name, n=n, geom=g, seed=seed_for(1, 0),
+                    desc=f"2D fan-beam n={n} forward+backprojection",
+                    config={"workload": f"2D fan-beam n={n}: {n}x{n} image, {n} views over "
+                                        f"[0,2pi), {g['det_shape']} cells x 1.5, DSO {2 * n}, "
+                                        f"DSD {3 * n}; forward + backprojection",
+                            "n": n, "views": n, "det": g["det_shape"]})
+    if name in ("cone256", "cone512"):
+        n = int(name[4:])
+        nangles, det = (360, 384) if n == 256 else (720, 768)
+        g = cone_config(n, nangles, det)
+        return dict(kind="cone", name=name, n=n, geom=g, seed=seed_for(2, n),
+                    desc=f"3D cone-beam {n}^3 forward+backprojection",
+                    config={"workload": f"3D circular cone-beam {n}^3 volume, {nangles} views, "
+                                        f"{det}x{det} cells x 1.5, DSO {2 * n}, DSD {3 * n}; "
+                                        "forward + backprojection",
+                            "n": n, "views": nangles, "det": det})
+    raise SystemExit(f"unknown workload {name}")
+
+
+def fan_sample_count(g) -> int:
+    """Interpolated samples of one 2D forward (sum over rays of rint(max|rd|)),
+    evaluated in float64 (unit spacing, zero offsets, as the workloads use)."""
+    H, W = g["vol_shape"]
+    det = g["det_shape"]
+    ds = float(g.get("det_spacing", 1.0))
+    a = np.asarray(g["angles"], np.float64)
+    dso = np.asarray(g["DSO"], np.float64)
+    dod = np.asarray(g["DSD"], np.float64) - dso
+    c, s_ = np.cos(a), np.sin(a)
+    swx, swy = dso * s_, dso * c
+    p0x, p1x = -det * ds / 2 + 0.5 * ds, -det * ds / 2 + 1.5 * ds
+    c0x, c0y = p0x * c - dod * s_ - swx, -p0x * s_ - dod * c - swy
+    c1x, c1y = p1x * c - dod * s_ - swx, -p1x * s_ - dod * c - swy
+    src = np.stack([swx + W / 2, swy + H / 2], 1)
+    u0 = np.stack([c0x, c0y], 1)
+    du = np.stack([c1x - c0x, c1y - c0y], 1)
+    u = np.arange(det, dtype=np.float64)
+    total = 0
+    for i in range(src.shape[0]):
+        dx = u0[i, 0] + u * du[i, 0]
+        dy = u0[i, 1] + u * du[i, 1]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            tmin = np.full(det, np.finfo(np.float32).tiny)
+            tmax = np.full(det, np.finfo(np.float32).max, dtype=np.float64)
+            for s, d, hi in ((src[i, 0], dx, W), (src[i, 1], dy, H)):
+                t1, t2 = (-1 - s) / d, (hi - s) / d
+                tmin = np.fmin(np.fmax(t1, tmin), np.fmax(t2, tmin))
+                tmax = np.fmax(np.fmin(t1, tmax), np.fmin(t2, tmax))
+        hit = tmin <= tmax - 1e-6
+        m = np.maximum(np.abs(dx), np.abs(dy)) * (tmax - tmin)
+        total += int(np.rint(m[hit]).sum())
+    return total
+
+
+def cone_sample_estimate(g) -> int:
+    n = g["vol_shape"][0]
+    nangles = len(g["angles"])
+    det = g["det_shape"][0]
+    # rays through the volume ~ detector cells covering its shadow, ~n samples each
+    return int(nangles * det * det * 0.6 * n)
+
+
+# ------------------------------------------------------------ clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            import tempfile
+
+            self.path = tempfile.mktemp(suffix=".csv")
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.index), "-lms", "50"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ------------------------------------------------------------ ours
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    import curadon_gb300 as cg
+    from curadon_gb300 import _build
+    from curadon_gb300.phantom import ellipses_2d, ellipsoids_3d
+
+    _build.build()
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    wl = workload(args.workload)
+    g = wl["geom"]
+    if wl["kind"] == "fan":
+        geom = cg.FanGeometry(**g, device=local_rank)
+        vol = ellipses_2d(wl["n"], wl["seed"], device=dev).contiguous()
+    else:
+        geom = cg.ConeGeometry(**g, device=local_rank)
+        vol = ellipsoids_3d(wl["n"], wl["seed"], device=dev).contiguous()
+    sino = torch.zeros(geom.sinogram_shape(), device=dev)
+    vbp = torch.zeros_like(vol)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    launches_per_step = 4  # re-layout + forward, re-layout + backprojection
+
+    def step():
+        cg.forward(vol, sino, geom)
+        vbp.zero_()
+        cg.backward(sino, vbp, geom)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local_rank) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.2)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()
+        e0, e1, e2 = ev[k]
+        e0.record(stream)
+        cg.forward(vol, sino, geom)
+        e1.record(stream)
+        vbp.zero_()
+        cg.backward(sino, vbp, geom)
+        e2.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t_fwd = [ev[k][0].elapsed_time(ev[k][1]) for k in range(args.steps)]
+    t_bwd = [ev[k][1].elapsed_time(ev[k][2]) for k in range(args.steps)]
+    total_ms = sum(t_fwd) + sum(t_bwd)
+
+    # end to end: pinned host volume in, sinogram and backprojection out
+    host_vol = torch.empty(vol.shape, dtype=torch.float32, pin_memory=True)
+    host_vol.copy_(vol.cpu())
+    host_sino = torch.empty(sino.shape, dtype=torch.float32, pin_memory=True)
+    host_vbp = torch.empty(vol.shape, dtype=torch.float32, pin_memory=True)
+    dvol = torch.empty_like(vol)
+    h2d = host_vol.numel() * 4
+    d2h = (host_sino.numel() + host_vbp.numel()) * 4
+
+    def e2e_step():
+        dvol.copy_(host_vol, non_blocking=True)
+        cg.forward(dvol, sino, geom)
+        vbp.zero_()
+        cg.backward(sino, vbp, geom)
+        host_sino.copy_(sino, non_blocking=True)
+        host_vbp.copy_(vbp, non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    e_ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()
+        e_ev[k][0].record(stream)
+        e2e_step()
+        e_ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    e2e_ms = sum(a.elapsed_time(b) for a, b in e_ev)
+    clocks = sampler.stop() if sampler else None
+
+    # max over ranks
+    tt = torch.tensor([total_ms, e2e_ms, sum(t_fwd), sum(t_bwd)], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    total_ms, e2e_ms, fwd_ms, bwd_ms = (float(v) for v in tt.cpu())
+    if rank != 0:
+        return None
+
+    ops = 2 * args.steps * world
+    value = ops / (total_ms / 1e3)
+    ms_fwd = fwd_ms / args.steps
+    ms_bwd = bwd_ms / args.steps
+
+    # roofline of the dominant operator: compulsory bytes per call / its time
+    if wl["kind"] == "fan":
+        nvox = wl["n"] * wl["n"]
+        nrays = len(g["angles"]) * g["det_shape"]
+        s_fwd = fan_sample_count(g)
+        s_bwd = nvox * len(g["angles"])
+        gather = {"forward": 16, "backward": 8}
+    else:
+        nvox = wl["n"] ** 3
+        nrays = len(g["angles"]) * g["det_shape"][0] * g["det_shape"][1]
+        s_fwd = cone_sample_estimate(g)
+        s_bwd = nvox * len(g["angles"])
+        gather = {"forward": 32, "backward": 16}
+    b_alg = {"forward": 4 * (nvox + nrays), "backward": 4 * (nrays + 2 * nvox)}
+    dom = "forward" if ms_fwd >= ms_bwd else "backward"
+    t_dom = (ms_fwd if dom == "forward" else ms_bwd) / 1e3
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    achieved = b_alg[dom] / t_dom / 1e9
+    samples = s_fwd if dom == "forward" else s_bwd
+    traffic = NCU_TRAFFIC.get((wl["name"], dom))
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 3), "peak": peak,
+                "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "algorithmic_bytes": b_alg[dom],
+                "samples_per_s": samples / t_dom,
+                "gather_GBps": samples * gather[dom] / t_dom / 1e9,
+                "note": "gather-bound (L1/issue), not HBM-bound: the compulsory bytes are "
+                        "L2-resident; samples_per_s is the efficiency figure"}
+
+    line = {
+        "metric": "fwd/bwd proj ops/s", "value": value, "unit": "ops/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded ellipse phantom)",
+        "config": dict(wl["config"], l2="flushed between timed steps (512 MiB write, outside "
+                                          "the per-step events)", parallelism=f"replicas{world}"),
+        "fwd_ops_s": args.steps * world / (fwd_ms / 1e3),
+        "bwd_ops_s": args.steps * world / (bwd_ms / 1e3),
+        "ms_forward": ms_fwd, "ms_backward": ms_bwd,
+        "e2e": {"value": ops / (e2e_ms / 1e3), "unit": "ops/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": roofline,
+        "clocks": clocks,
+    }
+    return line
+
+
+# ------------------------------------------------------------ CPU (oracle)
+
+def _sub_geom(g, kind, views):
+    h = dict(g)
+    h["angles"] = np.asarray(g["angles"])[:views]
+    if kind == "fan":
+        h["DSO"] = np.asarray(g["DSO"])[:views]
+        h["DSD"] = np.asarray(g["DSD"])[:views]
+    return h
+
+
+def cpu_sample(wl, budget_s: float, threads: int):
+    """Times the oracle on the first v views of forward and backprojection,
+    v sized to the budget, and scales to full operators.  Returns
+    (ops_per_s, description)."""
+    import oracle
+    from curadon_gb300.phantom import ellipses_2d, ellipsoids_3d
+
+    g = wl["geom"]
+    kind = wl["kind"]
+    nviews = len(g["angles"])
+    if kind == "fan":
+        vol = ellipses_2d(wl["n"], wl["seed"]).numpy()
+        fwd, bwd = oracle.fwd2d, oracle.bwd2d
+    else:
+        vol = ellipsoids_3d(wl["n"], wl["seed"]).numpy()
+        fwd, bwd = oracle.fwd3d, oracle.bwd3d
+
+    def run(v):
+        h = _sub_geom(g, kind, v)
+        t0 = time.perf_counter()
+        s = fwd(h, vol, nthreads=threads)
+        t1 = time.perf_counter()
+        bwd(h, s.astype(np.float32), nthreads=threads)
+        t2 = time.perf_counter()
+        return t1 - t0, t2 - t1
+
+    tf1, tb1 = run(1)
+    per_view = max(tf1 + tb1, 1e-4)
+    v = int(max(1, min(nviews, budget_s / per_view)))
+    tf, tb = run(v)
+    full = (tf + tb) * nviews / v
+    return 2.0 / full, (f"forward and backprojection over the first {v} of {nviews} views, "
+                        f"FP64 oracle, scaled by {nviews}/{v}")
+
+
+def run_reference_cpu(args, rank, world):
+    if rank != 0:
+        return None
+    wl = workload(args.workload)
+    threads = os.cpu_count() or 1
+    per_step = []
+    desc = ""
+    budget = 2.0
+    for k in range(args.warmup + args.steps):
+        ops_s, desc = cpu_sample(wl, budget, threads)
+        if k >= args.warmup:
+            per_step.append(2.0 / ops_s)
+    total = sum(per_step)
+    value = 2 * args.steps / total
+    return {
+        "impl": "reference", "metric": "fwd/bwd proj ops/s", "value": value, "unit": "ops/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ellipse phantom)",
+        "config": dict(wl["config"], parallelism="host cores"),
+        "cpu_baseline": {"value": value, "unit": "ops/s", "cores": threads, "kind": "port",
+                         "sample": desc + " (the reference has no CPU path; its operators "
+                                          "restated by the oracle)"},
+        "e2e": {"value": value, "unit": "ops/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def run_reference_gpu(args, rank, world, local_rank):
+    if rank != 0:
+        return None
+    import torch
+
+    import oracle
+    from oracle import build_ref
+    from curadon_gb300.phantom import ellipses_2d, ellipsoids_3d
+
+    if build_ref.build() is None or not oracle.ref_available():
+        return {"impl": "reference-gpu", "unavailable": "reference headers not staged/built"}
+    ref = oracle.RefOps()
+    dev = torch.device("cuda", local_rank)
+    wl = workload(args.workload)
+    g = wl["geom"]
+    tf, tb = [], []
+    if wl["kind"] == "fan":
+        vol = ellipses_2d(wl["n"], wl["seed"], device=dev).contiguous()
+        h, n = ref.plan2d(g)
+        sino = torch.zeros((n, g["det_shape"]), device=dev)
+        vbp = torch.zeros_like(vol)
+
+        def fwd():
+            ref.forward2d(h, vol.data_ptr(), sino.data_ptr())
+
+        def bwd():
+            vbp.zero_()
+            ref.backward2d(h, vbp.data_ptr(), sino.data_ptr())
+    else:
+        vol = ellipsoids_3d(wl["n"], wl["seed"], device=dev).contiguous()
+        n = len(g["angles"])
+        sino = torch.zeros((n, *g["det_shape"]), device=dev)
+        vbp = torch.zeros_like(vol)
+
+        def fwd():
+            ref.forward3d(g, vol.data_ptr(), sino.data_ptr())
+
+        def bwd():
+            vbp.zero_()
+            ref.backward3d(g, vbp.data_ptr(), sino.data_ptr())
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        fwd(), bwd()
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fwd()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        bwd()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        tf.append(t1 - t0)
+        tb.append(t2 - t1)
+    total = sum(tf) + sum(tb)
+    return {
+        "impl": "reference-gpu", "metric": "fwd/bwd proj ops/s",
+        "value": 2 * args.steps / total, "unit": "ops/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded ellipse phantom)", "config": wl["config"],
+        "fwd_ops_s": args.steps / sum(tf), "bwd_ops_s": args.steps / sum(tb),
+        "ms_forward": sum(tf) / args.steps * 1e3, "ms_backward": sum(tb) / args.steps * 1e3,
+        "timing": "wall clock around each synchronous reference call (its own protocol)",
+    }
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        line = run_reference_cpu(args, rank, world)
+    elif args.impl == "reference-gpu":
+        line = run_reference_gpu(args, rank, world, local_rank)
+    else:
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+
+            torch.cuda.set_device(local_rank)
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+        line = run_ours(args, rank, world, local_rank)
+        if line is not None and world == 1 and not args.no_cpu_baseline:
+            wl = workload(args.workload)
+            threads = os.cpu_count() or 1
+            ops_s, desc = cpu_sample(wl, args.cpu_seconds, threads)
+            line["cpu_baseline"] = {"value": ops_s, "unit": "ops/s", "cores": threads,
+                                    "kind": "port", "sample": desc}
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,21 @@
+"""curadon_gb300 -- curadon's X-ray CT projection operators on GB300 (sm_103a).
+
+Drop-in for the reference package ``curadon``: ``FanGeometry``,
+``ConeGeometry``, ``forward(volume, sinogram, geom)``,
+``backward(sinogram, volume, geom)``, ``TorchForward``,
+``TorchBackprojection`` and the native module's ``plan_2d``, ``forward_2d``,
+``backward_2d``, ``forward_3d``, ``backward_3d``.  The operators are
+hand-written CUDA kernels behind the C ABI of ``include/curadon_gb300.h``;
+there is no CPU fallback.
+"""
+from . import backend
+from .backend import backward_2d, backward_3d, forward_2d, forward_3d, plan_2d, plan_3d
+from .geometry import ConeGeometry, FanGeometry, geom_to_str
+from .ops import TorchBackprojection, TorchForward, backward, forward
+
+__all__ = [
+    "FanGeometry", "ConeGeometry", "geom_to_str", "forward", "backward", "TorchForward",
+    "TorchBackprojection", "plan_2d", "plan_3d", "forward_2d", "backward_2d", "forward_3d",
+    "backward_3d", "backend",
+]
+__version__ = "1.0.0"

@@ -1,0 +1,499 @@
+// capi.cu -- the extern "C" boundary (include/curadon_gb300.h): argument
+// checking, plan construction and the operator entry points.
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace cg {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+int set_error(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+template <class T>
+static int alloc_copy(T **dst, const T *src, size_t n) {
+    CG_TRY_CUDA(cudaMalloc(dst, sizeof(T) * (n ? n : 1)));
+    if (n) CG_TRY_CUDA(cudaMemcpy(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice));
+    return CG_OK;
+}
+
+void free_plan2d(Plan2d *p) {
+    if (!p) return;
+    void *ptrs[] = {p->d_angles, p->d_DSO, p->d_DSD, p->d_src,  p->d_u0,
+                    p->d_du,     p->d_bmeta, p->d_layA, p->d_layB, p->d_sinoP};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+}
+
+void free_plan3d(Plan3d *p) {
+    if (!p) return;
+    void *ptrs[] = {p->d_forg, p->d_fdu, p->d_fdv, p->d_fsrc, p->d_borg, p->d_bdx,
+                    p->d_bdy,  p->d_bdz, p->d_volA, p->d_volB, p->d_sinoP};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+}
+
+// ------------------------------------------------------------ 3D geometry
+
+namespace {
+
+// Three-vector with the component-wise float operations of the reference's
+// vec<f32, 3> (vec.hpp), used to evaluate the per-view geometry in the same
+// FP32 operation order as the reference's host code.
+struct V3 {
+    float v[3];
+    float &operator[](int i) { return v[i]; }
+    float operator[](int i) const { return v[i]; }
+};
+inline V3 operator+(const V3 &a, const V3 &b) { return {{a[0] + b[0], a[1] + b[1], a[2] + b[2]}}; }
+inline V3 operator-(const V3 &a, const V3 &b) { return {{a[0] - b[0], a[1] - b[1], a[2] - b[2]}}; }
+inline V3 operator/(const V3 &a, const V3 &b) { return {{a[0] / b[0], a[1] / b[1], a[2] / b[2]}}; }
+inline V3 operator/(const V3 &a, float s) { return {{a[0] / s, a[1] / s, a[2] / s}}; }
+
+// Y-Z-Y Euler rotation, rotation.hpp:7-28 (matrix written out there).
+V3 rot_yzy(const V3 &v, float phi, float theta, float psi) {
+    const float cphi = std::cos(phi), sphi = std::sin(phi);
+    const float ctheta = std::cos(theta), stheta = std::sin(theta);
+    const float spsi = std::sin(psi), cpsi = std::cos(psi);
+    V3 r;
+    r[0] = v[0] * (cphi * cpsi * ctheta - sphi * spsi) - v[1] * stheta * cphi +
+           v[2] * (sphi * cpsi + spsi * cphi * ctheta);
+    r[1] = v[0] * (stheta * cpsi) + v[1] * ctheta + v[2] * spsi * stheta;
+    r[2] = v[0] * (-sphi * cpsi * ctheta - spsi * cphi) + v[1] * sphi * stheta +
+           v[2] * (-sphi * spsi * ctheta + cpsi * cphi);
+    return r;
+}
+
+// Roll-pitch-yaw rotation, rotation.hpp:31-48.
+V3 rot_rpy(const V3 &v, float roll, float pitch, float yaw) {
+    const float croll = std::cos(roll), sroll = std::sin(roll);
+    const float cpitch = std::cos(pitch), spitch = std::sin(pitch);
+    const float syaw = std::sin(yaw), cyaw = std::cos(yaw);
+    V3 r;
+    r[0] = croll * cpitch * v[0] + (croll * spitch * syaw - sroll * cyaw) * v[1] +
+           (croll * spitch * cyaw + sroll * syaw) * v[2];
+    r[1] = sroll * cpitch * v[0] + (sroll * spitch * syaw + croll * cyaw) * v[1] +
+           (sroll * spitch * cyaw - croll * syaw) * v[2];
+    r[2] = -spitch * v[0] + cpitch * syaw * v[1] + cpitch * cyaw * v[2];
+    return r;
+}
+
+inline float4 f4(const V3 &a) { return make_float4(a[0], a[1], a[2], 0.f); }
+
+struct Cone {
+    V3 shape_f, spacing, offset;  // internal (x, y, z)
+    float U, V;                   // detector cells as float (u, v)
+    float su, sv, offu, offv;
+    float pitch, roll, yaw, DSO, DSD, COR;
+};
+
+// Forward tables: forward_3d.hpp:117-190.
+void cone_fwd_tables(const Cone &c, const float *phi, const float *theta, const float *psi,
+                     int n, std::vector<float4> &org, std::vector<float4> &du,
+                     std::vector<float4> &dv, std::vector<float4> &src) {
+    const V3 vol_size = {{c.shape_f[0] * c.spacing[0], c.shape_f[1] * c.spacing[1],
+                          c.shape_f[2] * c.spacing[2]}};
+    const float DOD = c.DSD - c.DSO;
+    for (int i = 0; i < n; ++i) {
+        V3 s0 = {{0.f, 0.f, -c.DSO}};
+        V3 o0 = {{-c.su * (c.U / 2.f) + c.su * 0.5f, -c.sv * (c.V / 2.f) + c.sv * 0.5f, 0.f}};
+        V3 u0 = o0 + V3{{c.su, 0.f, 0.f}};
+        V3 v0 = o0 + V3{{0.f, c.sv, 0.f}};
+        o0 = rot_rpy(o0, c.roll, c.pitch, c.yaw);
+        u0 = rot_rpy(u0, c.roll, c.pitch, c.yaw);
+        v0 = rot_rpy(v0, c.roll, c.pitch, c.yaw);
+        o0[2] += DOD;
+        u0[2] += DOD;
+        v0[2] += DOD;
+        V3 o = rot_yzy(o0, phi[i], theta[i], psi[i]);
+        V3 pu = rot_yzy(u0, phi[i], theta[i], psi[i]);
+        V3 pv = rot_yzy(v0, phi[i], theta[i], psi[i]);
+        V3 s = rot_yzy(s0, phi[i], theta[i], psi[i]);
+        const V3 tr = vol_size / 2.f - c.spacing / 2.f;
+        o = o - c.offset + tr;
+        pu = pu - c.offset + tr;
+        pv = pv - c.offset + tr;
+        s = s - c.offset + tr;
+        o = o / c.spacing;
+        pu = pu / c.spacing;
+        pv = pv / c.spacing;
+        s = s / c.spacing;
+        const float cor_x = c.COR * std::sin(phi[i]) / c.spacing[0];
+        const float cor_z = c.COR * std::cos(phi[i]) / c.spacing[2];
+        o[0] += cor_x, o[2] += cor_z, pu[0] += cor_x, pu[2] += cor_z;
+        pv[0] += cor_x, pv[2] += cor_z, s[0] += cor_x, s[2] += cor_z;
+        org.push_back(f4(o));
+        du.push_back(f4(pu - o));
+        dv.push_back(f4(pv - o));
+        src.push_back(f4(s));
+    }
+}
+
+// Backward tables: backward_3d.hpp:122-166 and the source of :218-227.
+void cone_bwd_tables(const Cone &c, const float *phi, const float *theta, const float *psi,
+                     int n, std::vector<float4> &org, std::vector<float4> &dx,
+                     std::vector<float4> &dy, std::vector<float4> &dz, float src[3]) {
+    const V3 ext = {{c.shape_f[0] * c.spacing[0], c.shape_f[1] * c.spacing[1],
+                     c.shape_f[2] * c.spacing[2]}};
+    const float DOD = c.DSD - c.DSO;
+    const V3 neg_ext = {{-ext[0], -ext[1], -ext[2]}};
+    const V3 init = neg_ext / 2.f + c.spacing / 2.f + c.offset;
+    for (int i = 0; i < n; ++i) {
+        auto fn = [&](V3 p) {
+            p = rot_yzy(p, phi[i], theta[i], psi[i]);
+            p[0] += c.offu;
+            p[1] += c.offv;
+            p[2] -= DOD;
+            p = rot_rpy(p, c.roll, c.pitch, c.yaw);
+            p[2] += DOD;
+            return p;
+        };
+        const V3 o = fn(init);
+        org.push_back(f4(o));
+        V3 d = init;
+        d[0] += c.spacing[0];
+        dx.push_back(f4(fn(d) - o));
+        d = init;
+        d[1] += c.spacing[1];
+        dy.push_back(f4(fn(d) - o));
+        d = init;
+        d[2] += c.spacing[2];
+        dz.push_back(f4(fn(d) - o));
+    }
+    V3 s = {{-c.offu, -c.offv, -c.DSO}};
+    s[2] -= DOD;
+    s = rot_rpy(s, c.roll, c.pitch, c.yaw);
+    s[2] += DOD;
+    src[0] = s[0], src[1] = s[1], src[2] = s[2];
+}
+
+bool finite_all(const float *a, uint64_t n) {
+    for (uint64_t i = 0; i < n; ++i)
+        if (!std::isfinite(a[i])) return false;
+    return true;
+}
+
+int check_device(int device) {
+    int count = 0;
+    CG_TRY_CUDA(cudaGetDeviceCount(&count));
+    CG_REQUIRE(device >= 0 && device < count, "device index out of range");
+    return CG_OK;
+}
+
+int make_plan3d(cg_plan3d **out, int device, const uint64_t vol_shape[3], const float vol_spacing[3],
+                const float vol_offset[3], const float *phi, const float *theta,
+                const float *psi, uint64_t nangles, const uint64_t det_shape[2],
+                const float det_spacing[2], const float det_offset[2],
+                const float det_rotation[3], float DSO, float DSD, float COR) {
+    CG_REQUIRE(out, "plan output pointer is NULL");
+    *out = nullptr;
+    CG_REQUIRE(vol_shape && vol_spacing && vol_offset && det_shape && det_spacing && det_offset &&
+                   det_rotation,
+               "geometry array is NULL");
+    CG_REQUIRE(nangles > 0 && phi && theta && psi, "angles are missing");
+    CG_REQUIRE(nangles <= 65535, "at most 65535 views per plan");
+    for (int d = 0; d < 3; ++d)
+        CG_REQUIRE(vol_shape[d] > 0 && vol_shape[d] <= (1u << 16), "volume shape out of range");
+    for (int d = 0; d < 2; ++d)
+        CG_REQUIRE(det_shape[d] > 0 && det_shape[d] <= (1u << 16), "detector shape out of range");
+    CG_REQUIRE(finite_all(phi, nangles) && finite_all(theta, nangles) && finite_all(psi, nangles),
+               "angles must be finite");
+    CG_REQUIRE(std::isfinite(DSO) && std::isfinite(DSD) && std::isfinite(COR),
+               "DSO, DSD and COR must be finite");
+    {
+        int rc = check_device(device);
+        if (rc) return rc;
+    }
+    DeviceGuard guard(device);
+    CG_REQUIRE(guard.ok(), "cannot select device");
+
+    std::unique_ptr<cg_plan3d> p(new cg_plan3d());
+    p->device = device;
+    // Python (z, y, x) -> internal (x, y, z); (v, u) -> (u, v) (forward.cu:47-58)
+    p->X = (int)vol_shape[2], p->Y = (int)vol_shape[1], p->Z = (int)vol_shape[0];
+    p->U = (int)det_shape[1], p->V = (int)det_shape[0];
+    p->nangles = (int)nangles;
+    p->DSO = DSO, p->DSD = DSD;
+    Cone c;
+    c.shape_f = {{(float)vol_shape[2], (float)vol_shape[1], (float)vol_shape[0]}};
+    c.spacing = {{vol_spacing[2], vol_spacing[1], vol_spacing[0]}};
+    c.offset = {{vol_offset[2], vol_offset[1], vol_offset[0]}};
+    c.U = (float)det_shape[1], c.V = (float)det_shape[0];
+    c.su = det_spacing[1], c.sv = det_spacing[0];
+    c.offu = det_offset[1], c.offv = det_offset[0];
+    c.pitch = det_rotation[0], c.roll = det_rotation[1], c.yaw = det_rotation[2];
+    c.DSO = DSO, c.DSD = DSD, c.COR = COR;
+
+    std::vector<float4> fo, fu, fv, fs, bo, bx, by, bz;
+    cone_fwd_tables(c, phi, theta, psi, (int)nangles, fo, fu, fv, fs);
+    cone_bwd_tables(c, phi, theta, psi, (int)nangles, bo, bx, by, bz, p->bsrc);
+    int rc = CG_OK;
+    auto fail = [&](int code) {
+        free_plan3d(p.get());
+        return code;
+    };
+    if ((rc = alloc_copy(&p->d_forg, fo.data(), nangles))) return fail(rc);
+    if ((rc = alloc_copy(&p->d_fdu, fu.data(), nangles))) return fail(rc);
+    if ((rc = alloc_copy(&p->d_fdv, fv.data(), nangles))) return fail(rc);
+    if ((rc = alloc_copy(&p->d_fsrc, fs.data(), nangles))) return fail(rc);
+    if ((rc = alloc_copy(&p->d_borg, bo.data(), nangles))) return fail(rc);
+    if ((rc = alloc_copy(&p->d_bdx, bx.data(), nangles))) return fail(rc);
+    if ((rc = alloc_copy(&p->d_bdy, by.data(), nangles))) return fail(rc);
+    if ((rc = alloc_copy(&p->d_bdz, bz.data(), nangles))) return fail(rc);
+    *out = p.release();
+    return CG_OK;
+}
+
+}  // namespace
+}  // namespace cg
+
+using namespace cg;
+
+// ============================================================ C ABI
+
+extern "C" {
+
+const char *cg_last_error(void) { return g_last_error.c_str(); }
+
+int cg_version(void) { return 1 * 10000 + 0 * 100 + 0; }
+
+int cg_plan2d_create(cg_plan2d **plan, int device, uint32_t vol_prec, const uint64_t vol_shape[2],
+                     const float vol_spacing[2], const float vol_offset[2], uint32_t det_prec,
+                     uint64_t det_count, float det_spacing, float det_offset, const float *DSO,
+                     const float *DSD, const float *angles, uint64_t nangles, float det_pitch,
+                     float COR) {
+    clear_error();
+    CG_REQUIRE(plan, "plan output pointer is NULL");
+    *plan = nullptr;
+    // dtype_to_precision (plan.cu:20-28): 32 or 16, anything else is an error
+    CG_REQUIRE((vol_prec == 32 || vol_prec == 16) && (det_prec == 32 || det_prec == 16),
+               "Precision must either be f32 or f16");
+    if (vol_prec != 32 || det_prec != 32)
+        return set_error(CG_ERR_UNSUPPORTED, "f16 volumes/sinograms are not built (f32 only)");
+    CG_REQUIRE(vol_shape && vol_spacing && vol_offset, "volume geometry array is NULL");
+    CG_REQUIRE(DSO && DSD && angles, "DSO, DSD and angles must be given");
+    CG_REQUIRE(nangles > 0, "at least one view is needed");
+    CG_REQUIRE(nangles <= (1u << 22), "too many views");
+    CG_REQUIRE(det_count > 0 && det_count <= (1u << 20), "det_count out of range");
+    CG_REQUIRE(vol_shape[0] > 0 && vol_shape[1] > 0 && vol_shape[0] <= (1u << 15) &&
+                   vol_shape[1] <= (1u << 15),
+               "volume shape out of range");
+    CG_REQUIRE(finite_all(angles, nangles) && finite_all(DSO, nangles) && finite_all(DSD, nangles),
+               "angles, DSO and DSD must be finite");
+    CG_REQUIRE(std::isfinite(det_spacing) && det_spacing != 0.f, "det_spacing must be nonzero");
+    CG_REQUIRE(vol_spacing[0] != 0.f && vol_spacing[1] != 0.f, "vol_spacing must be nonzero");
+    {
+        int rc = check_device(device);
+        if (rc) return rc;
+    }
+    DeviceGuard guard(device);
+    CG_REQUIRE(guard.ok(), "cannot select device");
+
+    std::unique_ptr<cg_plan2d> p(new cg_plan2d());
+    p->device = device;
+    // Python (y, x) -> internal (x, y) (plan.cu:48-50)
+    p->W = (int)vol_shape[1], p->H = (int)vol_shape[0];
+    p->sx = vol_spacing[1], p->sy = vol_spacing[0];
+    p->ox = vol_offset[1], p->oy = vol_offset[0];
+    p->det = (int)det_count, p->ds = det_spacing, p->doff = det_offset;
+    p->nangles = (int)nangles, p->pitch = det_pitch, p->COR = COR;
+    int rc = CG_OK;
+    auto fail = [&](int code) {
+        free_plan2d(p.get());
+        return code;
+    };
+    const size_t n = nangles;
+    if ((rc = alloc_copy(&p->d_angles, angles, n))) return fail(rc);
+    if ((rc = alloc_copy(&p->d_DSO, DSO, n))) return fail(rc);
+    if ((rc = alloc_copy(&p->d_DSD, DSD, n))) return fail(rc);
+    auto try_malloc = [&](auto **ptr, size_t elems) {
+        cudaError_t e = cudaMalloc(ptr, sizeof(**ptr) * elems);
+        if (e != cudaSuccess)
+            return set_error(e == cudaErrorMemoryAllocation ? CG_ERR_NOMEM : CG_ERR_CUDA,
+                             std::string("plan allocation: ") + cudaGetErrorString(e));
+        return CG_OK;
+    };
+    if ((rc = try_malloc(&p->d_src, n))) return fail(rc);
+    if ((rc = try_malloc(&p->d_u0, n))) return fail(rc);
+    if ((rc = try_malloc(&p->d_du, n))) return fail(rc);
+    if ((rc = try_malloc(&p->d_bmeta, n))) return fail(rc);
+    if ((rc = try_malloc(&p->d_layA, (size_t)p->pitchA() * (p->H + 2 * kPad)))) return fail(rc);
+    if ((rc = try_malloc(&p->d_layB, (size_t)p->pitchB() * (p->W + 2 * kPad)))) return fail(rc);
+    if ((rc = try_malloc(&p->d_sinoP, (size_t)p->pitchS() * n))) return fail(rc);
+    if ((rc = launch_plan2d_tables(*p, 0))) return fail(rc);
+    {
+        cudaError_t e = cudaStreamSynchronize(0);
+        if (e != cudaSuccess) return fail(set_error(CG_ERR_CUDA, cudaGetErrorString(e)));
+    }
+    *plan = p.release();
+    return CG_OK;
+}
+
+int cg_plan2d_destroy(cg_plan2d *plan) {
+    clear_error();
+    if (!plan) return CG_OK;
+    {
+        DeviceGuard guard(plan->device);
+        free_plan2d(plan);
+    }
+    delete plan;
+    return CG_OK;
+}
+
+int cg_plan2d_get_forward_block(const cg_plan2d *plan, uint64_t *bx, uint64_t *by) {
+    clear_error();
+    CG_REQUIRE(plan && bx && by, "NULL argument");
+    *bx = (uint64_t)plan->fwd_bx, *by = (uint64_t)plan->fwd_by;
+    return CG_OK;
+}
+
+int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by) {
+    clear_error();
+    CG_REQUIRE(plan, "plan is NULL");
+    CG_REQUIRE(bx >= 32 && bx % 32 == 0 && by >= 1 && bx * by <= 256,
+               "forward block must be a multiple of 32 cells wide and at most 256 threads");
+    plan->fwd_bx = (int)bx, plan->fwd_by = (int)by;
+    return CG_OK;
+}
+
+int cg_plan2d_tables(const cg_plan2d *plan, float *sources, float *u_origins, float *delta_us) {
+    clear_error();
+    CG_REQUIRE(plan, "plan is NULL");
+    DeviceGuard guard(plan->device);
+    const size_t bytes = sizeof(float2) * plan->nangles;
+    if (sources) CG_TRY_CUDA(cudaMemcpy(sources, plan->d_src, bytes, cudaMemcpyDeviceToHost));
+    if (u_origins) CG_TRY_CUDA(cudaMemcpy(u_origins, plan->d_u0, bytes, cudaMemcpyDeviceToHost));
+    if (delta_us) CG_TRY_CUDA(cudaMemcpy(delta_us, plan->d_du, bytes, cudaMemcpyDeviceToHost));
+    return CG_OK;
+}
+
+int cg_forward_2d(cg_plan2d *plan, const float *volume, float *sinogram, void *stream) {
+    clear_error();
+    CG_REQUIRE(plan, "plan is NULL");
+    CG_REQUIRE(volume && sinogram, "volume and sinogram must be device pointers");
+    DeviceGuard guard(plan->device);
+    CG_REQUIRE(guard.ok(), "cannot select the plan's device");
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = launch_relayout2d(*plan, volume, s);
+    if (rc) return rc;
+    return launch_forward2d(*plan, sinogram, s);
+}
+
+int cg_backward_2d(cg_plan2d *plan, float *volume, const float *sinogram, void *stream) {
+    clear_error();
+    CG_REQUIRE(plan, "plan is NULL");
+    CG_REQUIRE(volume && sinogram, "volume and sinogram must be device pointers");
+    DeviceGuard guard(plan->device);
+    CG_REQUIRE(guard.ok(), "cannot select the plan's device");
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = launch_relayout_sino2d(*plan, sinogram, s);
+    if (rc) return rc;
+    return launch_backward2d(*plan, volume, s);
+}
+
+int cg_plan3d_create(cg_plan3d **plan, int device, const uint64_t vol_shape[3],
+                     const float vol_spacing[3], const float vol_offset[3], const float *phi,
+                     const float *theta, const float *psi, uint64_t nangles,
+                     const uint64_t det_shape[2], const float det_spacing[2],
+                     const float det_offset[2], const float det_rotation[3], float DSO, float DSD,
+                     float COR) {
+    clear_error();
+    return make_plan3d(plan, device, vol_shape, vol_spacing, vol_offset, phi, theta, psi, nangles,
+                       det_shape, det_spacing, det_offset, det_rotation, DSO, DSD, COR);
+}
+
+int cg_plan3d_destroy(cg_plan3d *plan) {
+    clear_error();
+    if (!plan) return CG_OK;
+    {
+        DeviceGuard guard(plan->device);
+        free_plan3d(plan);
+    }
+    delete plan;
+    return CG_OK;
+}
+
+int cg_forward_3d_plan(cg_plan3d *plan, const float *volume, float *sinogram, void *stream) {
+    clear_error();
+    CG_REQUIRE(plan, "plan is NULL");
+    CG_REQUIRE(volume && sinogram, "volume and sinogram must be device pointers");
+    DeviceGuard guard(plan->device);
+    CG_REQUIRE(guard.ok(), "cannot select the plan's device");
+    int rc = ensure_plan3d_scratch(*plan, true, false);
+    if (rc) return rc;
+    return launch_forward3d(*plan, volume, sinogram, (cudaStream_t)stream);
+}
+
+int cg_backward_3d_plan(cg_plan3d *plan, float *volume, const float *sinogram, void *stream) {
+    clear_error();
+    CG_REQUIRE(plan, "plan is NULL");
+    CG_REQUIRE(volume && sinogram, "volume and sinogram must be device pointers");
+    DeviceGuard guard(plan->device);
+    CG_REQUIRE(guard.ok(), "cannot select the plan's device");
+    int rc = ensure_plan3d_scratch(*plan, false, true);
+    if (rc) return rc;
+    return launch_backward3d(*plan, volume, sinogram, (cudaStream_t)stream);
+}
+
+static int current_device(int *dev) {
+    CG_TRY_CUDA(cudaGetDevice(dev));
+    return CG_OK;
+}
+
+int cg_forward_3d(const float *x, const uint64_t vol_shape[3], const float vol_spacing[3],
+                  const float vol_offset[3], float *sinogram, const float *phi,
+                  const float *theta, const float *psi, uint64_t nangles,
+                  const uint64_t det_shape[2], const float det_spacing[2],
+                  const float det_offset[2], const float det_rotation[3], float DSO, float DSD,
+                  float COR, void *stream) {
+    clear_error();
+    int dev = 0, rc = current_device(&dev);
+    if (rc) return rc;
+    cg_plan3d *p = nullptr;
+    rc = make_plan3d(&p, dev, vol_shape, vol_spacing, vol_offset, phi, theta, psi, nangles,
+                     det_shape, det_spacing, det_offset, det_rotation, DSO, DSD, COR);
+    if (rc) return rc;
+    rc = ensure_plan3d_scratch(*p, true, false);
+    if (!rc) rc = launch_forward3d(*p, x, sinogram, (cudaStream_t)stream);
+    // The transient plan's memory is released once the stream has used it.
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (!rc && e != cudaSuccess) rc = set_error(CG_ERR_CUDA, cudaGetErrorString(e));
+    free_plan3d(p);
+    delete p;
+    return rc;
+}
+
+int cg_backward_3d(float *x, const uint64_t vol_shape[3], const float vol_spacing[3],
+                   const float vol_offset[3], const float *sinogram, const float *phi,
+                   const float *theta, const float *psi, uint64_t nangles,
+                   const uint64_t det_shape[2], const float det_spacing[2],
+                   const float det_offset[2], const float det_rotation[3], float DSO, float DSD,
+                   float COR, void *stream) {
+    clear_error();
+    int dev = 0, rc = current_device(&dev);
+    if (rc) return rc;
+    cg_plan3d *p = nullptr;
+    rc = make_plan3d(&p, dev, vol_shape, vol_spacing, vol_offset, phi, theta, psi, nangles,
+                     det_shape, det_spacing, det_offset, det_rotation, DSO, DSD, COR);
+    if (rc) return rc;
+    rc = ensure_plan3d_scratch(*p, false, true);
+    if (!rc) rc = launch_backward3d(*p, x, sinogram, (cudaStream_t)stream);
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (!rc && e != cudaSuccess) rc = set_error(CG_ERR_CUDA, cudaGetErrorString(e));
+    free_plan3d(p);
+    delete p;
+    return rc;
+}
+
+}  // extern "C"

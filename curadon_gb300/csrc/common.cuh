@@ -1,0 +1,131 @@
+// common.cuh -- error reporting, plan structures and small device helpers
+// shared by the sm_103a projection kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "curadon_gb300.h"
+
+namespace cg {
+
+// ------------------------------------------------------------ error state
+
+// Records `msg` as this thread's last error and returns `code`.
+int set_error(int code, const std::string &msg);
+void clear_error();
+
+#define CG_TRY_CUDA(expr)                                                                     \
+    do {                                                                                      \
+        cudaError_t cg_err_ = (expr);                                                         \
+        if (cg_err_ != cudaSuccess) {                                                         \
+            return ::cg::set_error(cg_err_ == cudaErrorMemoryAllocation ? CG_ERR_NOMEM        \
+                                                                        : CG_ERR_CUDA,        \
+                                   std::string(#expr) + ": " + cudaGetErrorName(cg_err_) +    \
+                                       " (" + cudaGetErrorString(cg_err_) + ")");             \
+        }                                                                                     \
+    } while (0)
+
+#define CG_REQUIRE(cond, msg)                                                                 \
+    do {                                                                                      \
+        if (!(cond)) return ::cg::set_error(CG_ERR_INVALID, (msg));                           \
+    } while (0)
+
+// Runs `expr` on the plan's device and restores the caller's device after.
+class DeviceGuard {
+  public:
+    explicit DeviceGuard(int device) {
+        cudaGetDevice(&prev_);
+        if (prev_ != device) {
+            ok_ = cudaSetDevice(device) == cudaSuccess;
+            switched_ = true;
+        }
+    }
+    ~DeviceGuard() {
+        if (switched_) cudaSetDevice(prev_);
+    }
+    bool ok() const { return ok_; }
+
+  private:
+    int prev_ = 0;
+    bool switched_ = false;
+    bool ok_ = true;
+};
+
+// Padding, in texels, around the pair-packed copies of volumes and
+// sinograms.  Sample coordinates are clamped into the padded range, whose
+// outer texels are zero, which reproduces the texture unit's border mode.
+constexpr int kPad = 2;
+
+// ------------------------------------------------------------ plan types
+
+struct Plan2d {
+    int device = 0;
+    int W = 0, H = 0;                 // internal x (contiguous), y
+    float sx = 1, sy = 1, ox = 0, oy = 0;
+    int det = 0;
+    float ds = 1, doff = 0;
+    int nangles = 0;
+    float pitch = 0, COR = 0;
+    int fwd_bx = 32, fwd_by = 8;
+
+    // per-view tables (device)
+    float *d_angles = nullptr, *d_DSO = nullptr, *d_DSD = nullptr;
+    float2 *d_src = nullptr, *d_u0 = nullptr, *d_du = nullptr;
+    float4 *d_bmeta = nullptr;        // (-sin, cos, DSD, DSO)
+
+    // scratch (device)
+    float2 *d_layA = nullptr;         // (H+2P) x (W+2P) pairs along x
+    float2 *d_layB = nullptr;         // (W+2P) x (H+2P) pairs along y
+    float2 *d_sinoP = nullptr;        // nangles x (det+2P) pairs along u
+
+    int pitchA() const { return W + 2 * kPad; }
+    int pitchB() const { return H + 2 * kPad; }
+    int pitchS() const { return det + 2 * kPad; }
+};
+
+struct Plan3d {
+    int device = 0;
+    int X = 0, Y = 0, Z = 0;          // internal volume extents (x fastest)
+    int U = 0, V = 0;                 // detector cells (u fastest)
+    int nangles = 0;
+    float DSO = 0, DSD = 0;
+
+    // forward tables: detector origin, u step, v step, source (voxel units)
+    float4 *d_forg = nullptr, *d_fdu = nullptr, *d_fdv = nullptr, *d_fsrc = nullptr;
+    // backward tables: voxel (0,0,0) origin, x/y/z steps (world units)
+    float4 *d_borg = nullptr, *d_bdx = nullptr, *d_bdy = nullptr, *d_bdz = nullptr;
+    float bsrc[3] = {0, 0, 0};        // backward source (same for all views)
+
+    // scratch (device), allocated on first use
+    float2 *d_volA = nullptr;         // (Z+2P)(Y+2P)(X+2P) pairs along x
+    float2 *d_volB = nullptr;         // (X+2P)(Y+2P)(Z+2P) pairs along z
+    float2 *d_sinoP = nullptr;        // nangles (V+2P)(U+2P) pairs along u
+    size_t volA_elems = 0, volB_elems = 0, sinoP_elems = 0;
+};
+
+void free_plan2d(Plan2d *p);
+void free_plan3d(Plan3d *p);
+
+// ------------------------------------------------------------ kernels
+
+int launch_plan2d_tables(Plan2d &p, cudaStream_t s);
+int launch_relayout2d(const Plan2d &p, const float *vol, cudaStream_t s);
+int launch_forward2d(const Plan2d &p, float *sino, cudaStream_t s);
+int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s);
+int launch_backward2d(const Plan2d &p, float *vol, cudaStream_t s);
+
+int ensure_plan3d_scratch(Plan3d &p, bool fwd, bool bwd);
+int launch_forward3d(const Plan3d &p, const float *vol, float *sino, cudaStream_t s);
+int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s);
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace cg
+
+// C-ABI handles are the plan structures themselves.
+struct cg_plan2d : cg::Plan2d {};
+struct cg_plan3d : cg::Plan3d {};

@@ -1,0 +1,291 @@
+// proj2d.cu -- 2D fan-beam projection kernels for sm_103a.
+//
+// Data layout in HBM (all float32, per plan):
+//   layA  (H+2P) rows x (W+2P) float2: layA[y][x] = (v[y][x], v[y][x+1])
+//   layB  (W+2P) rows x (H+2P) float2: layB[x][y] = (v[y][x], v[y+1][x])
+//   sinoP nangles rows x (det+2P) float2: sinoP[a][k] = (s[a][k], s[a][k+1])
+// with P = kPad texels of zeros around every edge.  One 8-byte load then
+// returns both texels a linear filter needs along the contiguous axis, and a
+// warp of adjacent detector cells (forward) or adjacent pixels (backward)
+// reads consecutive addresses whatever the view angle: rays that advance
+// along y read layA, rays that advance along x read the transposed layB.
+// Interpolation is FP32 in registers (no texture unit); clamping a texel
+// index into the zero padding reproduces cudaAddressModeBorder.
+#include <cfloat>
+
+#include "common.cuh"
+
+namespace cg {
+namespace {
+
+// ------------------------------------------------------------ plan tables
+
+// Clockwise rotation of v by (cs, sn) about the origin, minus t; the same
+// expression as the reference's geometry::rotate (rotation.hpp:51-61) so that
+// the compiler forms the same products and roundings.
+__device__ __forceinline__ float2 rotate_minus(float2 v, float cs, float sn, float2 t) {
+    return make_float2(v.x * cs + v.y * sn - t.x, -v.x * sn + v.y * cs - t.y);
+}
+
+// Per-view tables in voxel-index units, evaluated in FP32 with __cosf/__sinf
+// in the order plan_2d::precompute uses (plan_2d.hpp:189-241, functors
+// :17-80): the per-cell step is the difference of two rotated detector cells,
+// so its rounding is amplified by the cell index and must match the
+// reference's exactly for drop-in results at large detectors.
+__global__ void k_plan2d_tables(int n, const float *__restrict__ ang,
+                                const float *__restrict__ DSO, const float *__restrict__ DSD,
+                                float det_ext, float ds, float doff, float sx, float sy,
+                                float ox, float oy, float extx, float exty, float2 *src,
+                                float2 *u0, float2 *du, float4 *bmeta) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float a = ang[i], dso = DSO[i], dsd = DSD[i];
+    const float dod = dsd - dso;
+    const float2 cell0 = make_float2(-det_ext / 2.f + ds * .5f, -dod);
+    const float2 cell1 = make_float2(-det_ext / 2.f + ds * 1.5f, -dod);
+    const float cs = __cosf(a), sn = __sinf(a);
+    const float2 s = rotate_minus(make_float2(doff, dso), cs, sn, make_float2(0.f, 0.f));
+    float2 o = rotate_minus(cell0, cs, sn, s);
+    o = make_float2(o.x / sx, o.y / sy);
+    float2 d = rotate_minus(cell1, cs, sn, s);
+    d = make_float2(d.x / sx, d.y / sy);
+    d = make_float2(d.x - o.x, d.y - o.y);
+    const float2 ext = make_float2(0.5f * extx, 0.5f * exty);
+    src[i] = make_float2((s.x - ox + ext.x) / sx, (s.y - oy + ext.y) / sy);
+    u0[i] = o;
+    du[i] = d;
+    // (-sin, cos, DSD, DSO) as the backprojector's shared table
+    // (backward_2d.hpp:45-55), with the same intrinsics.
+    bmeta[i] = make_float4(-__sinf(a), __cosf(a), dsd, dso);
+}
+
+// ------------------------------------------------------------ re-layouts
+
+constexpr int kTile = 32;
+
+// Writes layA and layB for one 32 x 32 tile of padded texel space.
+__global__ void __launch_bounds__(256)
+    k_relayout2d(const float *__restrict__ vol, int W, int H, float2 *__restrict__ A,
+                 float2 *__restrict__ B) {
+    __shared__ float tile[kTile + 1][kTile + 1];
+    const int x0 = blockIdx.x * kTile - kPad, y0 = blockIdx.y * kTile - kPad;
+    for (int j = threadIdx.y; j < kTile + 1; j += blockDim.y)
+        for (int i = threadIdx.x; i < kTile + 1; i += blockDim.x) {
+            const int x = x0 + i, y = y0 + j;
+            tile[j][i] = (x >= 0 && x < W && y >= 0 && y < H) ? vol[(size_t)y * W + x] : 0.f;
+        }
+    __syncthreads();
+    const int pa = W + 2 * kPad, pb = H + 2 * kPad;
+    const int tx = threadIdx.x;
+    for (int j = threadIdx.y; j < kTile; j += blockDim.y) {
+        const int y = y0 + j, x = x0 + tx;
+        if (y < H + kPad && x < W + kPad)
+            A[(size_t)(y + kPad) * pa + (x + kPad)] = make_float2(tile[j][tx], tile[j][tx + 1]);
+    }
+    for (int i = threadIdx.y; i < kTile; i += blockDim.y) {
+        const int x = x0 + i, y = y0 + tx;
+        if (x < W + kPad && y < H + kPad)
+            B[(size_t)(x + kPad) * pb + (y + kPad)] = make_float2(tile[tx][i], tile[tx + 1][i]);
+    }
+}
+
+__global__ void k_relayout_sino2d(const float *__restrict__ sino, int det, int nangles,
+                                  float2 *__restrict__ S) {
+    const int pitch = det + 2 * kPad;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)pitch * nangles) return;
+    const int a = (int)(idx / pitch);
+    const int k = (int)(idx % pitch) - kPad;
+    const float *row = sino + (size_t)a * det;
+    const float t0 = (k >= 0 && k < det) ? row[k] : 0.f;
+    const float t1 = (k + 1 >= 0 && k + 1 < det) ? row[k + 1] : 0.f;
+    S[idx] = make_float2(t0, t1);
+}
+
+// ------------------------------------------------------------ forward
+
+// One thread per ray (detector cell u, view): the reference's ray set-up
+// (forward_2d.hpp:52-68, intersection.h:31-46) in the same FP32 operations,
+// then rint(max|rd|) unit steps along the dominant axis.  Along that axis the
+// step is exactly +-1, so the row index advances by one and the vertical
+// filter weight stays fixed; the two row sums are blended once at the end.
+__global__ void __launch_bounds__(256)
+    k_fwd2d(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
+            float *__restrict__ sino, const float2 *__restrict__ tsrc,
+            const float2 *__restrict__ tu0, const float2 *__restrict__ tdu, int W, int H,
+            int det, int nangles, float sx, float sy) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    const int view = blockIdx.y * blockDim.y + threadIdx.y;
+    if (u >= det || view >= nangles) return;
+    const float2 s = tsrc[view], o = tu0[view], du = tdu[view];
+    const float fu = (float)u;
+    const float dx = fmaf(du.x, fu, o.x);
+    const float dy = fmaf(du.y, fu, o.y);
+
+    float tmin = FLT_MIN, tmax = FLT_MAX;
+    {
+        const float t1 = __fdividef(-1.f - s.x, dx), t2 = __fdividef((float)W - s.x, dx);
+        tmin = fminf(fmaxf(t1, tmin), fmaxf(t2, tmin));
+        tmax = fmaxf(fminf(t1, tmax), fminf(t2, tmax));
+    }
+    {
+        const float t1 = __fdividef(-1.f - s.y, dy), t2 = __fdividef((float)H - s.y, dy);
+        tmin = fminf(fmaxf(t1, tmin), fmaxf(t2, tmin));
+        tmax = fmaxf(fminf(t1, tmax), fminf(t2, tmax));
+    }
+    float *out = sino + (size_t)view * det + u;
+    if ((double)tmin > (double)tmax - 1e-6) {
+        *out = 0.f;
+        return;
+    }
+    const float rox = fmaf(dx, tmin, s.x), roy = fmaf(dy, tmin, s.y);
+    const float tl = tmax - tmin;
+    const float rdx = dx * tl, rdy = dy * tl;
+    const float m = fmaxf(fabsf(rdx), fabsf(rdy));
+    int n = __float2int_rn(m);
+    const float vx = rdx / m, vy = rdy / m;
+
+    const bool ymajor = fabsf(rdy) >= fabsf(rdx);
+    float p = (ymajor ? rox : roy) - 0.5f;
+    const float vp = ymajor ? vx : vy;
+    const float q = (ymajor ? roy : rox) - 0.5f;
+    const int sq = ((ymajor ? vy : vx) > 0.f) ? 1 : -1;
+    const float2 *lay = ymajor ? layA : layB;
+    const int pitch = (ymajor ? W : H) + 2 * kPad;
+    const float pmax = (float)(ymajor ? W : H);
+    const int qmax = ymajor ? H : W;
+
+    const float qf = floorf(q);
+    const float fq = q - qf;
+    const int iq = (int)fminf(fmaxf(qf, -(float)kPad), (float)qmax);
+    n = min(n, sq > 0 ? qmax - iq + 1 : iq + kPad + 1);
+    const float2 *row = lay + (size_t)(iq + kPad) * pitch + kPad;
+    const long long rstep = (long long)sq * pitch;
+
+    float acc_lo = 0.f, acc_hi = 0.f;
+#pragma unroll 4
+    for (int j = 0; j < n; ++j) {
+        const float pf = fminf(fmaxf(floorf(p), -(float)kPad), pmax);
+        const float fp = p - pf;
+        const int ip = (int)pf;
+        const float2 lo = __ldg(row + ip);
+        const float2 hi = __ldg(row + pitch + ip);
+        acc_lo += fmaf(fp, lo.y - lo.x, lo.x);
+        acc_hi += fmaf(fp, hi.y - hi.x, hi.x);
+        p += vp;
+        row += rstep;
+    }
+    const float acc = fmaf(fq, acc_hi - acc_lo, acc_lo);
+    *out = acc * hypotf(vx * sx, vy * sy);
+}
+
+// ------------------------------------------------------------ backward
+
+constexpr int kBwdRows = 4;        // pixels per thread, 8 rows apart
+constexpr int kBwdViews = 256;     // per-view table entries staged per pass
+
+// One thread per 4 pixels of a column; a 32 x 32 pixel tile per block.  Per
+// view: x' = -s X - c Y, w = DSD / (x' + DSO), u = w (c X - s Y) / ds + det/2
+// in the reference's FP32 operations (backward_2d.hpp:61-96), a linear
+// sample of the pair-packed sinogram row, acc += sample * w; finally the
+// volume gets acc / ds added (:99).
+__global__ void __launch_bounds__(256)
+    k_bwd2d(float *__restrict__ vol, const float2 *__restrict__ S,
+            const float4 *__restrict__ meta, int W, int H, int det, int nangles, float sx,
+            float sy, float ox, float oy, float ds) {
+    __shared__ float4 smeta[kBwdViews];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    const int y0 = blockIdx.y * 32 + threadIdx.y;
+    const float ex = (float)W / 2.0f, ey = (float)H / 2.0f, ed = (float)det / 2.0f;
+    const float inv = __fdividef(1.0f, ds);
+    const float X = ((float)x - ex) * sx + ox + 0.5f;
+    const float SX = X * inv;
+    float Y[kBwdRows], SY[kBwdRows], acc[kBwdRows];
+#pragma unroll
+    for (int r = 0; r < kBwdRows; ++r) {
+        Y[r] = ((float)(y0 + 8 * r) - ey) * sy + oy + 0.5f;
+        SY[r] = Y[r] * inv;
+        acc[r] = 0.f;
+    }
+    const int pitch = det + 2 * kPad;
+    const float kmax = (float)det;
+    for (int v0 = 0; v0 < nangles; v0 += kBwdViews) {
+        const int nv = min(kBwdViews, nangles - v0);
+        __syncthreads();
+        for (int i = tid; i < nv; i += 256) smeta[i] = meta[v0 + i];
+        __syncthreads();
+        const float2 *rowbase = S + (size_t)v0 * pitch + kPad;
+#pragma unroll 2
+        for (int j = 0; j < nv; ++j) {
+            const float4 m = smeta[j];  // (-sin, cos, DSD, DSO)
+            const float2 *row = rowbase + (size_t)j * pitch;
+#pragma unroll
+            for (int r = 0; r < kBwdRows; ++r) {
+                const float xi = m.x * X - m.y * Y[r];
+                const float yi = m.y * SX + m.x * SY[r];
+                const float w = __fdividef(m.z, xi + m.w);
+                const float ub = (w * yi + ed) - 0.5f;
+                const float kf = fminf(fmaxf(floorf(ub), -(float)kPad), kmax);
+                const float a = ub - kf;
+                const float2 t = __ldg(row + (int)kf);
+                acc[r] = fmaf(fmaf(a, t.y - t.x, t.x), w, acc[r]);
+            }
+        }
+    }
+    if (x < W) {
+#pragma unroll
+        for (int r = 0; r < kBwdRows; ++r) {
+            const int y = y0 + 8 * r;
+            if (y < H) vol[(size_t)y * W + x] += acc[r] * inv;
+        }
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ launchers
+
+int launch_plan2d_tables(Plan2d &p, cudaStream_t s) {
+    const float det_ext = (float)p.det * p.ds;
+    const float extx = (float)p.W * p.sx, exty = (float)p.H * p.sy;
+    k_plan2d_tables<<<ceil_div(p.nangles, 128), 128, 0, s>>>(
+        p.nangles, p.d_angles, p.d_DSO, p.d_DSD, det_ext, p.ds, p.doff, p.sx, p.sy, p.ox, p.oy,
+        extx, exty, p.d_src, p.d_u0, p.d_du, p.d_bmeta);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
+int launch_relayout2d(const Plan2d &p, const float *vol, cudaStream_t s) {
+    dim3 grid(ceil_div(p.W + 2 * kPad, kTile), ceil_div(p.H + 2 * kPad, kTile));
+    k_relayout2d<<<grid, dim3(32, 8), 0, s>>>(vol, p.W, p.H, p.d_layA, p.d_layB);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
+int launch_forward2d(const Plan2d &p, float *sino, cudaStream_t s) {
+    dim3 block(p.fwd_bx, p.fwd_by);
+    dim3 grid(ceil_div(p.det, p.fwd_bx), ceil_div(p.nangles, p.fwd_by));
+    if (grid.y > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
+    k_fwd2d<<<grid, block, 0, s>>>(p.d_layA, p.d_layB, sino, p.d_src, p.d_u0, p.d_du, p.W, p.H,
+                                   p.det, p.nangles, p.sx, p.sy);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
+int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s) {
+    const long long n = (long long)p.pitchS() * p.nangles;
+    k_relayout_sino2d<<<ceil_div(n, 256), 256, 0, s>>>(sino, p.det, p.nangles, p.d_sinoP);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
+int launch_backward2d(const Plan2d &p, float *vol, cudaStream_t s) {
+    dim3 grid(ceil_div(p.W, 32), ceil_div(p.H, 32));
+    k_bwd2d<<<grid, dim3(32, 8), 0, s>>>(vol, p.d_sinoP, p.d_bmeta, p.W, p.H, p.det, p.nangles,
+                                         p.sx, p.sy, p.ox, p.oy, p.ds);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
+}  // namespace cg

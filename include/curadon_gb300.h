@@ -1,0 +1,143 @@
+/*
+ * curadon_gb300.h -- C ABI of the GB300 (sm_103a) projection operators.
+ *
+ * Drop-in boundary for curadon's native extension `curadon_ext`
+ * (python/standalone/src/bind.cpp:58-66 of the reference).  Every entry point
+ * below replaces one function of that extension and keeps its argument
+ * meaning; reference locations are given beside each declaration.
+ *
+ * Conventions
+ *  - All data pointers are CUDA device pointers to C-contiguous float32
+ *    arrays; geometry arrays are host pointers.
+ *  - Python axis order is used for shapes, as in the reference's bindings:
+ *      2D volume (H, W), 2D sinogram (nangles, det_count);
+ *      3D volume (Z, Y, X), 3D sinogram (nangles, V, U).
+ *  - Work is enqueued on `stream` (a cudaStream_t, NULL = legacy default
+ *    stream) and is asynchronous; nothing synchronises the host.
+ *  - Every function returns CG_OK or an error code; the message of the last
+ *    error on the calling thread is returned by cg_last_error().  No function
+ *    aborts the process (the reference's gpuErrchk exits; error.h:6-18).
+ *  - Forward projections overwrite the sinogram (2D: every ray; 3D: every ray
+ *    that hits the volume's bounding box, as forward_3d.hpp:74-76 skips the
+ *    others).  Backprojections ADD into the volume, as the reference does
+ *    (backward_2d.hpp:99, backward_3d.hpp:115-121).
+ *  - Plans are immutable after creation except for the forward block shape;
+ *    one plan may be used from several threads on different streams, but two
+ *    calls on the same plan must not overlap on the GPU (they share scratch).
+ */
+#ifndef CURADON_GB300_H
+#define CURADON_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CG_OK 0
+#define CG_ERR_INVALID 1     /* bad argument: null pointer, shape, size      */
+#define CG_ERR_CUDA 2        /* a CUDA runtime call or launch failed         */
+#define CG_ERR_NOMEM 3       /* device allocation failed                     */
+#define CG_ERR_UNSUPPORTED 4 /* valid in the reference, not built here (f16) */
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *cg_last_error(void);
+
+/* ABI version: major * 10000 + minor * 100 + patch. */
+int cg_version(void);
+
+/* ------------------------------------------------------------------ 2D -- */
+
+typedef struct cg_plan2d cg_plan2d;
+
+/* Fan-beam plan.  Replaces `plan_2d.__init__` (plan.cu:20-59) and the
+ * plan_2d constructor (plan_2d.hpp:103-126): per-view source, detector origin
+ * and detector step are precomputed on the device exactly as
+ * plan_2d::precompute does (plan_2d.hpp:189-241), and the scratch the
+ * operators need is allocated here, once.  vol_prec / det_prec are bit widths
+ * (32; 16 is valid in the reference and returns CG_ERR_UNSUPPORTED here).
+ * vol_shape / vol_spacing / vol_offset are in Python order (y, x).
+ * det_pitch and COR are accepted and, as in the reference, unused. */
+int cg_plan2d_create(cg_plan2d **plan, int device, uint32_t vol_prec,
+                     const uint64_t vol_shape[2], const float vol_spacing[2],
+                     const float vol_offset[2], uint32_t det_prec, uint64_t det_count,
+                     float det_spacing, float det_offset, const float *DSO, const float *DSD,
+                     const float *angles, uint64_t nangles, float det_pitch, float COR);
+
+/* Frees the plan and its device memory (plan_2d destructor). */
+int cg_plan2d_destroy(cg_plan2d *plan);
+
+/* The reference's read-write `forward_block_x` / `forward_block_y`
+ * (plan.cu:57-58, plan_2d.hpp:184-186): here they set the detector-cells x
+ * views shape of one forward thread block (product 32..1024, x multiple of 32). */
+int cg_plan2d_get_forward_block(const cg_plan2d *plan, uint64_t *bx, uint64_t *by);
+int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by);
+
+/* Copies the plan's per-view tables to host arrays of 2 * nangles floats each
+ * (x, y interleaved): source position, direction to detector cell 0 and
+ * per-cell step, in voxel-index units (plan_2d::sources/u_origins/delta_us,
+ * plan_2d.hpp:174-182).  Any pointer may be NULL. */
+int cg_plan2d_tables(const cg_plan2d *plan, float *sources, float *u_origins, float *delta_us);
+
+/* 2D ray-driven forward projection.  Replaces `forward_2d(volume, sinogram,
+ * plan)` (forward.cu:92-139 -> fp::forward_2d, forward_2d.hpp:135-139). */
+int cg_forward_2d(cg_plan2d *plan, const float *volume, float *sinogram, void *stream);
+
+/* 2D voxel-driven backprojection, accumulating into `volume`.  Replaces
+ * `backward_2d(volume, sinogram, plan)` (backward.cu:233-280 ->
+ * bp::backproject_2d, backward_2d.hpp:302-306). */
+int cg_backward_2d(cg_plan2d *plan, float *volume, const float *sinogram, void *stream);
+
+/* ------------------------------------------------------------------ 3D -- */
+
+typedef struct cg_plan3d cg_plan3d;
+
+/* Cone-beam plan: the argument list of the reference's per-call
+ * `forward_3d` / `backward_3d` (forward.cu:23-38, backward.cu:20-35), held
+ * once so the per-view geometry (forward_3d.hpp:97-211,
+ * backward_3d.hpp:110-178) is computed and uploaded once.
+ *   vol_shape/vol_spacing/vol_offset: Python order (z, y, x)
+ *   phi/theta/psi: per-view Euler angles, `nangles` each.  `phi` is the
+ *     array the reference receives in its 6th position (curadon.forward
+ *     passes geom.angles[0]) and uses as phi (forward.cu:60-66).
+ *   det_shape/det_spacing/det_offset: Python order (v, u)
+ *   det_rotation: (pitch, roll, yaw) */
+int cg_plan3d_create(cg_plan3d **plan, int device, const uint64_t vol_shape[3],
+                     const float vol_spacing[3], const float vol_offset[3], const float *phi,
+                     const float *theta, const float *psi, uint64_t nangles,
+                     const uint64_t det_shape[2], const float det_spacing[2],
+                     const float det_offset[2], const float det_rotation[3], float DSO, float DSD,
+                     float COR);
+int cg_plan3d_destroy(cg_plan3d *plan);
+
+/* 3D ray-driven forward projection with a plan (fp::forward_3d,
+ * forward_3d.hpp:214-274). */
+int cg_forward_3d_plan(cg_plan3d *plan, const float *volume, float *sinogram, void *stream);
+
+/* 3D voxel-driven backprojection with a plan, accumulating
+ * (bp::backproject_3d, backward_3d.hpp:457-529). */
+int cg_backward_3d_plan(cg_plan3d *plan, float *volume, const float *sinogram, void *stream);
+
+/* Per-call forms with the reference's exact argument list: they build a
+ * transient plan (as the reference allocates its texture array per call),
+ * run, and release it once the stream has finished with it.
+ * Replace `forward_3d(...)` (forward.cu:23-75) and `backward_3d(...)`
+ * (backward.cu:20-72). */
+int cg_forward_3d(const float *x, const uint64_t vol_shape[3], const float vol_spacing[3],
+                  const float vol_offset[3], float *sinogram, const float *phi,
+                  const float *theta, const float *psi, uint64_t nangles,
+                  const uint64_t det_shape[2], const float det_spacing[2],
+                  const float det_offset[2], const float det_rotation[3], float DSO, float DSD,
+                  float COR, void *stream);
+int cg_backward_3d(float *x, const uint64_t vol_shape[3], const float vol_spacing[3],
+                   const float vol_offset[3], const float *sinogram, const float *phi,
+                   const float *theta, const float *psi, uint64_t nangles,
+                   const uint64_t det_shape[2], const float det_spacing[2],
+                   const float det_offset[2], const float det_rotation[3], float DSO, float DSD,
+                   float COR, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CURADON_GB300_H */

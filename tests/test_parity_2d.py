@@ -1,0 +1,194 @@
+"""GPU parity of the 2D fan-beam operators (through the C ABI).
+
+Tolerance: relative L2 <= 1e-3 against the reference's own operators and
+against the FP64 oracle (the bar of the drop-in contract); max abs error is
+printed.  The per-view geometry tables must equal the reference's bit for
+bit, because their rounding is amplified by the detector index."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from conftest import load_golden, max_abs, rel_l2
+from curadon_gb300 import FanGeometry, backward, backward_2d, forward, forward_2d, plan_2d
+from curadon_gb300.phantom import ellipses_2d, fan_config
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-3
+
+
+def make(g, dev):
+    kw = {k: g[k] for k in ("DSD", "DSO", "angles", "vol_shape", "det_shape")}
+    for k in ("det_spacing", "det_offset", "vol_spacing", "vol_offset"):
+        if k in g:
+            kw[k] = g[k]
+    return FanGeometry(**kw, device=dev.index or 0)
+
+
+def run_fwd(geom, vol, dev):
+    v = torch.as_tensor(vol, device=dev).contiguous()
+    s = torch.full(geom.sinogram_shape(), 123.0, device=dev)
+    forward(v, s, geom)
+    torch.cuda.synchronize()
+    return s.cpu().numpy()
+
+
+def run_bwd(geom, sino, dev, vol0=None):
+    s = torch.as_tensor(sino, device=dev, dtype=torch.float32).contiguous()
+    v = (torch.zeros(tuple(geom.vol_shape), device=dev) if vol0 is None
+         else torch.as_tensor(vol0, device=dev, dtype=torch.float32).clone())
+    backward(s, v, geom)
+    torch.cuda.synchronize()
+    return v.cpu().numpy()
+
+
+@pytest.mark.parametrize("case", ["fan_cfg0", "fan_var"])
+def test_against_golden(cuda_device, case):
+    z, g = load_golden(case)
+    geom = make(g, cuda_device)
+    src, u0, du = geom.plan.tables()
+    assert np.array_equal(src, z["sources"]) and np.array_equal(u0, z["u_origins"])
+    assert np.array_equal(du, z["delta_us"]), max_abs(du, z["delta_us"])
+    s = run_fwd(geom, z["volume"], cuda_device)
+    e = rel_l2(s, z["sino_ref"])
+    print(f"{case} fwd rel-L2 {e:.2e} max-abs {max_abs(s, z['sino_ref']):.2e}")
+    assert e < TOL
+    b = run_bwd(geom, z["sino_ref"], cuda_device)
+    e = rel_l2(b, z["bwd_ref"])
+    print(f"{case} bwd rel-L2 {e:.2e} max-abs {max_abs(b, z['bwd_ref']):.2e}")
+    assert e < TOL
+
+
+@pytest.mark.parametrize("n,nangles", [(64, 360), (96, 50), (128, 128), (200, 1500)])
+def test_against_oracle(cuda_device, n, nangles):
+    g = fan_config(n, nangles)
+    geom = make(g, cuda_device)
+    ph = ellipses_2d(n, n).numpy()
+    s = run_fwd(geom, ph, cuda_device)
+    so = oracle.fwd2d(g, ph)
+    assert rel_l2(s, so) < TOL, rel_l2(s, so)
+    b = run_bwd(geom, so.astype(np.float32), cuda_device)
+    bo = oracle.bwd2d(g, so.astype(np.float32))
+    assert rel_l2(b, bo) < TOL, rel_l2(b, bo)
+
+
+@pytest.mark.parametrize("n", [256, 512, 1024, 2048])
+def test_against_reference_sweep(cuda_device, ref_ops, n):
+    """The n-sweep workload at full size against the reference's kernels."""
+    g = fan_config(n)
+    geom = make(g, cuda_device)
+    h, nv = ref_ops.plan2d(g)
+    try:
+        rs, ru, rd = ref_ops.plan2d_tables(h, nv)
+        src, u0, du = geom.plan.tables()
+        assert np.array_equal(src, rs) and np.array_equal(u0, ru) and np.array_equal(du, rd)
+        v = ellipses_2d(n, n, device=cuda_device).contiguous()
+        s_ref = torch.zeros(geom.sinogram_shape(), device=cuda_device)
+        ref_ops.forward2d(h, v.data_ptr(), s_ref.data_ptr())
+        ref_ops.sync()
+        s = torch.zeros_like(s_ref)
+        forward(v, s, geom)
+        torch.cuda.synchronize()
+        e = rel_l2(s.cpu(), s_ref.cpu())
+        print(f"n={n} fwd rel-L2 {e:.2e} max-abs {max_abs(s.cpu(), s_ref.cpu()):.2e}")
+        assert e < TOL
+        if nv <= 1024:  # the reference's multi-chunk backprojection races (see DESIGN)
+            b_ref = torch.zeros_like(v)
+            ref_ops.backward2d(h, b_ref.data_ptr(), s_ref.data_ptr())
+            ref_ops.sync()
+            b = torch.zeros_like(v)
+            backward(s_ref, b, geom)
+            torch.cuda.synchronize()
+            e = rel_l2(b.cpu(), b_ref.cpu())
+            print(f"n={n} bwd rel-L2 {e:.2e} max-abs {max_abs(b.cpu(), b_ref.cpu()):.2e}")
+            assert e < TOL
+    finally:
+        ref_ops.destroy2d(h)
+
+
+def test_edge_geometries(cuda_device):
+    cases = [
+        dict(fan_config(1, 3, 1, 1.0, 10.0, 20.0)),                       # 1x1 image, 1 cell
+        dict(fan_config(17, 1, 5, 0.5, 40.0, 60.0)),                      # one view, odd sizes
+        dict(fan_config(33, 7, 64, 2.0, 60.0, 100.0), vol_shape=(33, 45),
+             vol_spacing=(0.7, 1.3), vol_offset=(-4.0, 2.5), det_offset=3.0),
+        dict(fan_config(40, 9, 30, 1.0, 500.0, 700.0), vol_offset=(1000.0, 0.0)),  # all miss
+    ]
+    for g in cases:
+        geom = make(g, cuda_device)
+        H, W = g["vol_shape"]
+        ph = np.random.default_rng(H * W).uniform(0, 1, (H, W)).astype(np.float32)
+        s = run_fwd(geom, ph, cuda_device)
+        so = oracle.fwd2d(g, ph)
+        if np.linalg.norm(so) == 0:
+            assert np.all(s == 0)
+        else:
+            assert rel_l2(s, so) < TOL, (g["vol_shape"], rel_l2(s, so))
+        b = run_bwd(geom, so.astype(np.float32), cuda_device)
+        bo = oracle.bwd2d(g, so.astype(np.float32))
+        assert rel_l2(b, bo) < TOL or np.linalg.norm(bo) == 0
+
+
+def test_backward_accumulates_and_is_linear(cuda_device):
+    g = fan_config(128, 96)
+    geom = make(g, cuda_device)
+    rng = np.random.default_rng(0)
+    s1 = rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32)
+    s2 = rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32)
+    v0 = rng.uniform(0, 1, (128, 128)).astype(np.float32)
+    b1, b2 = run_bwd(geom, s1, cuda_device), run_bwd(geom, s2, cuda_device)
+    b12 = run_bwd(geom, 2 * s1 + 3 * s2, cuda_device)
+    assert rel_l2(b12, 2 * b1 + 3 * b2) < 1e-5
+    bacc = run_bwd(geom, s1, cuda_device, vol0=v0)
+    assert rel_l2(bacc, b1 + v0) < 1e-6
+
+
+def test_forward_linear_and_deterministic(cuda_device):
+    g = fan_config(256)
+    geom = make(g, cuda_device)
+    x = ellipses_2d(256, 1).numpy()
+    y = ellipses_2d(256, 2).numpy()
+    a, b = run_fwd(geom, x, cuda_device), run_fwd(geom, y, cuda_device)
+    assert rel_l2(run_fwd(geom, 2 * x - y, cuda_device), 2 * a - b) < 1e-5
+    assert np.array_equal(a, run_fwd(geom, x, cuda_device))
+
+
+def test_native_api_and_errors(cuda_device):
+    g = fan_config(32, 8)
+    plan = plan_2d(0, 32, (32, 32), (1.0, 1.0), (0.0, 0.0), 32, g["det_shape"], 1.5, 0.0,
+                   g["DSO"], g["DSD"], g["angles"], 0.0, 0.0)
+    v = torch.rand(32, 32, device=cuda_device)
+    s = torch.zeros(8, g["det_shape"], device=cuda_device)
+    forward_2d(v, s, plan)
+    backward_2d(v, s, plan)
+    plan.forward_block_x, plan.forward_block_y = 64, 2
+    assert (plan.forward_block_x, plan.forward_block_y) == (64, 2)
+    forward_2d(v, s, plan)
+    with pytest.raises(TypeError):
+        forward_2d(v.double(), s, plan)
+    with pytest.raises(TypeError):
+        forward_2d(v.cpu(), s, plan)
+    with pytest.raises(ValueError):
+        forward_2d(v[:16].contiguous(), s, plan)
+    with pytest.raises(TypeError):
+        forward_2d(v.t(), s, plan)
+    with pytest.raises(AttributeError):
+        plan_2d(0, 8, (32, 32), (1.0, 1.0), (0.0, 0.0), 32, 10, 1.5, 0.0, [1.0], [2.0], [0.0])
+    with pytest.raises(ValueError):
+        plan.forward_block_x = 48
+
+
+def test_runs_on_the_current_stream(cuda_device):
+    g = fan_config(256)
+    geom = make(g, cuda_device)
+    x = ellipses_2d(256, 4, device=cuda_device)
+    expect = torch.zeros(geom.sinogram_shape(), device=cuda_device)
+    forward(x, expect, geom)
+    st = torch.cuda.Stream()
+    with torch.cuda.stream(st):
+        y = x * 1.0
+        s = torch.zeros_like(expect)
+        forward(y, s, geom)
+        r = s.sum()
+    st.synchronize()
+    assert torch.equal(s, expect) and float(r) == pytest.approx(float(expect.sum()), rel=1e-6)
