@@ -9,12 +9,13 @@ hand-written CUDA kernels behind the C ABI of ``include/curadon_gb300.h``;
 there is no CPU fallback.
 """
 from . import backend
-from .backend import backward_2d, backward_3d, forward_2d, forward_3d, plan_2d, plan_3d
+from .backend import (adjoint_2d, backward_2d, backward_3d, forward_2d, forward_3d, plan_2d,
+                      plan_3d)
 from .geometry import ConeGeometry, FanGeometry, geom_to_str
-from .ops import TorchBackprojection, TorchForward, backward, forward
+from .ops import TorchBackprojection, TorchForward, adjoint, backward, forward
 
 __all__ = [
-    "FanGeometry", "ConeGeometry", "geom_to_str", "forward", "backward", "TorchForward",
+    "FanGeometry", "ConeGeometry", "geom_to_str", "forward", "backward", "adjoint", "TorchForward",
     "TorchBackprojection", "plan_2d", "plan_3d", "forward_2d", "backward_2d", "forward_3d",
     "backward_3d", "backend",
 ]

@@ -27,12 +27,14 @@ SIGNATURES = [
     ("cg_plan2d_tables", C.c_int, [C.c_void_p, f32p, f32p, f32p]),
     ("cg_forward_2d", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cg_backward_2d", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("cg_adjoint_2d", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cg_plan3d_create", C.c_int,
      [C.POINTER(C.c_void_p), C.c_int, u64p, f32p, f32p, f32p, f32p, f32p, C.c_uint64, u64p, f32p,
       f32p, f32p, C.c_float, C.c_float, C.c_float]),
     ("cg_plan3d_destroy", C.c_int, [C.c_void_p]),
     ("cg_forward_3d_plan", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cg_backward_3d_plan", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("cg_adjoint_3d_plan", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cg_forward_3d", C.c_int,
      [C.c_void_p, u64p, f32p, f32p, C.c_void_p, f32p, f32p, f32p, C.c_uint64, u64p, f32p, f32p,
       f32p, C.c_float, C.c_float, C.c_float, C.c_void_p]),

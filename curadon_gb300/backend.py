@@ -21,7 +21,8 @@ import torch
 
 from ._lib import check, load
 
-__all__ = ["plan_2d", "plan_3d", "forward_2d", "backward_2d", "forward_3d", "backward_3d"]
+__all__ = ["plan_2d", "plan_3d", "forward_2d", "backward_2d", "adjoint_2d", "forward_3d",
+           "backward_3d"]
 
 
 def _u64(a):
@@ -151,6 +152,14 @@ def backward_2d(volume, sinogram, plan: plan_2d):
                                  C.c_void_p(sinogram.data_ptr()), _stream(volume)))
 
 
+def adjoint_2d(volume, sinogram, plan: plan_2d):
+    """Adds the matched adjoint (exact transpose of ``forward_2d``) of
+    ``sinogram`` to ``volume``."""
+    _check_2d(volume, sinogram, plan)
+    check(plan._L.cg_adjoint_2d(plan.handle, C.c_void_p(volume.data_ptr()),
+                                C.c_void_p(sinogram.data_ptr()), _stream(volume)))
+
+
 class plan_3d:
     """Cone-beam plan over the argument list of ``forward_3d``/``backward_3d``;
     ``angles`` is (3, nangles) = (phi, theta, psi)."""
@@ -207,6 +216,13 @@ class plan_3d:
         self._check(volume, sinogram)
         check(self._L.cg_backward_3d_plan(self._h, C.c_void_p(volume.data_ptr()),
                                           C.c_void_p(sinogram.data_ptr()), _stream(volume)))
+
+
+    def adjoint(self, volume, sinogram):
+        """Adds the matched adjoint of ``forward`` to ``volume``."""
+        self._check(volume, sinogram)
+        check(self._L.cg_adjoint_3d_plan(self._h, C.c_void_p(volume.data_ptr()),
+                                         C.c_void_p(sinogram.data_ptr()), _stream(volume)))
 
 
 def _call_3d(fn_name, x, vol_shape, vol_spacing, vol_offset, sinogram, a0, a1, a2, sino_shape,

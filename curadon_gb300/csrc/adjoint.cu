@@ -1,0 +1,211 @@
+// adjoint.cu -- matched adjoints (exact transposes) of the ray-driven
+// forward projectors, for gradients and for solvers that need A^T.
+//
+// Each kernel repeats its forward's ray set-up and sample points exactly and
+// scatters y_ray * (filter weights) into the same pair-packed, zero-padded
+// layouts the forward gathers from, with one 8-byte vector atomic per pair
+// (red.global.add.v2.f32).  A fold pass then adds the pair entries back onto
+// the texels they cover; entries that land in the padding correspond to the
+// zero border the forward reads and are dropped, so the result is the exact
+// transpose of the forward as implemented.  The curadon reference has no
+// matched adjoint (its backward of the forward is the voxel-driven
+// backprojector, diffable.py:21-24); this is an addition beside it.
+#include <cfloat>
+
+#include "common.cuh"
+
+namespace cg {
+namespace {
+
+// ------------------------------------------------------------ 2D
+
+__global__ void __launch_bounds__(256)
+    k_adj2d(float2 *__restrict__ accA, float2 *__restrict__ accB, const float *__restrict__ sino,
+            const float2 *__restrict__ tsrc, const float2 *__restrict__ tu0,
+            const float2 *__restrict__ tdu, int W, int H, int det, int nangles, float sx,
+            float sy) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    const int view = blockIdx.y * blockDim.y + threadIdx.y;
+    if (u >= det || view >= nangles) return;
+    const float2 s = tsrc[view], o = tu0[view], du = tdu[view];
+    const float fu = (float)u;
+    const float dx = fmaf(du.x, fu, o.x);
+    const float dy = fmaf(du.y, fu, o.y);
+    float tmin = FLT_MIN, tmax = FLT_MAX;
+    {
+        const float t1 = __fdividef(-1.f - s.x, dx), t2 = __fdividef((float)W - s.x, dx);
+        tmin = fminf(fmaxf(t1, tmin), fmaxf(t2, tmin));
+        tmax = fmaxf(fminf(t1, tmax), fminf(t2, tmax));
+    }
+    {
+        const float t1 = __fdividef(-1.f - s.y, dy), t2 = __fdividef((float)H - s.y, dy);
+        tmin = fminf(fmaxf(t1, tmin), fmaxf(t2, tmin));
+        tmax = fmaxf(fminf(t1, tmax), fminf(t2, tmax));
+    }
+    if ((double)tmin > (double)tmax - 1e-6) return;
+    const float rox = fmaf(dx, tmin, s.x), roy = fmaf(dy, tmin, s.y);
+    const float tl = tmax - tmin;
+    const float rdx = dx * tl, rdy = dy * tl;
+    const float m = fmaxf(fabsf(rdx), fabsf(rdy));
+    int n = __float2int_rn(m);
+    const float vx = rdx / m, vy = rdy / m;
+    const float c = sino[(size_t)view * det + u] * hypotf(vx * sx, vy * sy);
+    if (c == 0.f) return;
+
+    const bool ymajor = fabsf(rdy) >= fabsf(rdx);
+    float p = (ymajor ? rox : roy) - 0.5f;
+    const float vp = ymajor ? vx : vy;
+    const float q = (ymajor ? roy : rox) - 0.5f;
+    const int sq = ((ymajor ? vy : vx) > 0.f) ? 1 : -1;
+    float2 *acc = ymajor ? accA : accB;
+    const int pitch = (ymajor ? W : H) + 2 * kPad;
+    const float pmax = (float)(ymajor ? W : H);
+    const int qmax = ymajor ? H : W;
+    const float qf = floorf(q);
+    const float fq = q - qf;
+    const int iq = (int)fminf(fmaxf(qf, -(float)kPad), (float)qmax);
+    n = min(n, sq > 0 ? qmax - iq + 1 : iq + kPad + 1);
+    float2 *row = acc + (size_t)(iq + kPad) * pitch + kPad;
+    const long long rstep = (long long)sq * pitch;
+    const float clo = c * (1.f - fq), chi = c * fq;
+    for (int j = 0; j < n; ++j) {
+        const float pf = fminf(fmaxf(floorf(p), -(float)kPad), pmax);
+        const float fp = p - pf;
+        const int ip = (int)pf;
+        // forward: lo = x + fp (y - x) -> weights (1 - fp, fp) on the pair
+        atomicAdd(row + ip, make_float2(clo * (1.f - fp), clo * fp));
+        atomicAdd(row + pitch + ip, make_float2(chi * (1.f - fp), chi * fp));
+        p += vp;
+        row += rstep;
+    }
+}
+
+// vol[y][x] += A[y][x].x + A[y][x-1].y + B[x][y].x + B[x][y-1].y (padded).
+__global__ void k_fold2d(float *__restrict__ vol, const float2 *__restrict__ A,
+                         const float2 *__restrict__ B, int W, int H) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const int pa = W + 2 * kPad, pb = H + 2 * kPad;
+    const float2 *ra = A + (size_t)(y + kPad) * pa + kPad;
+    const float2 *rb = B + (size_t)(x + kPad) * pb + kPad;
+    vol[(size_t)y * W + x] += (ra[x].x + ra[x - 1].y) + (rb[y].x + rb[y - 1].y);
+}
+
+// ------------------------------------------------------------ 3D
+
+__global__ void __launch_bounds__(256)
+    k_adj3d(float2 *__restrict__ A, float2 *__restrict__ B, const float *__restrict__ sino,
+            const float4 *__restrict__ torg, const float4 *__restrict__ tdu,
+            const float4 *__restrict__ tdv, const float4 *__restrict__ tsrc, int X, int Y, int Z,
+            int U, int V) {
+    const int iu = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iv = blockIdx.y * blockDim.y + threadIdx.y;
+    const int view = blockIdx.z;
+    if (iu >= U || iv >= V) return;
+    const float c = sino[((size_t)view * V + iv) * U + iu];
+    if (c == 0.f) return;
+    const float4 o = torg[view], du = tdu[view], dv = tdv[view], s = tsrc[view];
+    const float fu = (float)iu, fv = (float)iv;
+    const float detx = o.x + fu * du.x + fv * dv.x;
+    const float dety = o.y + fu * du.y + fv * dv.y;
+    const float detz = o.z + fu * du.z + fv * dv.z;
+    const float dx = detx - s.x, dy = dety - s.y, dz = detz - s.z;
+    const float len = sqrtf(dx * dx + dy * dy + dz * dz);
+    const long long nsamples = (long long)ceilf(__fdividef(len, 1.0f));
+    float tmin = FLT_MIN, tmax = FLT_MAX;
+    {
+        const float t1 = __fdividef(-1.f - s.x, dx), t2 = __fdividef((float)(X + 1) - s.x, dx);
+        tmin = fminf(fmaxf(t1, tmin), fmaxf(t2, tmin));
+        tmax = fmaxf(fminf(t1, tmax), fminf(t2, tmax));
+    }
+    {
+        const float t1 = __fdividef(-1.f - s.y, dy), t2 = __fdividef((float)(Y + 1) - s.y, dy);
+        tmin = fminf(fmaxf(t1, tmin), fmaxf(t2, tmin));
+        tmax = fmaxf(fminf(t1, tmax), fminf(t2, tmax));
+    }
+    {
+        const float t1 = __fdividef(-1.f - s.z, dz), t2 = __fdividef((float)(Z + 1) - s.z, dz);
+        tmin = fminf(fmaxf(t1, tmin), fmaxf(t2, tmin));
+        tmax = fmaxf(fminf(t1, tmax), fminf(t2, tmax));
+    }
+    if (!(tmin <= tmax)) return;
+    const int nsteps = (int)ceilf((tmax - tmin) * (float)nsamples);
+    const float h = (tmax - tmin) / (float)nsteps;
+    if (!(h > 0.f) || !isfinite(tmax) || nsteps > (1 << 22)) return;
+
+    const bool xmajor = fabsf(dx) > fabsf(dz);
+    const float sa = xmajor ? s.z : s.x, da = xmajor ? dz : dx;
+    const float sc = xmajor ? s.x : s.z, dc = xmajor ? dx : dz;
+    float2 *L = xmajor ? B : A;
+    const int Na = xmajor ? Z : X, Nc = xmajor ? X : Z;
+    const int pa = Na + 2 * kPad, pb = Y + 2 * kPad;
+    const float amax = (float)Na, bmax = (float)Y, cmax = (float)Nc;
+    const float lo = -(float)kPad;
+    float t = tmin;
+    for (int k = 0; k <= nsteps + 1; ++k) {
+        if (!(t <= tmax)) break;
+        const float pa_ = fmaf(da, t, sa), pb_ = fmaf(dy, t, s.y), pc_ = fmaf(dc, t, sc);
+        const float fa = fminf(fmaxf(floorf(pa_), lo), amax);
+        const float fb = fminf(fmaxf(floorf(pb_), lo), bmax);
+        const float fc = fminf(fmaxf(floorf(pc_), lo), cmax);
+        const float wa = pa_ - fa, wb = pb_ - fb, wc = pc_ - fc;
+        float2 *p00 = L + ((size_t)((int)fc + kPad) * pb + ((int)fb + kPad)) * pa + ((int)fa + kPad);
+        const float c00 = c * (1.f - wb) * (1.f - wc), c10 = c * wb * (1.f - wc);
+        const float c01 = c * (1.f - wb) * wc, c11 = c * wb * wc;
+        atomicAdd(p00, make_float2(c00 * (1.f - wa), c00 * wa));
+        atomicAdd(p00 + pa, make_float2(c10 * (1.f - wa), c10 * wa));
+        atomicAdd(p00 + (size_t)pa * pb, make_float2(c01 * (1.f - wa), c01 * wa));
+        atomicAdd(p00 + (size_t)pa * pb + pa, make_float2(c11 * (1.f - wa), c11 * wa));
+        t += h;
+    }
+}
+
+// vol[z][y][x] += A[z][y][x].x + A[z][y][x-1].y + B[x][y][z].x + B[x][y][z-1].y
+__global__ void k_fold3d(float *__restrict__ vol, const float2 *__restrict__ A,
+                         const float2 *__restrict__ B, int X, int Y, int Z) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)X * Y * Z) return;
+    const int x = (int)(idx % X);
+    const int y = (int)((idx / X) % Y);
+    const int z = (int)(idx / ((long long)X * Y));
+    const int PX = X + 2 * kPad, PY = Y + 2 * kPad, PZ = Z + 2 * kPad;
+    const float2 *ra = A + ((size_t)(z + kPad) * PY + (y + kPad)) * PX + (x + kPad);
+    const float2 *rb = B + ((size_t)(x + kPad) * PY + (y + kPad)) * PZ + (z + kPad);
+    vol[idx] += (ra[0].x + ra[-1].y) + (rb[0].x + rb[-1].y);
+}
+
+}  // namespace
+
+int launch_adjoint2d(const Plan2d &p, float *vol, const float *sino, cudaStream_t s) {
+    const size_t na = (size_t)p.pitchA() * (p.H + 2 * kPad);
+    const size_t nb = (size_t)p.pitchB() * (p.W + 2 * kPad);
+    CG_TRY_CUDA(cudaMemsetAsync(p.d_layA, 0, na * sizeof(float2), s));
+    CG_TRY_CUDA(cudaMemsetAsync(p.d_layB, 0, nb * sizeof(float2), s));
+    dim3 block(p.fwd_bx, p.fwd_by);
+    dim3 grid(ceil_div(p.det, p.fwd_bx), ceil_div(p.nangles, p.fwd_by));
+    if (grid.y > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
+    k_adj2d<<<grid, block, 0, s>>>(p.d_layA, p.d_layB, sino, p.d_src, p.d_u0, p.d_du, p.W, p.H,
+                                   p.det, p.nangles, p.sx, p.sy);
+    CG_TRY_CUDA(cudaGetLastError());
+    k_fold2d<<<dim3(ceil_div(p.W, 32), ceil_div(p.H, 8)), dim3(32, 8), 0, s>>>(
+        vol, p.d_layA, p.d_layB, p.W, p.H);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
+int launch_adjoint3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s) {
+    CG_TRY_CUDA(cudaMemsetAsync(p.d_volA, 0, p.volA_elems * sizeof(float2), s));
+    CG_TRY_CUDA(cudaMemsetAsync(p.d_volB, 0, p.volB_elems * sizeof(float2), s));
+    if (p.nangles > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
+    dim3 grid(ceil_div(p.U, 32), ceil_div(p.V, 8), p.nangles);
+    k_adj3d<<<grid, dim3(32, 8), 0, s>>>(p.d_volA, p.d_volB, sino, p.d_forg, p.d_fdu, p.d_fdv,
+                                         p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V);
+    CG_TRY_CUDA(cudaGetLastError());
+    const long long n = (long long)p.X * p.Y * p.Z;
+    k_fold3d<<<ceil_div(n, 256), 256, 0, s>>>(vol, p.d_volA, p.d_volB, p.X, p.Y, p.Z);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
+}  // namespace cg

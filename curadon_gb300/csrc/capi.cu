@@ -402,6 +402,15 @@ int cg_backward_2d(cg_plan2d *plan, float *volume, const float *sinogram, void *
     return launch_backward2d(*plan, volume, s);
 }
 
+int cg_adjoint_2d(cg_plan2d *plan, float *volume, const float *sinogram, void *stream) {
+    clear_error();
+    CG_REQUIRE(plan, "plan is NULL");
+    CG_REQUIRE(volume && sinogram, "volume and sinogram must be device pointers");
+    DeviceGuard guard(plan->device);
+    CG_REQUIRE(guard.ok(), "cannot select the plan's device");
+    return launch_adjoint2d(*plan, volume, sinogram, (cudaStream_t)stream);
+}
+
 int cg_plan3d_create(cg_plan3d **plan, int device, const uint64_t vol_shape[3],
                      const float vol_spacing[3], const float vol_offset[3], const float *phi,
                      const float *theta, const float *psi, uint64_t nangles,
@@ -444,6 +453,17 @@ int cg_backward_3d_plan(cg_plan3d *plan, float *volume, const float *sinogram, v
     int rc = ensure_plan3d_scratch(*plan, false, true);
     if (rc) return rc;
     return launch_backward3d(*plan, volume, sinogram, (cudaStream_t)stream);
+}
+
+int cg_adjoint_3d_plan(cg_plan3d *plan, float *volume, const float *sinogram, void *stream) {
+    clear_error();
+    CG_REQUIRE(plan, "plan is NULL");
+    CG_REQUIRE(volume && sinogram, "volume and sinogram must be device pointers");
+    DeviceGuard guard(plan->device);
+    CG_REQUIRE(guard.ok(), "cannot select the plan's device");
+    int rc = ensure_plan3d_scratch(*plan, true, false);
+    if (rc) return rc;
+    return launch_adjoint3d(*plan, volume, sinogram, (cudaStream_t)stream);
 }
 
 static int current_device(int *dev) {

@@ -122,6 +122,9 @@ int ensure_plan3d_scratch(Plan3d &p, bool fwd, bool bwd);
 int launch_forward3d(const Plan3d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s);
 
+int launch_adjoint2d(const Plan2d &p, float *vol, const float *sino, cudaStream_t s);
+int launch_adjoint3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s);
+
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 }  // namespace cg

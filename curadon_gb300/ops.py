@@ -21,7 +21,7 @@ from torch.autograd import Function
 from . import backend as _C
 from .geometry import ConeGeometry, FanGeometry
 
-__all__ = ["forward", "backward", "TorchForward", "TorchBackprojection"]
+__all__ = ["forward", "backward", "adjoint", "TorchForward", "TorchBackprojection"]
 
 
 def forward(volume, sinogram, geom: Union[FanGeometry, ConeGeometry]):
@@ -44,25 +44,44 @@ def backward(sinogram, volume, geom: Union[FanGeometry, ConeGeometry]):
     raise ValueError("Unknown geometry type")
 
 
+def adjoint(sinogram, volume, geom: Union[FanGeometry, ConeGeometry]):
+    """Adds the matched adjoint A^T sinogram (exact transpose of ``forward``)
+    to ``volume`` and returns it.  An addition beside the reference's API."""
+    if isinstance(geom, FanGeometry):
+        _C.adjoint_2d(volume, sinogram, geom.plan)
+        return volume
+    if isinstance(geom, ConeGeometry):
+        geom.plan.adjoint(volume, sinogram)
+        return volume
+    raise ValueError("Unknown geometry type")
+
+
 def _vol_shape(geom):
     return tuple(int(v) for v in geom.vol_shape)
 
 
 class TorchForward(Function):
-    """Differentiable forward projection; gradient = backprojection."""
+    """Differentiable forward projection.
+
+    ``TorchForward.apply(volume, geom)``: the gradient is the reference's
+    voxel-driven backprojector (as in diffable.py:21-24).
+    ``TorchForward.apply(volume, geom, True)``: the gradient is the matched
+    adjoint, so it is the exact gradient of the forward."""
 
     @staticmethod
-    def forward(ctx, volume, geom):
+    def forward(ctx, volume, geom, matched=False):
         sino = torch.zeros(geom.sinogram_shape(), device=volume.device, dtype=torch.float32)
         forward(volume.detach().contiguous(), sino, geom)
         ctx.geom = geom
+        ctx.matched = bool(matched)
         return sino
 
     @staticmethod
     def backward(ctx, grad_sino):
         grad = torch.zeros(_vol_shape(ctx.geom), device=grad_sino.device, dtype=torch.float32)
-        backward(grad_sino.detach().contiguous(), grad, ctx.geom)
-        return grad, None
+        op = adjoint if ctx.matched else backward
+        op(grad_sino.detach().contiguous(), grad, ctx.geom)
+        return grad, None, None
 
 
 class TorchBackprojection(Function):

@@ -69,7 +69,7 @@ int cg_plan2d_destroy(cg_plan2d *plan);
 
 /* The reference's read-write `forward_block_x` / `forward_block_y`
  * (plan.cu:57-58, plan_2d.hpp:184-186): here they set the detector-cells x
- * views shape of one forward thread block (product 32..1024, x multiple of 32). */
+ * views shape of one forward thread block (x a multiple of 32, x * y <= 256). */
 int cg_plan2d_get_forward_block(const cg_plan2d *plan, uint64_t *bx, uint64_t *by);
 int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by);
 
@@ -87,6 +87,13 @@ int cg_forward_2d(cg_plan2d *plan, const float *volume, float *sinogram, void *s
  * `backward_2d(volume, sinogram, plan)` (backward.cu:233-280 ->
  * bp::backproject_2d, backward_2d.hpp:302-306). */
 int cg_backward_2d(cg_plan2d *plan, float *volume, const float *sinogram, void *stream);
+
+/* Matched adjoint of cg_forward_2d, accumulating A^T sinogram into `volume`:
+ * the exact transpose of the ray-driven interpolation (same rays, sample
+ * points and weights), for gradients and solvers that need <Ax,y> = <x,A^T y>.
+ * No counterpart call in the reference, whose backward of the forward is the
+ * voxel-driven backprojector (diffable.py:21-24). */
+int cg_adjoint_2d(cg_plan2d *plan, float *volume, const float *sinogram, void *stream);
 
 /* ------------------------------------------------------------------ 3D -- */
 
@@ -117,6 +124,11 @@ int cg_forward_3d_plan(cg_plan3d *plan, const float *volume, float *sinogram, vo
 /* 3D voxel-driven backprojection with a plan, accumulating
  * (bp::backproject_3d, backward_3d.hpp:457-529). */
 int cg_backward_3d_plan(cg_plan3d *plan, float *volume, const float *sinogram, void *stream);
+
+/* Matched adjoint of cg_forward_3d_plan, accumulating into `volume`; rays
+ * that miss the volume contribute nothing.  No counterpart in the reference
+ * (see cg_adjoint_2d). */
+int cg_adjoint_3d_plan(cg_plan3d *plan, float *volume, const float *sinogram, void *stream);
 
 /* Per-call forms with the reference's exact argument list: they build a
  * transient plan (as the reference allocates its texture array per call),
