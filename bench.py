@@ -178,6 +178,21 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
+# ------------------------------------------------------------ ranks
+
+def reduce_max(values, world: int, device="cpu"):
+    """Element-wise max of per-rank timings over all ranks (the replicas run
+    independently; only their timings are exchanged)."""
+    import torch
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
 # ------------------------------------------------------------ ours
 
 def run_ours(args, rank, world, local_rank):
@@ -271,11 +286,8 @@ def run_ours(args, rank, world, local_rank):
     e2e_ms = sum(a.elapsed_time(b) for a, b in e_ev)
     clocks = sampler.stop() if sampler else None
 
-    # max over ranks
-    tt = torch.tensor([total_ms, e2e_ms, sum(t_fwd), sum(t_bwd)], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-    total_ms, e2e_ms, fwd_ms, bwd_ms = (float(v) for v in tt.cpu())
+    total_ms, e2e_ms, fwd_ms, bwd_ms = reduce_max([total_ms, e2e_ms, sum(t_fwd), sum(t_bwd)],
+                                                  world, dev)
     if rank != 0:
         return None
 

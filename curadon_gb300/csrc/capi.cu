@@ -1,6 +1,7 @@
 // capi.cu -- the extern "C" boundary (include/curadon_gb300.h): argument
 // checking, plan construction and the operator entry points.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -30,6 +31,10 @@ static int alloc_copy(T **dst, const T *src, size_t n) {
 
 void free_plan2d(Plan2d *p) {
     if (!p) return;
+    if (p->tex_vol) cudaDestroyTextureObject(p->tex_vol);
+    if (p->tex_sino) cudaDestroyTextureObject(p->tex_sino);
+    if (p->arr_vol) cudaFreeArray(p->arr_vol);
+    if (p->arr_sino) cudaFreeArray(p->arr_sino);
     void *ptrs[] = {p->d_angles, p->d_DSO, p->d_DSD, p->d_src,  p->d_u0,
                     p->d_du,     p->d_bmeta, p->d_layA, p->d_layB, p->d_sinoP};
     for (void *q : ptrs)
@@ -38,10 +43,34 @@ void free_plan2d(Plan2d *p) {
 
 void free_plan3d(Plan3d *p) {
     if (!p) return;
+    for (cudaTextureObject_t t : {p->tex3, p->texA, p->texB})
+        if (t) cudaDestroyTextureObject(t);
+    for (cudaArray_t a : {p->arr3, p->arrA, p->arrB})
+        if (a) cudaFreeArray(a);
+    if (p->d_volT) cudaFree(p->d_volT);
     void *ptrs[] = {p->d_forg, p->d_fdu, p->d_fdv, p->d_fsrc, p->d_borg, p->d_bdx,
                     p->d_bdy,  p->d_bdz, p->d_volA, p->d_volB, p->d_sinoP};
     for (void *q : ptrs)
         if (q) cudaFree(q);
+}
+
+void apply_algo_env(Plan2d *p2, Plan3d *p3) {
+    const char *env = std::getenv("CURADON_GB300_ALGO");
+    if (!env) return;
+    std::string e(env);
+    auto has = [&](const char *kv) { return e.find(kv) != std::string::npos; };
+    if (p2) {
+        if (has("fwd2d=alu")) p2->algo_fwd = 0;
+        if (has("fwd2d=tex")) p2->algo_fwd = 1;
+        if (has("bwd2d=alu")) p2->algo_bwd = 0;
+        if (has("bwd2d=tex")) p2->algo_bwd = 1;
+        if (has("bwd2d=smem")) p2->algo_bwd = 2;
+    }
+    if (p3) {
+        if (has("fwd3d=alu")) p3->algo_fwd = 0;
+        if (has("fwd3d=tex3")) p3->algo_fwd = 1;
+        if (has("fwd3d=tex2l")) p3->algo_fwd = 2;
+    }
 }
 
 // ------------------------------------------------------------ 3D geometry
@@ -225,6 +254,7 @@ int make_plan3d(cg_plan3d **out, int device, const uint64_t vol_shape[3], const 
     p->U = (int)det_shape[1], p->V = (int)det_shape[0];
     p->nangles = (int)nangles;
     p->DSO = DSO, p->DSD = DSD;
+    apply_algo_env(nullptr, p.get());
     Cone c;
     c.shape_f = {{(float)vol_shape[2], (float)vol_shape[1], (float)vol_shape[0]}};
     c.spacing = {{vol_spacing[2], vol_spacing[1], vol_spacing[0]}};
@@ -308,6 +338,7 @@ int cg_plan2d_create(cg_plan2d **plan, int device, uint32_t vol_prec, const uint
     p->ox = vol_offset[1], p->oy = vol_offset[0];
     p->det = (int)det_count, p->ds = det_spacing, p->doff = det_offset;
     p->nangles = (int)nangles, p->pitch = det_pitch, p->COR = COR;
+    apply_algo_env(p.get(), nullptr);
     int rc = CG_OK;
     auto fail = [&](int code) {
         free_plan2d(p.get());
@@ -385,6 +416,7 @@ int cg_forward_2d(cg_plan2d *plan, const float *volume, float *sinogram, void *s
     DeviceGuard guard(plan->device);
     CG_REQUIRE(guard.ok(), "cannot select the plan's device");
     cudaStream_t s = (cudaStream_t)stream;
+    if (plan->algo_fwd == 1) return launch_forward2d_tex(*plan, volume, sinogram, s);
     int rc = launch_relayout2d(*plan, volume, s);
     if (rc) return rc;
     return launch_forward2d(*plan, sinogram, s);
@@ -397,8 +429,10 @@ int cg_backward_2d(cg_plan2d *plan, float *volume, const float *sinogram, void *
     DeviceGuard guard(plan->device);
     CG_REQUIRE(guard.ok(), "cannot select the plan's device");
     cudaStream_t s = (cudaStream_t)stream;
+    if (plan->algo_bwd == 1) return launch_backward2d_tex(*plan, volume, sinogram, s);
     int rc = launch_relayout_sino2d(*plan, sinogram, s);
     if (rc) return rc;
+    if (plan->algo_bwd == 2) return launch_backward2d_smem(*plan, volume, s);
     return launch_backward2d(*plan, volume, s);
 }
 
@@ -439,6 +473,7 @@ int cg_forward_3d_plan(cg_plan3d *plan, const float *volume, float *sinogram, vo
     CG_REQUIRE(volume && sinogram, "volume and sinogram must be device pointers");
     DeviceGuard guard(plan->device);
     CG_REQUIRE(guard.ok(), "cannot select the plan's device");
+    if (plan->algo_fwd != 0) return launch_forward3d_tex(*plan, volume, sinogram, (cudaStream_t)stream);
     int rc = ensure_plan3d_scratch(*plan, true, false);
     if (rc) return rc;
     return launch_forward3d(*plan, volume, sinogram, (cudaStream_t)stream);
@@ -484,8 +519,12 @@ int cg_forward_3d(const float *x, const uint64_t vol_shape[3], const float vol_s
     rc = make_plan3d(&p, dev, vol_shape, vol_spacing, vol_offset, phi, theta, psi, nangles,
                      det_shape, det_spacing, det_offset, det_rotation, DSO, DSD, COR);
     if (rc) return rc;
-    rc = ensure_plan3d_scratch(*p, true, false);
-    if (!rc) rc = launch_forward3d(*p, x, sinogram, (cudaStream_t)stream);
+    if (p->algo_fwd != 0) {
+        rc = launch_forward3d_tex(*p, x, sinogram, (cudaStream_t)stream);
+    } else {
+        rc = ensure_plan3d_scratch(*p, true, false);
+        if (!rc) rc = launch_forward3d(*p, x, sinogram, (cudaStream_t)stream);
+    }
     // The transient plan's memory is released once the stream has used it.
     cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
     if (!rc && e != cudaSuccess) rc = set_error(CG_ERR_CUDA, cudaGetErrorString(e));
@@ -514,6 +553,18 @@ int cg_backward_3d(float *x, const uint64_t vol_shape[3], const float vol_spacin
     free_plan3d(p);
     delete p;
     return rc;
+}
+
+int cg_filter_rows(const float *in, float *out, const float *h, const float *pre, uint64_t nrows,
+                   uint64_t ncols, float scale, void *stream) {
+    clear_error();
+    CG_REQUIRE(in && out && h, "in, out and h must be device pointers");
+    CG_REQUIRE(in != out, "out must not alias in");
+    CG_REQUIRE(ncols > 0 && ncols <= 29056, "ncols out of range (1..29056)");
+    CG_REQUIRE(nrows > 0 && nrows <= (1u << 26), "nrows out of range");
+    CG_REQUIRE(ceil_div((long long)nrows, 1) <= 65535LL * 8, "too many rows for one launch");
+    return launch_filter_rows(in, out, h, pre, (int)nrows, (int)ncols, scale,
+                              (cudaStream_t)stream);
 }
 
 }  // extern "C"

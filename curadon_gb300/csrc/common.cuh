@@ -82,6 +82,14 @@ struct Plan2d {
     float2 *d_layB = nullptr;         // (W+2P) x (H+2P) pairs along y
     float2 *d_sinoP = nullptr;        // nangles x (det+2P) pairs along u
 
+    // texture-unit variants (allocated on first use)
+    cudaArray_t arr_vol = nullptr, arr_sino = nullptr;
+    cudaTextureObject_t tex_vol = 0, tex_sino = 0;
+
+    // algorithm per operator: forward 0 = registers, 1 = texture unit;
+    // backprojection 0 = registers, 1 = texture unit, 2 = shared-memory rows
+    int algo_fwd = 0, algo_bwd = 0;
+
     int pitchA() const { return W + 2 * kPad; }
     int pitchB() const { return H + 2 * kPad; }
     int pitchS() const { return det + 2 * kPad; }
@@ -105,6 +113,14 @@ struct Plan3d {
     float2 *d_volB = nullptr;         // (X+2P)(Y+2P)(Z+2P) pairs along z
     float2 *d_sinoP = nullptr;        // nangles (V+2P)(U+2P) pairs along u
     size_t volA_elems = 0, volB_elems = 0, sinoP_elems = 0;
+
+    // texture-unit variants (allocated on first use)
+    cudaArray_t arr3 = nullptr, arrA = nullptr, arrB = nullptr;
+    cudaTextureObject_t tex3 = 0, texA = 0, texB = 0;
+    float *d_volT = nullptr;          // x<->z transposed volume for arrB
+
+    // forward 0 = registers, 1 = tex3D, 2 = layered bilinear + lerp
+    int algo_fwd = 0, algo_bwd = 0;
 };
 
 void free_plan2d(Plan2d *p);
@@ -124,6 +140,18 @@ int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream
 
 int launch_adjoint2d(const Plan2d &p, float *vol, const float *sino, cudaStream_t s);
 int launch_adjoint3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s);
+
+int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s);
+int launch_forward2d_tex(Plan2d &p, const float *vol, float *sino, cudaStream_t s);
+int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t s);
+int launch_forward3d_tex(Plan3d &p, const float *vol, float *sino, cudaStream_t s);
+
+// Reads CURADON_GB300_ALGO ("fwd2d=tex,bwd2d=smem,fwd3d=tex2l,...") over the
+// defaults of a new plan.
+void apply_algo_env(Plan2d *p2, Plan3d *p3);
+
+int launch_filter_rows(const float *in, float *out, const float *h, const float *pre, int nrows,
+                       int N, float scale, cudaStream_t s);
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 

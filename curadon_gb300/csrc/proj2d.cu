@@ -12,6 +12,7 @@
 // Interpolation is FP32 in registers (no texture unit); clamping a texel
 // index into the zero padding reproduces cudaAddressModeBorder.
 #include <cfloat>
+#include <climits>
 
 #include "common.cuh"
 
@@ -242,6 +243,116 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// ------------------------------------------------------------ backward, staged
+
+constexpr int kSmViews = 32;  // views staged per pass
+constexpr int kSmWin = 96;    // pairs of one view's row staged for a tile
+
+// Same arithmetic as k_bwd2d, but per pass of 32 views each block first
+// computes, from its tile's four corner pixels, the window of detector cells
+// its pixels project to (a projective map sends the tile's convex hull to an
+// interval bounded by the corners), stages those pairs in shared memory and
+// samples them there.  A view whose window exceeds kSmWin pairs is sampled
+// from global memory instead.
+__global__ void __launch_bounds__(256)
+    k_bwd2d_smem(float *__restrict__ vol, const float2 *__restrict__ S,
+                 const float4 *__restrict__ meta, int W, int H, int det, int nangles, float sx,
+                 float sy, float ox, float oy, float ds) {
+    __shared__ float2 srow[kSmViews][kSmWin];
+    __shared__ float4 smeta[kSmViews];
+    __shared__ int skmin[kSmViews];
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int xt = blockIdx.x * 32, yt = blockIdx.y * 32;
+    const int x = xt + threadIdx.x;
+    const int y0 = yt + threadIdx.y;
+    const float ex = (float)W / 2.0f, ey = (float)H / 2.0f, ed = (float)det / 2.0f;
+    const float inv = __fdividef(1.0f, ds);
+    const float X = ((float)x - ex) * sx + ox + 0.5f;
+    const float SX = X * inv;
+    float Y[kBwdRows], SY[kBwdRows], acc[kBwdRows];
+#pragma unroll
+    for (int r = 0; r < kBwdRows; ++r) {
+        Y[r] = ((float)(y0 + 8 * r) - ey) * sy + oy + 0.5f;
+        SY[r] = Y[r] * inv;
+        acc[r] = 0.f;
+    }
+    const int pitch = det + 2 * kPad;
+    const float kmax = (float)det;
+    for (int v0 = 0; v0 < nangles; v0 += kSmViews) {
+        const int nv = min(kSmViews, nangles - v0);
+        __syncthreads();
+        if (tid < nv) {
+            const float4 m = meta[v0 + tid];
+            smeta[tid] = m;
+            float lo = FLT_MAX, hi = -FLT_MAX;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float cX = ((float)(xt + (c & 1) * 31) - ex) * sx + ox + 0.5f;
+                const float cY = ((float)(yt + (c >> 1) * 31) - ey) * sy + oy + 0.5f;
+                const float xi = m.x * cX - m.y * cY;
+                const float yi = m.y * (cX * inv) + m.x * (cY * inv);
+                const float w = __fdividef(m.z, xi + m.w);
+                const float ub = (w * yi + ed) - 0.5f;
+                lo = fminf(lo, ub);
+                hi = fmaxf(hi, ub);
+            }
+            int k0 = INT_MIN;
+            if (lo >= -1e6f && hi <= 1e6f) {
+                const int a = (int)floorf(lo) - 1, b = (int)floorf(hi) + 1;
+                if (b - a + 1 <= kSmWin) k0 = a;
+            }
+            skmin[tid] = k0;
+        }
+        __syncthreads();
+        for (int e = tid; e < nv * kSmWin; e += 256) {
+            const int j = e / kSmWin, i = e - j * kSmWin;
+            const int k0 = skmin[j];
+            if (k0 == INT_MIN) continue;
+            const int k = min(max(k0 + i, -kPad), det);
+            srow[j][i] = S[(size_t)(v0 + j) * pitch + kPad + k];
+        }
+        __syncthreads();
+        for (int j = 0; j < nv; ++j) {
+            const float4 m = smeta[j];
+            const int k0 = skmin[j];
+            if (k0 != INT_MIN) {
+#pragma unroll
+                for (int r = 0; r < kBwdRows; ++r) {
+                    const float xi = m.x * X - m.y * Y[r];
+                    const float yi = m.y * SX + m.x * SY[r];
+                    const float w = __fdividef(m.z, xi + m.w);
+                    const float ub = (w * yi + ed) - 0.5f;
+                    const float kf = floorf(ub);
+                    const float a = ub - kf;
+                    const int li = min(max((int)kf - k0, 0), kSmWin - 1);
+                    const float2 t = srow[j][li];
+                    acc[r] = fmaf(fmaf(a, t.y - t.x, t.x), w, acc[r]);
+                }
+            } else {
+                const float2 *row = S + (size_t)(v0 + j) * pitch + kPad;
+#pragma unroll
+                for (int r = 0; r < kBwdRows; ++r) {
+                    const float xi = m.x * X - m.y * Y[r];
+                    const float yi = m.y * SX + m.x * SY[r];
+                    const float w = __fdividef(m.z, xi + m.w);
+                    const float ub = (w * yi + ed) - 0.5f;
+                    const float kf = fminf(fmaxf(floorf(ub), -(float)kPad), kmax);
+                    const float a = ub - kf;
+                    const float2 t = __ldg(row + (int)kf);
+                    acc[r] = fmaf(fmaf(a, t.y - t.x, t.x), w, acc[r]);
+                }
+            }
+        }
+    }
+    if (x < W) {
+#pragma unroll
+        for (int r = 0; r < kBwdRows; ++r) {
+            const int y = y0 + 8 * r;
+            if (y < H) vol[(size_t)y * W + x] += acc[r] * inv;
+        }
+    }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------ launchers
@@ -276,6 +387,14 @@ int launch_forward2d(const Plan2d &p, float *sino, cudaStream_t s) {
 int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s) {
     const long long n = (long long)p.pitchS() * p.nangles;
     k_relayout_sino2d<<<ceil_div(n, 256), 256, 0, s>>>(sino, p.det, p.nangles, p.d_sinoP);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
+int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s) {
+    dim3 grid(ceil_div(p.W, 32), ceil_div(p.H, 32));
+    k_bwd2d_smem<<<grid, dim3(32, 8), 0, s>>>(vol, p.d_sinoP, p.d_bmeta, p.W, p.H, p.det,
+                                              p.nangles, p.sx, p.sy, p.ox, p.oy, p.ds);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }

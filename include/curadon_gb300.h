@@ -148,6 +148,18 @@ int cg_backward_3d(float *x, const uint64_t vol_shape[3], const float vol_spacin
                    const float det_offset[2], const float det_rotation[3], float DSO, float DSD,
                    float COR, void *stream);
 
+/* ----------------------------------------------------------------- FBP -- */
+
+/* Row filter of filtered backprojection: out[r][k] = scale * sum_j
+ * pre[j] * in[r][j] * h[(k - j) mod ncols] for each of the nrows rows, i.e. the
+ * circular convolution that the reference's FBP evaluates through the FFT
+ * (examples/fbp.py:51-56: multiply each row's DFT by a real response and
+ * keep the real part; h is the real part of that response's inverse DFT).
+ * in, out, h (ncols floats) and pre (ncols floats, or NULL for none) are
+ * device pointers; out must not alias in.  ncols <= 29056. */
+int cg_filter_rows(const float *in, float *out, const float *h, const float *pre, uint64_t nrows,
+                   uint64_t ncols, float scale, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

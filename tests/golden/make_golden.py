@@ -7,8 +7,10 @@ the reference's outputs for them:
   fan_cfg0   64x64, 360 views, det 91 x 1.5, DSO 256, DSD 384 (the CPU-runnable
              fan-beam workload): forward sinogram, backprojection into zeros,
              and the plan's per-view tables
-  fan_var    80 x 48 volume, anisotropic spacing, volume and detector offsets,
-             per-view jittered DSO/DSD, 97 irregular views
+  fan_var    96 x 48 volume, anisotropic spacing, volume and detector offsets,
+             per-view jittered DSO/DSD, 97 irregular views (the image is a
+             multiple of the reference backprojector's 32 x 8 thread block:
+             in partial blocks it reads an uninitialised shared table)
   cone_small 36 x 40 x 32 volume, 24 views, 48 x 40 detector
   cone_rot   as cone_small with volume/detector offsets, detector
              roll/pitch/yaw, COR and full (phi, theta, psi) angles
@@ -43,10 +45,10 @@ def fan_cases():
     n = 97
     angles = np.sort(rng.uniform(0, 2 * np.pi, n)).astype(np.float32)
     g1 = dict(angles=angles, DSO=(150 + rng.normal(0, 0.5, n)).astype(np.float32),
-              DSD=(260 + rng.normal(0, 0.5, n)).astype(np.float32), vol_shape=(48, 80),
-              vol_spacing=(0.8, 1.2), vol_offset=(3.0, -2.0), det_shape=100, det_spacing=1.3,
+              DSD=(260 + rng.normal(0, 0.5, n)).astype(np.float32), vol_shape=(48, 96),
+              vol_spacing=(0.8, 1.2), vol_offset=(3.0, -2.0), det_shape=120, det_spacing=1.3,
               det_offset=1.7)
-    ph = ellipses_2d(80, 1).numpy()[16:64, :]
+    ph = ellipses_2d(96, 1).numpy()[24:72, :]
     yield "fan_var", g1, np.ascontiguousarray(ph)
 
 
