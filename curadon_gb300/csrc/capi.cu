@@ -62,6 +62,10 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
     if (p2) {
         if (has("fwd2d=alu")) p2->algo_fwd = 0;
         if (has("fwd2d=tex")) p2->algo_fwd = 1;
+        for (int k = 1; k < 8; ++k) {
+            const std::string key = "fwd2d=hyb" + std::to_string(k);
+            if (has(key.c_str())) p2->algo_fwd = 2, p2->tex_eighths = k;
+        }
         if (has("bwd2d=alu")) p2->algo_bwd = 0;
         if (has("bwd2d=tex")) p2->algo_bwd = 1;
         if (has("bwd2d=smem")) p2->algo_bwd = 2;
@@ -417,6 +421,7 @@ int cg_forward_2d(cg_plan2d *plan, const float *volume, float *sinogram, void *s
     CG_REQUIRE(guard.ok(), "cannot select the plan's device");
     cudaStream_t s = (cudaStream_t)stream;
     if (plan->algo_fwd == 1) return launch_forward2d_tex(*plan, volume, sinogram, s);
+    if (plan->algo_fwd == 2) return launch_forward2d_hyb(*plan, volume, sinogram, s);
     int rc = launch_relayout2d(*plan, volume, s);
     if (rc) return rc;
     return launch_forward2d(*plan, sinogram, s);

@@ -89,6 +89,7 @@ struct Plan2d {
     // algorithm per operator: forward 0 = registers, 1 = texture unit;
     // backprojection 0 = registers, 1 = texture unit, 2 = shared-memory rows
     int algo_fwd = 0, algo_bwd = 0;
+    int tex_eighths = 4;              // hybrid forward: share of warps on the texture unit
 
     int pitchA() const { return W + 2 * kPad; }
     int pitchB() const { return H + 2 * kPad; }
@@ -143,6 +144,7 @@ int launch_adjoint3d(const Plan3d &p, float *vol, const float *sino, cudaStream_
 
 int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s);
 int launch_forward2d_tex(Plan2d &p, const float *vol, float *sino, cudaStream_t s);
+int launch_forward2d_hyb(Plan2d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t s);
 int launch_forward3d_tex(Plan3d &p, const float *vol, float *sino, cudaStream_t s);
 

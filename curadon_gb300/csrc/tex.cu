@@ -105,6 +105,91 @@ __global__ void __launch_bounds__(256)
     *out = acc * hypotf(vx * sx, vy * sy);
 }
 
+// Warps whose (block, warp) index falls in the first `tex_eighths` of every
+// eight march through the texture unit, the others gather pair-packed texels
+// and filter in registers, so both the texture pipeline and the load/ALU
+// pipelines carry samples at once.  Ray set-up is shared.
+__global__ void __launch_bounds__(256)
+    k_fwd2d_hyb(cudaTextureObject_t tex, const float2 *__restrict__ layA,
+                const float2 *__restrict__ layB, float *__restrict__ sino,
+                const float2 *__restrict__ tsrc, const float2 *__restrict__ tu0,
+                const float2 *__restrict__ tdu, int W, int H, int det, int nangles, float sx,
+                float sy, int tex_eighths) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    const int view = blockIdx.y * blockDim.y + threadIdx.y;
+    if (u >= det || view >= nangles) return;
+    const int warp = (threadIdx.y * blockDim.x + threadIdx.x) >> 5;
+    const bool use_tex = ((blockIdx.x + blockIdx.y * 3 + warp) & 7) < tex_eighths;
+    const float2 s = tsrc[view], o = tu0[view], du = tdu[view];
+    const float fu = (float)u;
+    const float dx = fmaf(du.x, fu, o.x);
+    const float dy = fmaf(du.y, fu, o.y);
+    float tmin = FLT_MIN, tmax = FLT_MAX;
+    {
+        const float t1 = __fdividef(-1.f - s.x, dx), t2 = __fdividef((float)W - s.x, dx);
+        tmin = fminf(fmaxf(t1, tmin), fmaxf(t2, tmin));
+        tmax = fmaxf(fminf(t1, tmax), fminf(t2, tmax));
+    }
+    {
+        const float t1 = __fdividef(-1.f - s.y, dy), t2 = __fdividef((float)H - s.y, dy);
+        tmin = fminf(fmaxf(t1, tmin), fmaxf(t2, tmin));
+        tmax = fmaxf(fminf(t1, tmax), fminf(t2, tmax));
+    }
+    float *out = sino + (size_t)view * det + u;
+    if ((double)tmin > (double)tmax - 1e-6) {
+        *out = 0.f;
+        return;
+    }
+    const float rox = fmaf(dx, tmin, s.x), roy = fmaf(dy, tmin, s.y);
+    const float tl = tmax - tmin;
+    const float rdx = dx * tl, rdy = dy * tl;
+    const float m = fmaxf(fabsf(rdx), fabsf(rdy));
+    int n = __float2int_rn(m);
+    const float vx = rdx / m, vy = rdy / m;
+    float acc;
+    if (use_tex) {
+        float x = rox, y = roy;
+        acc = 0.f;
+#pragma unroll 4
+        for (int j = 0; j < n; ++j) {
+            acc += tex2D<float>(tex, x, y);
+            x += vx;
+            y += vy;
+        }
+    } else {
+        const bool ymajor = fabsf(rdy) >= fabsf(rdx);
+        float p = (ymajor ? rox : roy) - 0.5f;
+        const float vp = ymajor ? vx : vy;
+        const float q = (ymajor ? roy : rox) - 0.5f;
+        const int sq = ((ymajor ? vy : vx) > 0.f) ? 1 : -1;
+        const float2 *lay = ymajor ? layA : layB;
+        const int pitch = (ymajor ? W : H) + 2 * kPad;
+        const float pmax = (float)(ymajor ? W : H);
+        const int qmax = ymajor ? H : W;
+        const float qf = floorf(q);
+        const float fq = q - qf;
+        const int iq = (int)fminf(fmaxf(qf, -(float)kPad), (float)qmax);
+        n = min(n, sq > 0 ? qmax - iq + 1 : iq + kPad + 1);
+        const float2 *row = lay + (size_t)(iq + kPad) * pitch + kPad;
+        const long long rstep = (long long)sq * pitch;
+        float acc_lo = 0.f, acc_hi = 0.f;
+#pragma unroll 4
+        for (int j = 0; j < n; ++j) {
+            const float pf = fminf(fmaxf(floorf(p), -(float)kPad), pmax);
+            const float fp = p - pf;
+            const int ip = (int)pf;
+            const float2 lo = __ldg(row + ip);
+            const float2 hi = __ldg(row + pitch + ip);
+            acc_lo += fmaf(fp, lo.y - lo.x, lo.x);
+            acc_hi += fmaf(fp, hi.y - hi.x, hi.x);
+            p += vp;
+            row += rstep;
+        }
+        acc = fmaf(fq, acc_hi - acc_lo, acc_lo);
+    }
+    *out = acc * hypotf(vx * sx, vy * sy);
+}
+
 // ------------------------------------------------------------ 2D backward
 
 constexpr int kTexBwdRows = 4;
@@ -289,6 +374,26 @@ int launch_forward2d_tex(Plan2d &p, const float *vol, float *sino, cudaStream_t 
     if (grid.y > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     k_fwd2d_tex<<<grid, block, 0, s>>>(p.tex_vol, sino, p.d_src, p.d_u0, p.d_du, p.W, p.H, p.det,
                                        p.nangles, p.sx, p.sy);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
+int launch_forward2d_hyb(Plan2d &p, const float *vol, float *sino, cudaStream_t s) {
+    if (!p.arr_vol) {
+        int rc = alloc_array(&p.arr_vol, p.W, p.H, 0, cudaArrayDefault);
+        if (rc) return rc;
+        if ((rc = make_texture(p.arr_vol, &p.tex_vol))) return rc;
+    }
+    CG_TRY_CUDA(cudaMemcpy2DToArrayAsync(p.arr_vol, 0, 0, vol, sizeof(float) * p.W,
+                                         sizeof(float) * p.W, p.H, cudaMemcpyDeviceToDevice, s));
+    int rc = launch_relayout2d(p, vol, s);
+    if (rc) return rc;
+    dim3 block(p.fwd_bx, p.fwd_by);
+    dim3 grid(ceil_div(p.det, p.fwd_bx), ceil_div(p.nangles, p.fwd_by));
+    if (grid.y > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
+    k_fwd2d_hyb<<<grid, block, 0, s>>>(p.tex_vol, p.d_layA, p.d_layB, sino, p.d_src, p.d_u0,
+                                       p.d_du, p.W, p.H, p.det, p.nangles, p.sx, p.sy,
+                                       p.tex_eighths);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }
