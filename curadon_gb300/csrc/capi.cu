@@ -74,6 +74,13 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
         if (has("fwd3d=alu")) p3->algo_fwd = 0;
         if (has("fwd3d=tex3")) p3->algo_fwd = 1;
         if (has("fwd3d=tex2l")) p3->algo_fwd = 2;
+        const size_t at = e.find("fwd3d_block=");
+        if (at != std::string::npos) {
+            int bx = 0, by = 0, bz = 0;
+            if (std::sscanf(e.c_str() + at + 12, "%dx%dx%d", &bx, &by, &bz) == 3 && bx > 0 &&
+                by > 0 && bz > 0 && bx * by * bz <= 1024 && bx % 8 == 0)
+                p3->fwd_bx = bx, p3->fwd_by = by, p3->fwd_bz = bz;
+        }
     }
 }
 

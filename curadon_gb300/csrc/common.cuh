@@ -122,6 +122,8 @@ struct Plan3d {
 
     // forward 0 = registers, 1 = tex3D, 2 = layered bilinear + lerp
     int algo_fwd = 0, algo_bwd = 0;
+    // texture forwards: detector cells (u, v) x views per thread block
+    int fwd_bx = 32, fwd_by = 8, fwd_bz = 1;
 };
 
 void free_plan2d(Plan2d *p);

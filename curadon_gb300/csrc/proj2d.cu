@@ -3,7 +3,7 @@
 // Data layout in HBM (all float32, per plan):
 //   layA  (H+2P) rows x (W+2P) float2: layA[y][x] = (v[y][x], v[y][x+1])
 //   layB  (W+2P) rows x (H+2P) float2: layB[x][y] = (v[y][x], v[y+1][x])
-//   sinoP nangles rows x (det+2P) float2: sinoP[a][k] = (s[a][k], s[a][k+1])
+//   sinoP nangles rows x (det+2P) float2: sinoP[a][k] = (s[a][k], s[a][k+1] - s[a][k])
 // with P = kPad texels of zeros around every edge.  One 8-byte load then
 // returns both texels a linear filter needs along the contiguous axis, and a
 // warp of adjacent detector cells (forward) or adjacent pixels (backward)
@@ -21,11 +21,14 @@ namespace {
 
 // ------------------------------------------------------------ plan tables
 
-// Clockwise rotation of v by (cs, sn) about the origin, minus t; the same
-// expression as the reference's geometry::rotate (rotation.hpp:51-61) so that
-// the compiler forms the same products and roundings.
+// Clockwise rotation of v by (cs, sn) about the origin, minus t, as
+// geometry::rotate (rotation.hpp:51-61) evaluates it when the reference's
+// plan precompute is compiled: in each component the first product is
+// rounded and the second is fused with it.  Written out with fmaf so the
+// roundings do not depend on how the compiler contracts this call site
+// (checked bit for bit against the reference's tables).
 __device__ __forceinline__ float2 rotate_minus(float2 v, float cs, float sn, float2 t) {
-    return make_float2(v.x * cs + v.y * sn - t.x, -v.x * sn + v.y * cs - t.y);
+    return make_float2(fmaf(v.y, sn, v.x * cs) - t.x, fmaf(v.y, cs, -(v.x * sn)) - t.y);
 }
 
 // Per-view tables in voxel-index units, evaluated in FP32 with __cosf/__sinf
@@ -100,7 +103,7 @@ __global__ void k_relayout_sino2d(const float *__restrict__ sino, int det, int n
     const float *row = sino + (size_t)a * det;
     const float t0 = (k >= 0 && k < det) ? row[k] : 0.f;
     const float t1 = (k + 1 >= 0 && k + 1 < det) ? row[k + 1] : 0.f;
-    S[idx] = make_float2(t0, t1);
+    S[idx] = make_float2(t0, t1 - t0);
 }
 
 // ------------------------------------------------------------ forward
@@ -230,7 +233,7 @@ __global__ void __launch_bounds__(256)
                 const float kf = fminf(fmaxf(floorf(ub), -(float)kPad), kmax);
                 const float a = ub - kf;
                 const float2 t = __ldg(row + (int)kf);
-                acc[r] = fmaf(fmaf(a, t.y - t.x, t.x), w, acc[r]);
+                acc[r] = fmaf(fmaf(a, t.y, t.x), w, acc[r]);
             }
         }
     }
@@ -245,15 +248,20 @@ __global__ void __launch_bounds__(256)
 
 // ------------------------------------------------------------ backward, staged
 
+constexpr int kSmRows = 8;    // pixels per thread, 8 rows apart: 32 x 64 tiles
 constexpr int kSmViews = 32;  // views staged per pass
-constexpr int kSmWin = 96;    // pairs of one view's row staged for a tile
+constexpr int kSmWin = 128;   // pairs of one view's row staged for a tile
 
-// Same arithmetic as k_bwd2d, but per pass of 32 views each block first
-// computes, from its tile's four corner pixels, the window of detector cells
-// its pixels project to (a projective map sends the tile's convex hull to an
-// interval bounded by the corners), stages those pairs in shared memory and
-// samples them there.  A view whose window exceeds kSmWin pairs is sampled
-// from global memory instead.
+// The backprojection with each tile's detector window in shared memory.
+// Per pass of 32 views, threads 0..31 project the tile's four corner pixels
+// (a projective map sends the tile to an interval bounded by its corners),
+// the block stages that window of the difference-encoded pair row, and every
+// pixel samples it there; a view whose window exceeds kSmWin pairs is read
+// from global memory instead.  Per (pixel, view) the reference's quantities
+// (backward_2d.hpp:61-96) are formed with the per-view terms hoisted:
+//   x' + DSO = -cos Y + (-sin X + DSO),  yi = -sin SY + cos SX,
+//   w = DSD / (x' + DSO),  u = w yi + det/2,
+// then one 8-byte shared load and two FMAs.
 __global__ void __launch_bounds__(256)
     k_bwd2d_smem(float *__restrict__ vol, const float2 *__restrict__ S,
                  const float4 *__restrict__ meta, int W, int H, int det, int nangles, float sx,
@@ -262,42 +270,44 @@ __global__ void __launch_bounds__(256)
     __shared__ float4 smeta[kSmViews];
     __shared__ int skmin[kSmViews];
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int xt = blockIdx.x * 32, yt = blockIdx.y * 32;
+    const int xt = blockIdx.x * 32, yt = blockIdx.y * (8 * kSmRows);
     const int x = xt + threadIdx.x;
     const int y0 = yt + threadIdx.y;
-    const float ex = (float)W / 2.0f, ey = (float)H / 2.0f, ed = (float)det / 2.0f;
+    const float ex = (float)W / 2.0f, ey = (float)H / 2.0f;
+    const float edm = (float)det / 2.0f - 0.5f;
     const float inv = __fdividef(1.0f, ds);
     const float X = ((float)x - ex) * sx + ox + 0.5f;
     const float SX = X * inv;
-    float Y[kBwdRows], SY[kBwdRows], acc[kBwdRows];
+    float Y[kSmRows], SY[kSmRows], acc[kSmRows];
 #pragma unroll
-    for (int r = 0; r < kBwdRows; ++r) {
+    for (int r = 0; r < kSmRows; ++r) {
         Y[r] = ((float)(y0 + 8 * r) - ey) * sy + oy + 0.5f;
         SY[r] = Y[r] * inv;
         acc[r] = 0.f;
     }
     const int pitch = det + 2 * kPad;
-    const float kmax = (float)det;
     for (int v0 = 0; v0 < nangles; v0 += kSmViews) {
         const int nv = min(kSmViews, nangles - v0);
         __syncthreads();
         if (tid < nv) {
-            const float4 m = meta[v0 + tid];
+            const float4 m = meta[v0 + tid];  // (-sin, cos, DSD, DSO)
             smeta[tid] = m;
-            float lo = FLT_MAX, hi = -FLT_MAX;
+            float lo = FLT_MAX, hi = -FLT_MAX, dmin = FLT_MAX;
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 const float cX = ((float)(xt + (c & 1) * 31) - ex) * sx + ox + 0.5f;
-                const float cY = ((float)(yt + (c >> 1) * 31) - ey) * sy + oy + 0.5f;
-                const float xi = m.x * cX - m.y * cY;
-                const float yi = m.y * (cX * inv) + m.x * (cY * inv);
-                const float w = __fdividef(m.z, xi + m.w);
-                const float ub = (w * yi + ed) - 0.5f;
+                const float cY = ((float)(yt + (c >> 1) * (8 * kSmRows - 1)) - ey) * sy + oy + 0.5f;
+                const float den = fmaf(-m.y, cY, fmaf(m.x, cX, m.w));
+                const float yi = fmaf(m.x, cY * inv, m.y * (cX * inv));
+                const float ub = fmaf(__fdividef(m.z, den), yi, edm);
                 lo = fminf(lo, ub);
                 hi = fmaxf(hi, ub);
+                dmin = fminf(dmin, den);
             }
+            // the window bound holds when the tile lies wholly in front of the
+            // source (x' + DSO > 0 at every corner, hence on the whole tile)
             int k0 = INT_MIN;
-            if (lo >= -1e6f && hi <= 1e6f) {
+            if (dmin > 0.f && lo >= -1e6f && hi <= 1e6f) {
                 const int a = (int)floorf(lo) - 1, b = (int)floorf(hi) + 1;
                 if (b - a + 1 <= kSmWin) k0 = a;
             }
@@ -315,38 +325,41 @@ __global__ void __launch_bounds__(256)
         for (int j = 0; j < nv; ++j) {
             const float4 m = smeta[j];
             const int k0 = skmin[j];
+            const float A = fmaf(m.x, X, m.w), B = m.y * SX, nc = -m.y;
             if (k0 != INT_MIN) {
+                const float2 *sr = srow[j];
 #pragma unroll
-                for (int r = 0; r < kBwdRows; ++r) {
-                    const float xi = m.x * X - m.y * Y[r];
-                    const float yi = m.y * SX + m.x * SY[r];
-                    const float w = __fdividef(m.z, xi + m.w);
-                    const float ub = (w * yi + ed) - 0.5f;
+                for (int r = 0; r < kSmRows; ++r) {
+                    const float den = fmaf(nc, Y[r], A);
+                    const float yi = fmaf(m.x, SY[r], B);
+                    const float w = __fdividef(m.z, den);
+                    const float ub = fmaf(w, yi, edm);
                     const float kf = floorf(ub);
                     const float a = ub - kf;
-                    const int li = min(max((int)kf - k0, 0), kSmWin - 1);
-                    const float2 t = srow[j][li];
-                    acc[r] = fmaf(fmaf(a, t.y - t.x, t.x), w, acc[r]);
+                    const unsigned li = min((unsigned)((int)kf - k0), (unsigned)(kSmWin - 1));
+                    const float2 t = sr[li];
+                    acc[r] = fmaf(fmaf(a, t.y, t.x), w, acc[r]);
                 }
             } else {
-                const float2 *row = S + (size_t)(v0 + j) * pitch + kPad;
+                const float2 *row = S + (size_t)(v0 + j) * pitch;
 #pragma unroll
-                for (int r = 0; r < kBwdRows; ++r) {
-                    const float xi = m.x * X - m.y * Y[r];
-                    const float yi = m.y * SX + m.x * SY[r];
-                    const float w = __fdividef(m.z, xi + m.w);
-                    const float ub = (w * yi + ed) - 0.5f;
-                    const float kf = fminf(fmaxf(floorf(ub), -(float)kPad), kmax);
+                for (int r = 0; r < kSmRows; ++r) {
+                    const float den = fmaf(nc, Y[r], A);
+                    const float yi = fmaf(m.x, SY[r], B);
+                    const float w = __fdividef(m.z, den);
+                    const float ub = fmaf(w, yi, edm);
+                    const float kf = floorf(ub);
                     const float a = ub - kf;
-                    const float2 t = __ldg(row + (int)kf);
-                    acc[r] = fmaf(fmaf(a, t.y - t.x, t.x), w, acc[r]);
+                    const unsigned col = min((unsigned)((int)kf + kPad), (unsigned)(det + kPad));
+                    const float2 t = __ldg(row + col);
+                    acc[r] = fmaf(fmaf(a, t.y, t.x), w, acc[r]);
                 }
             }
         }
     }
     if (x < W) {
 #pragma unroll
-        for (int r = 0; r < kBwdRows; ++r) {
+        for (int r = 0; r < kSmRows; ++r) {
             const int y = y0 + 8 * r;
             if (y < H) vol[(size_t)y * W + x] += acc[r] * inv;
         }
@@ -392,7 +405,7 @@ int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s) {
 }
 
 int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s) {
-    dim3 grid(ceil_div(p.W, 32), ceil_div(p.H, 32));
+    dim3 grid(ceil_div(p.W, 32), ceil_div(p.H, 8 * kSmRows));
     k_bwd2d_smem<<<grid, dim3(32, 8), 0, s>>>(vol, p.d_sinoP, p.d_bmeta, p.W, p.H, p.det,
                                               p.nangles, p.sx, p.sy, p.ox, p.oy, p.ds);
     CG_TRY_CUDA(cudaGetLastError());

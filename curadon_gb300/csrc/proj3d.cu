@@ -3,7 +3,7 @@
 // Data layout in HBM (all float32, per plan, allocated on first use):
 //   volA  (Z+2P)(Y+2P)(X+2P) float2, pairs along x: (v[z][y][x], v[z][y][x+1])
 //   volB  (X+2P)(Y+2P)(Z+2P) float2, pairs along z: (v[z][y][x], v[z+1][y][x])
-//   sinoP nangles (V+2P)(U+2P) float2, pairs along u
+//   sinoP nangles (V+2P)(U+2P) float2, pairs along u as (s[u], s[u+1] - s[u])
 // with P = kPad zero texels on every face.  A warp handles 32 adjacent
 // detector cells; for a circular orbit about y those cells are spread along
 // x when the ray runs along z and along z when it runs along x, so each ray
@@ -79,7 +79,7 @@ __global__ void k_relayout_sino3d(const float *__restrict__ sino, int U, int V, 
         if (a >= 0 && a < U) t0 = row[a];
         if (a + 1 >= 0 && a + 1 < U) t1 = row[a + 1];
     }
-    S[idx] = make_float2(t0, t1);
+    S[idx] = make_float2(t0, t1 - t0);
 }
 
 // ------------------------------------------------------------ forward
@@ -180,9 +180,10 @@ struct BwdTab {
 // Blocks are visited brick by brick (2 x 8 x 8 tiles) so that the blocks
 // resident at one time cover a compact region of the volume and share the
 // detector footprint they read from L2.  Per voxel and view: the reference's
-// ray/plane intersection (backward_3d.hpp:78-94), then a bilinear sample of
-// the pair-packed projection, accumulated in registers; the volume is read
-// and written once.
+// ray/plane intersection (backward_3d.hpp:78-94) -- the ray direction is
+// stepped along z from the run's first voxel -- then a bilinear sample of the
+// difference-encoded pair-packed projection in two 8-byte loads and three
+// FMAs, accumulated in registers; the volume is read and written once.
 __global__ void __launch_bounds__(256)
     k_bwd3d(float *__restrict__ vol, const float2 *__restrict__ S,
             const float4 *__restrict__ torg, const float4 *__restrict__ tdx,
@@ -202,10 +203,12 @@ __global__ void __launch_bounds__(256)
 
     const int x = tx_ * 32 + threadIdx.x, y = ty_ * 8 + threadIdx.y, z0 = tz_ * kBZ;
     const int tid = threadIdx.y * 32 + threadIdx.x;
-    const float fx = (float)x, fy = (float)y;
+    const float fx = (float)x, fy = (float)y, fz0 = (float)z0;
     const int PU = U + 2 * kP3, PV = V + 2 * kP3;
-    const float umax = (float)U, vmax = (float)V, lo = -(float)kP3;
+    const unsigned ucap = (unsigned)(U + kP3), vcap = (unsigned)(V + kP3);
     const float num = zplane - srcz;
+    // detector coordinate minus the texel-centre half: (dir t + s) + U/2 - 1/2
+    const float su = srcx + hu - 0.5f, sv = srcy + hv - 0.5f;
 
     float acc[kBZ];
 #pragma unroll
@@ -223,28 +226,27 @@ __global__ void __launch_bounds__(256)
         if (!tile_ok) continue;
         for (int j = 0; j < nv; ++j) {
             const BwdTab tb = stab[j];
-            // P = o + x dx + y dy (+ z dz below), as the reference forms it
-            const float px = fmaf(fy, tb.dy.x, fmaf(fx, tb.dx.x, tb.o.x));
-            const float py = fmaf(fy, tb.dy.y, fmaf(fx, tb.dx.y, tb.o.y));
-            const float pz = fmaf(fy, tb.dy.z, fmaf(fx, tb.dx.z, tb.o.z));
+            // direction source -> voxel (x, y, z0), P = o + x dx + y dy + z dz
+            float dirx = fmaf(fz0, tb.dz.x, fmaf(fy, tb.dy.x, fmaf(fx, tb.dx.x, tb.o.x))) - srcx;
+            float diry = fmaf(fz0, tb.dz.y, fmaf(fy, tb.dy.y, fmaf(fx, tb.dx.y, tb.o.y))) - srcy;
+            float dirz = fmaf(fz0, tb.dz.z, fmaf(fy, tb.dy.z, fmaf(fx, tb.dx.z, tb.o.z))) - srcz;
             const float2 *plane = S + (size_t)(v0 + j) * PU * PV;
 #pragma unroll
             for (int k = 0; k < kBZ; ++k) {
-                const float fz = (float)(z0 + k);
-                const float dirx = fmaf(fz, tb.dz.x, px) - srcx;
-                const float diry = fmaf(fz, tb.dz.y, py) - srcy;
-                const float dirz = fmaf(fz, tb.dz.z, pz) - srcz;
                 const float t = __fdividef(num, dirz);
-                const float ub = (fmaf(dirx, t, srcx) + hu) - 0.5f;
-                const float vb = (fmaf(diry, t, srcy) + hv) - 0.5f;
-                const float fu = fminf(fmaxf(floorf(ub), lo), umax);
-                const float fv = fminf(fmaxf(floorf(vb), lo), vmax);
-                const float wu = ub - fu, wv = vb - fv;
-                const float2 *q = plane + ((int)fv + kP3) * PU + ((int)fu + kP3);
+                const float ub = fmaf(dirx, t, su), vb = fmaf(diry, t, sv);
+                const int iu = __float2int_rd(ub), iv = __float2int_rd(vb);
+                const float wu = ub - (float)iu, wv = vb - (float)iv;
+                const unsigned cu = min((unsigned)(iu + kP3), ucap);
+                const unsigned cv = min((unsigned)(iv + kP3), vcap);
+                const float2 *q = plane + cv * PU + cu;
                 const float2 a = __ldg(q), b = __ldg(q + PU);
-                const float l0 = fmaf(wu, a.y - a.x, a.x);
-                const float l1 = fmaf(wu, b.y - b.x, b.x);
+                const float l0 = fmaf(wu, a.y, a.x);
+                const float l1 = fmaf(wu, b.y, b.x);
                 acc[k] += fmaf(wv, l1 - l0, l0);
+                dirx += tb.dz.x;
+                diry += tb.dz.y;
+                dirz += tb.dz.z;
             }
         }
     }

@@ -290,11 +290,11 @@ __global__ void __launch_bounds__(256)
     k_fwd3d_tex3(cudaTextureObject_t tex, float *__restrict__ sino,
                  const float4 *__restrict__ torg, const float4 *__restrict__ tdu,
                  const float4 *__restrict__ tdv, const float4 *__restrict__ tsrc, int X, int Y,
-                 int Z, int U, int V) {
+                 int Z, int U, int V, int P) {
     const int iu = blockIdx.x * blockDim.x + threadIdx.x;
     const int iv = blockIdx.y * blockDim.y + threadIdx.y;
-    const int view = blockIdx.z;
-    if (iu >= U || iv >= V) return;
+    const int view = blockIdx.z * blockDim.z + threadIdx.z;
+    if (iu >= U || iv >= V || view >= P) return;
     const RaySeg r = ray3d(torg[view], tdu[view], tdv[view], tsrc[view], iu, iv, X, Y, Z);
     if (!r.hit) return;
     float acc = 0.f, t = r.tmin;
@@ -312,11 +312,11 @@ __global__ void __launch_bounds__(256)
     k_fwd3d_tex2l(cudaTextureObject_t texA, cudaTextureObject_t texB, float *__restrict__ sino,
                   const float4 *__restrict__ torg, const float4 *__restrict__ tdu,
                   const float4 *__restrict__ tdv, const float4 *__restrict__ tsrc, int X, int Y,
-                  int Z, int U, int V) {
+                  int Z, int U, int V, int P) {
     const int iu = blockIdx.x * blockDim.x + threadIdx.x;
     const int iv = blockIdx.y * blockDim.y + threadIdx.y;
-    const int view = blockIdx.z;
-    if (iu >= U || iv >= V) return;
+    const int view = blockIdx.z * blockDim.z + threadIdx.z;
+    if (iu >= U || iv >= V || view >= P) return;
     const RaySeg r = ray3d(torg[view], tdu[view], tdv[view], tsrc[view], iu, iv, X, Y, Z);
     if (!r.hit) return;
     // layered along the ray's dominant horizontal axis
@@ -419,8 +419,9 @@ int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t
 }
 
 int launch_forward3d_tex(Plan3d &p, const float *vol, float *sino, cudaStream_t s) {
-    if (p.nangles > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
-    dim3 grid(ceil_div(p.U, 32), ceil_div(p.V, 8), p.nangles);
+    const dim3 block(p.fwd_bx, p.fwd_by, p.fwd_bz);
+    const dim3 grid(ceil_div(p.U, p.fwd_bx), ceil_div(p.V, p.fwd_by), ceil_div(p.nangles, p.fwd_bz));
+    if (grid.z > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     if (p.algo_fwd == 1) {
         if (!p.arr3) {
             int rc = alloc_array(&p.arr3, p.X, p.Y, p.Z, cudaArrayDefault);
@@ -429,8 +430,8 @@ int launch_forward3d_tex(Plan3d &p, const float *vol, float *sino, cudaStream_t 
         }
         int rc = copy_to_array(p.arr3, vol, p.X, p.Y, p.Z, s);
         if (rc) return rc;
-        k_fwd3d_tex3<<<grid, dim3(32, 8), 0, s>>>(p.tex3, sino, p.d_forg, p.d_fdu, p.d_fdv,
-                                                  p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V);
+        k_fwd3d_tex3<<<grid, block, 0, s>>>(p.tex3, sino, p.d_forg, p.d_fdu, p.d_fdv, p.d_fsrc,
+                                            p.X, p.Y, p.Z, p.U, p.V, p.nangles);
         CG_TRY_CUDA(cudaGetLastError());
         return CG_OK;
     }
@@ -448,8 +449,8 @@ int launch_forward3d_tex(Plan3d &p, const float *vol, float *sino, cudaStream_t 
         vol, p.d_volT, p.X, p.Y, p.Z);
     CG_TRY_CUDA(cudaGetLastError());
     if ((rc = copy_to_array(p.arrB, p.d_volT, p.Z, p.Y, p.X, s))) return rc;
-    k_fwd3d_tex2l<<<grid, dim3(32, 8), 0, s>>>(p.texA, p.texB, sino, p.d_forg, p.d_fdu, p.d_fdv,
-                                               p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V);
+    k_fwd3d_tex2l<<<grid, block, 0, s>>>(p.texA, p.texB, sino, p.d_forg, p.d_fdu, p.d_fdv,
+                                         p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V, p.nangles);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }

@@ -42,10 +42,19 @@ def run_bwd(geom, sino, dev, vol0):
 
 
 def check_fwd(s, ref):
-    missed = ref == SENTINEL
-    assert np.array_equal(missed, s == SENTINEL), "miss pattern differs"
-    e = rel_l2(s[~missed], ref[~missed])
-    print(f"fwd rel-L2 {e:.2e} max-abs {max_abs(s[~missed], ref[~missed]):.2e}")
+    """Same written/unwritten pattern as the reference and rel-L2 <= TOL.
+
+    A ray that only grazes the box [-1, N+1]^3 can flip between hit and miss
+    on the last bit of its slab test; it touches only the zero border, so
+    where one side wrote it the value is exactly 0.  Such flips are allowed
+    at a rate of at most one ray per million."""
+    miss_ref, miss = ref == SENTINEL, s == SENTINEL
+    flip = miss_ref != miss
+    assert flip.sum() <= max(2, 1e-6 * flip.size), f"{flip.sum()} rays differ in hit/miss"
+    assert np.all(ref[flip & ~miss_ref] == 0) and np.all(s[flip & ~miss] == 0)
+    both = ~miss_ref & ~miss
+    e = rel_l2(s[both], ref[both])
+    print(f"fwd rel-L2 {e:.2e} max-abs {max_abs(s[both], ref[both]):.2e} flips {flip.sum()}")
     assert e < TOL
 
 
