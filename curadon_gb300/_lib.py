@@ -41,6 +41,9 @@ SIGNATURES = [
     ("cg_backward_3d", C.c_int,
      [C.c_void_p, u64p, f32p, f32p, C.c_void_p, f32p, f32p, f32p, C.c_uint64, u64p, f32p, f32p,
       f32p, C.c_float, C.c_float, C.c_float, C.c_void_p]),
+    ("cg_backward_2d_static", C.c_int,
+     [C.c_void_p, C.c_void_p, u64p, f32p, f32p, C.c_uint64, C.c_float, f32p, f32p, f32p,
+      C.c_uint64, C.c_void_p]),
     ("cg_filter_rows", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64, C.c_float,
       C.c_void_p]),

@@ -148,6 +148,25 @@ int cg_backward_3d(float *x, const uint64_t vol_shape[3], const float vol_spacin
                    const float det_offset[2], const float det_rotation[3], float DSO, float DSD,
                    float COR, void *stream);
 
+/* 2D backprojection that allocates nothing, for callers that cannot call
+ * cudaMalloc (a server whose device memory is reserved up front by its own
+ * pool, a real-time loop that must not wait on or fail in the allocator, a
+ * plugin host that forbids allocations by the libraries it loads).  It has no
+ * counterpart in the reference.  Same result as cg_plan2d_create +
+ * cg_backward_2d on the same arguments (plan_2d's geometry without
+ * det_offset, which the backprojection does not use), accumulating into
+ * `volume`; all scratch lives in one 16 MiB device array that the library
+ * holds on every GPU that loads it, so problems needing more --
+ * nangles * (det_count + 4) * 8 bytes plus 60 bytes per view -- are rejected
+ * with CG_ERR_INVALID.  The first call on a device looks the array up (make
+ * it before any stream capture).  All calls share the array: calls that
+ * overlap on the GPU race and must be ordered by the caller. */
+int cg_backward_2d_static(float *volume, const float *sinogram, const uint64_t vol_shape[2],
+                          const float vol_spacing[2], const float vol_offset[2],
+                          uint64_t det_count, float det_spacing, const float *DSO,
+                          const float *DSD, const float *angles, uint64_t nangles,
+                          void *stream);
+
 /* ----------------------------------------------------------------- FBP -- */
 
 /* Row filter of filtered backprojection: out[r][k] = scale * sum_j
