@@ -24,6 +24,8 @@ SIGNATURES = [
     ("cg_plan2d_destroy", C.c_int, [C.c_void_p]),
     ("cg_plan2d_get_forward_block", C.c_int, [C.c_void_p, u64p, u64p]),
     ("cg_plan2d_set_forward_block", C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64]),
+    ("cg_plan2d_set_algorithm", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    ("cg_plan2d_get_algorithm", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("cg_plan2d_tables", C.c_int, [C.c_void_p, f32p, f32p, f32p]),
     ("cg_forward_2d", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cg_backward_2d", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -32,6 +34,8 @@ SIGNATURES = [
      [C.POINTER(C.c_void_p), C.c_int, u64p, f32p, f32p, f32p, f32p, f32p, C.c_uint64, u64p, f32p,
       f32p, f32p, C.c_float, C.c_float, C.c_float]),
     ("cg_plan3d_destroy", C.c_int, [C.c_void_p]),
+    ("cg_plan3d_set_algorithm", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    ("cg_plan3d_get_algorithm", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("cg_forward_3d_plan", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cg_backward_3d_plan", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cg_adjoint_3d_plan", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -39,6 +39,20 @@ def _stream(t: torch.Tensor) -> C.c_void_p:
     return C.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
 
 
+FORWARD_2D = ("registers", "texture", "hybrid", "slab")
+BACKWARD_2D = ("registers", "texture", "shared")
+FORWARD_3D = ("registers", "texture", "layered")
+BACKWARD_3D = ("registers",)
+
+
+def _algo_index(name, names, what):
+    if name is None:
+        return -1
+    if name not in names:
+        raise ValueError(f"{what} algorithm must be one of {names}, got {name!r}")
+    return names.index(name)
+
+
 def _check_tensor(t, name: str, ndim: int | None = None):
     if not isinstance(t, torch.Tensor):
         raise TypeError(f"{name} must be a torch.Tensor")
@@ -115,6 +129,19 @@ class plan_2d:
     @forward_block_y.setter
     def forward_block_y(self, v):
         check(self._L.cg_plan2d_set_forward_block(self._h, self._block()[0], int(v)))
+
+    @property
+    def algorithm(self):
+        """(forward, backward) algorithm names of this plan."""
+        f, b = C.c_int(), C.c_int()
+        check(self._L.cg_plan2d_get_algorithm(self._h, C.byref(f), C.byref(b)))
+        return FORWARD_2D[f.value], BACKWARD_2D[b.value]
+
+    def set_algorithm(self, forward=None, backward=None):
+        """Selects the algorithms (names from FORWARD_2D / BACKWARD_2D)."""
+        check(self._L.cg_plan2d_set_algorithm(
+            self._h, _algo_index(forward, FORWARD_2D, "forward"),
+            _algo_index(backward, BACKWARD_2D, "backward")))
 
     def tables(self):
         """(sources, u_origins, delta_us), each (nangles, 2) float32."""
@@ -193,6 +220,17 @@ class plan_3d:
     @property
     def handle(self):
         return self._h
+
+    @property
+    def algorithm(self):
+        f, b = C.c_int(), C.c_int()
+        check(self._L.cg_plan3d_get_algorithm(self._h, C.byref(f), C.byref(b)))
+        return FORWARD_3D[f.value], BACKWARD_3D[b.value]
+
+    def set_algorithm(self, forward=None, backward=None):
+        check(self._L.cg_plan3d_set_algorithm(
+            self._h, _algo_index(forward, FORWARD_3D, "forward"),
+            _algo_index(backward, BACKWARD_3D, "backward")))
 
     def _check(self, vol, sino):
         _check_tensor(vol, "volume", 3)

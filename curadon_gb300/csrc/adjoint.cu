@@ -23,7 +23,7 @@ __global__ void __launch_bounds__(256)
     k_adj2d(float2 *__restrict__ accA, float2 *__restrict__ accB, const float *__restrict__ sino,
             const float2 *__restrict__ tsrc, const float2 *__restrict__ tu0,
             const float2 *__restrict__ tdu, int W, int H, int det, int nangles, float sx,
-            float sy) {
+            float sy, int pa, int pb) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     const int view = blockIdx.y * blockDim.y + threadIdx.y;
     if (u >= det || view >= nangles) return;
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256)
     const float q = (ymajor ? roy : rox) - 0.5f;
     const int sq = ((ymajor ? vy : vx) > 0.f) ? 1 : -1;
     float2 *acc = ymajor ? accA : accB;
-    const int pitch = (ymajor ? W : H) + 2 * kPad;
+    const int pitch = ymajor ? pa : pb;
     const float pmax = (float)(ymajor ? W : H);
     const int qmax = ymajor ? H : W;
     const float qf = floorf(q);
@@ -82,11 +82,10 @@ __global__ void __launch_bounds__(256)
 
 // vol[y][x] += A[y][x].x + A[y][x-1].y + B[x][y].x + B[x][y-1].y (padded).
 __global__ void k_fold2d(float *__restrict__ vol, const float2 *__restrict__ A,
-                         const float2 *__restrict__ B, int W, int H) {
+                         const float2 *__restrict__ B, int W, int H, int pa, int pb) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= W || y >= H) return;
-    const int pa = W + 2 * kPad, pb = H + 2 * kPad;
     const float2 *ra = A + (size_t)(y + kPad) * pa + kPad;
     const float2 *rb = B + (size_t)(x + kPad) * pb + kPad;
     vol[(size_t)y * W + x] += (ra[x].x + ra[x - 1].y) + (rb[y].x + rb[y - 1].y);
@@ -186,10 +185,10 @@ int launch_adjoint2d(const Plan2d &p, float *vol, const float *sino, cudaStream_
     dim3 grid(ceil_div(p.det, p.fwd_bx), ceil_div(p.nangles, p.fwd_by));
     if (grid.y > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     k_adj2d<<<grid, block, 0, s>>>(p.d_layA, p.d_layB, sino, p.d_src, p.d_u0, p.d_du, p.W, p.H,
-                                   p.det, p.nangles, p.sx, p.sy);
+                                   p.det, p.nangles, p.sx, p.sy, p.pitchA(), p.pitchB());
     CG_TRY_CUDA(cudaGetLastError());
     k_fold2d<<<dim3(ceil_div(p.W, 32), ceil_div(p.H, 8)), dim3(32, 8), 0, s>>>(
-        vol, p.d_layA, p.d_layB, p.W, p.H);
+        vol, p.d_layA, p.d_layB, p.W, p.H, p.pitchA(), p.pitchB());
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }

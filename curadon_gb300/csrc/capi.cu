@@ -62,6 +62,7 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
     if (p2) {
         if (has("fwd2d=alu")) p2->algo_fwd = 0;
         if (has("fwd2d=tex")) p2->algo_fwd = 1;
+        if (has("fwd2d=slab")) p2->algo_fwd = 3;
         for (int k = 1; k < 8; ++k) {
             const std::string key = "fwd2d=hyb" + std::to_string(k);
             if (has(key.c_str())) p2->algo_fwd = 2, p2->tex_eighths = k;
@@ -409,6 +410,23 @@ int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by) {
     return CG_OK;
 }
 
+int cg_plan2d_set_algorithm(cg_plan2d *plan, int forward, int backward) {
+    clear_error();
+    CG_REQUIRE(plan, "plan is NULL");
+    CG_REQUIRE(forward >= -1 && forward <= 3, "2D forward algorithm must be -1..3");
+    CG_REQUIRE(backward >= -1 && backward <= 2, "2D backward algorithm must be -1..2");
+    if (forward >= 0) plan->algo_fwd = forward;
+    if (backward >= 0) plan->algo_bwd = backward;
+    return CG_OK;
+}
+
+int cg_plan2d_get_algorithm(const cg_plan2d *plan, int *forward, int *backward) {
+    clear_error();
+    CG_REQUIRE(plan && forward && backward, "NULL argument");
+    *forward = plan->algo_fwd, *backward = plan->algo_bwd;
+    return CG_OK;
+}
+
 int cg_plan2d_tables(const cg_plan2d *plan, float *sources, float *u_origins, float *delta_us) {
     clear_error();
     CG_REQUIRE(plan, "plan is NULL");
@@ -431,6 +449,8 @@ int cg_forward_2d(cg_plan2d *plan, const float *volume, float *sinogram, void *s
     if (plan->algo_fwd == 2) return launch_forward2d_hyb(*plan, volume, sinogram, s);
     int rc = launch_relayout2d(*plan, volume, s);
     if (rc) return rc;
+    if (plan->algo_fwd == 3 && slab_supported(*plan))
+        return launch_forward2d_slab(*plan, sinogram, s);
     return launch_forward2d(*plan, sinogram, s);
 }
 
@@ -466,6 +486,23 @@ int cg_plan3d_create(cg_plan3d **plan, int device, const uint64_t vol_shape[3],
     clear_error();
     return make_plan3d(plan, device, vol_shape, vol_spacing, vol_offset, phi, theta, psi, nangles,
                        det_shape, det_spacing, det_offset, det_rotation, DSO, DSD, COR);
+}
+
+int cg_plan3d_set_algorithm(cg_plan3d *plan, int forward, int backward) {
+    clear_error();
+    CG_REQUIRE(plan, "plan is NULL");
+    CG_REQUIRE(forward >= -1 && forward <= 2, "3D forward algorithm must be -1..2");
+    CG_REQUIRE(backward >= -1 && backward <= 0, "3D backward algorithm must be -1..0");
+    if (forward >= 0) plan->algo_fwd = forward;
+    if (backward >= 0) plan->algo_bwd = backward;
+    return CG_OK;
+}
+
+int cg_plan3d_get_algorithm(const cg_plan3d *plan, int *forward, int *backward) {
+    clear_error();
+    CG_REQUIRE(plan && forward && backward, "NULL argument");
+    *forward = plan->algo_fwd, *backward = plan->algo_bwd;
+    return CG_OK;
 }
 
 int cg_plan3d_destroy(cg_plan3d *plan) {

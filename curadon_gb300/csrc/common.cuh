@@ -78,21 +78,24 @@ struct Plan2d {
     float4 *d_bmeta = nullptr;        // (-sin, cos, DSD, DSO)
 
     // scratch (device)
-    float2 *d_layA = nullptr;         // (H+2P) x (W+2P) pairs along x
-    float2 *d_layB = nullptr;         // (W+2P) x (H+2P) pairs along y
+    float2 *d_layA = nullptr;         // (H+2P) rows x pitchA() pairs along x
+    float2 *d_layB = nullptr;         // (W+2P) rows x pitchB() pairs along y
     float2 *d_sinoP = nullptr;        // nangles x (det+2P) pairs along u
 
     // texture-unit variants (allocated on first use)
     cudaArray_t arr_vol = nullptr, arr_sino = nullptr;
     cudaTextureObject_t tex_vol = 0, tex_sino = 0;
 
-    // algorithm per operator: forward 0 = registers, 1 = texture unit;
-    // backprojection 0 = registers, 1 = texture unit, 2 = shared-memory rows
-    int algo_fwd = 0, algo_bwd = 0;
+    // algorithm per operator: forward 0 = registers, 1 = texture unit,
+    // 2 = texture + registers, 3 = shared-memory row slabs;
+    // backprojection 0 = registers, 1 = texture unit, 2 = shared-memory rows.
+    // Defaults: the fastest measured on GB300 (2D n-sweep).
+    int algo_fwd = 1, algo_bwd = 2;
     int tex_eighths = 4;              // hybrid forward: share of warps on the texture unit
 
-    int pitchA() const { return W + 2 * kPad; }
-    int pitchB() const { return H + 2 * kPad; }
+    // row pitches of layA / layB in pairs, even so every row starts on 16 bytes
+    int pitchA() const { return (W + 2 * kPad + 1) & ~1; }
+    int pitchB() const { return (H + 2 * kPad + 1) & ~1; }
     int pitchS() const { return det + 2 * kPad; }
 };
 
@@ -120,10 +123,11 @@ struct Plan3d {
     cudaTextureObject_t tex3 = 0, texA = 0, texB = 0;
     float *d_volT = nullptr;          // x<->z transposed volume for arrB
 
-    // forward 0 = registers, 1 = tex3D, 2 = layered bilinear + lerp
-    int algo_fwd = 0, algo_bwd = 0;
+    // forward 0 = registers, 1 = tex3D, 2 = layered bilinear + lerp;
+    // defaults: the fastest measured on GB300 (256^3 and 512^3 workloads)
+    int algo_fwd = 1, algo_bwd = 0;
     // texture forwards: detector cells (u, v) x views per thread block
-    int fwd_bx = 32, fwd_by = 8, fwd_bz = 1;
+    int fwd_bx = 8, fwd_by = 4, fwd_bz = 8;
 };
 
 void free_plan2d(Plan2d *p);
@@ -145,6 +149,8 @@ int launch_adjoint2d(const Plan2d &p, float *vol, const float *sino, cudaStream_
 int launch_adjoint3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s);
 
 int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s);
+bool slab_supported(const Plan2d &p);
+int launch_forward2d_slab(const Plan2d &p, float *sino, cudaStream_t s);
 int launch_forward2d_tex(Plan2d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_forward2d_hyb(Plan2d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t s);

@@ -1,16 +1,19 @@
 // proj2d.cu -- 2D fan-beam projection kernels for sm_103a.
 //
 // Data layout in HBM (all float32, per plan):
-//   layA  (H+2P) rows x (W+2P) float2: layA[y][x] = (v[y][x], v[y][x+1])
-//   layB  (W+2P) rows x (H+2P) float2: layB[x][y] = (v[y][x], v[y+1][x])
+//   layA  (H+2P) rows x pitchA float2: layA[y][x] = (v[y][x], v[y][x+1] - v[y][x])
+//   layB  (W+2P) rows x pitchB float2: layB[x][y] = (v[y][x], v[y+1][x] - v[y][x])
 //   sinoP nangles rows x (det+2P) float2: sinoP[a][k] = (s[a][k], s[a][k+1] - s[a][k])
-// with P = kPad texels of zeros around every edge.  One 8-byte load then
-// returns both texels a linear filter needs along the contiguous axis, and a
+// with P = kPad texels of zeros around every edge (pitches rounded up to an
+// even number of pairs so rows start on 16 bytes).  One 8-byte load then
+// returns what a linear filter needs along the contiguous axis (the value and
+// the difference to its neighbour, so the lerp is a single FMA), and a
 // warp of adjacent detector cells (forward) or adjacent pixels (backward)
 // reads consecutive addresses whatever the view angle: rays that advance
 // along y read layA, rays that advance along x read the transposed layB.
 // Interpolation is FP32 in registers (no texture unit); clamping a texel
 // index into the zero padding reproduces cudaAddressModeBorder.
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 
@@ -23,12 +26,13 @@ namespace {
 
 // Clockwise rotation of v by (cs, sn) about the origin, minus t, as
 // geometry::rotate (rotation.hpp:51-61) evaluates it when the reference's
-// plan precompute is compiled: in each component the first product is
-// rounded and the second is fused with it.  Written out with fmaf so the
-// roundings do not depend on how the compiler contracts this call site
-// (checked bit for bit against the reference's tables).
+// plan precompute is compiled: x = fma(v.x, cs, v.y sn) - t.x (the sum of
+// two products fuses the first), y = fma(v.y, cs, -(v.x sn)) - t.y (the
+// negated product becomes a subtraction that fuses the other).  Written out
+// with fmaf so the roundings do not depend on how the compiler contracts
+// this call site; checked bit for bit against the reference's tables.
 __device__ __forceinline__ float2 rotate_minus(float2 v, float cs, float sn, float2 t) {
-    return make_float2(fmaf(v.y, sn, v.x * cs) - t.x, fmaf(v.y, cs, -(v.x * sn)) - t.y);
+    return make_float2(fmaf(v.x, cs, v.y * sn) - t.x, fmaf(v.y, cs, -(v.x * sn)) - t.y);
 }
 
 // Per-view tables in voxel-index units, evaluated in FP32 with __cosf/__sinf
@@ -70,7 +74,7 @@ constexpr int kTile = 32;
 // Writes layA and layB for one 32 x 32 tile of padded texel space.
 __global__ void __launch_bounds__(256)
     k_relayout2d(const float *__restrict__ vol, int W, int H, float2 *__restrict__ A,
-                 float2 *__restrict__ B) {
+                 float2 *__restrict__ B, int pa, int pb) {
     __shared__ float tile[kTile + 1][kTile + 1];
     const int x0 = blockIdx.x * kTile - kPad, y0 = blockIdx.y * kTile - kPad;
     for (int j = threadIdx.y; j < kTile + 1; j += blockDim.y)
@@ -79,17 +83,18 @@ __global__ void __launch_bounds__(256)
             tile[j][i] = (x >= 0 && x < W && y >= 0 && y < H) ? vol[(size_t)y * W + x] : 0.f;
         }
     __syncthreads();
-    const int pa = W + 2 * kPad, pb = H + 2 * kPad;
     const int tx = threadIdx.x;
     for (int j = threadIdx.y; j < kTile; j += blockDim.y) {
         const int y = y0 + j, x = x0 + tx;
         if (y < H + kPad && x < W + kPad)
-            A[(size_t)(y + kPad) * pa + (x + kPad)] = make_float2(tile[j][tx], tile[j][tx + 1]);
+            A[(size_t)(y + kPad) * pa + (x + kPad)] =
+                make_float2(tile[j][tx], tile[j][tx + 1] - tile[j][tx]);
     }
     for (int i = threadIdx.y; i < kTile; i += blockDim.y) {
         const int x = x0 + i, y = y0 + tx;
         if (x < W + kPad && y < H + kPad)
-            B[(size_t)(x + kPad) * pb + (y + kPad)] = make_float2(tile[tx][i], tile[tx + 1][i]);
+            B[(size_t)(x + kPad) * pb + (y + kPad)] =
+                make_float2(tile[tx][i], tile[tx + 1][i] - tile[tx][i]);
     }
 }
 
@@ -117,7 +122,7 @@ __global__ void __launch_bounds__(256)
     k_fwd2d(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
             float *__restrict__ sino, const float2 *__restrict__ tsrc,
             const float2 *__restrict__ tu0, const float2 *__restrict__ tdu, int W, int H,
-            int det, int nangles, float sx, float sy) {
+            int det, int nangles, float sx, float sy, int pa, int pb) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     const int view = blockIdx.y * blockDim.y + threadIdx.y;
     if (u >= det || view >= nangles) return;
@@ -155,7 +160,7 @@ __global__ void __launch_bounds__(256)
     const float q = (ymajor ? roy : rox) - 0.5f;
     const int sq = ((ymajor ? vy : vx) > 0.f) ? 1 : -1;
     const float2 *lay = ymajor ? layA : layB;
-    const int pitch = (ymajor ? W : H) + 2 * kPad;
+    const int pitch = ymajor ? pa : pb;
     const float pmax = (float)(ymajor ? W : H);
     const int qmax = ymajor ? H : W;
 
@@ -174,14 +179,219 @@ __global__ void __launch_bounds__(256)
         const int ip = (int)pf;
         const float2 lo = __ldg(row + ip);
         const float2 hi = __ldg(row + pitch + ip);
-        acc_lo += fmaf(fp, lo.y - lo.x, lo.x);
-        acc_hi += fmaf(fp, hi.y - hi.x, hi.x);
+        acc_lo += fmaf(fp, lo.y, lo.x);
+        acc_hi += fmaf(fp, hi.y, hi.x);
         p += vp;
         row += rstep;
     }
     const float acc = fmaf(fq, acc_hi - acc_lo, acc_lo);
     *out = acc * hypotf(vx * sx, vy * sy);
 }
+
+// ------------------------------------------------------------ forward, slab
+
+constexpr int kSlabThreads = 1024;
+constexpr int kSlabRing = 3;  // staged rows: r, r+1 in use, r+2 in flight
+
+// Ray set-up shared by the slab kernel's two passes: the reference's FP32
+// sequence (forward_2d.hpp:52-68, intersection.h:31-46).  Returns false for a
+// ray that misses the box.
+struct FanRay {
+    float p, vp, q, fq, nrm;
+    int n, sq;
+    bool ymajor;
+};
+
+__device__ __forceinline__ bool fan_ray(const float2 s, const float2 o, const float2 du, int u,
+                                        int W, int H, float sx, float sy, FanRay &r) {
+    const float fu = (float)u;
+    const float dx = fmaf(du.x, fu, o.x);
+    const float dy = fmaf(du.y, fu, o.y);
+    float tmin = FLT_MIN, tmax = FLT_MAX;
+    {
+        const float t1 = __fdividef(-1.f - s.x, dx), t2 = __fdividef((float)W - s.x, dx);
+        tmin = fminf(fmaxf(t1, tmin), fmaxf(t2, tmin));
+        tmax = fmaxf(fminf(t1, tmax), fminf(t2, tmax));
+    }
+    {
+        const float t1 = __fdividef(-1.f - s.y, dy), t2 = __fdividef((float)H - s.y, dy);
+        tmin = fminf(fmaxf(t1, tmin), fmaxf(t2, tmin));
+        tmax = fmaxf(fminf(t1, tmax), fminf(t2, tmax));
+    }
+    if ((double)tmin > (double)tmax - 1e-6) return false;
+    const float rox = fmaf(dx, tmin, s.x), roy = fmaf(dy, tmin, s.y);
+    const float tl = tmax - tmin;
+    const float rdx = dx * tl, rdy = dy * tl;
+    const float m = fmaxf(fabsf(rdx), fabsf(rdy));
+    const float vx = rdx / m, vy = rdy / m;
+    r.n = __float2int_rn(m);
+    r.ymajor = fabsf(rdy) >= fabsf(rdx);
+    r.p = (r.ymajor ? rox : roy) - 0.5f;
+    r.vp = r.ymajor ? vx : vy;
+    r.q = (r.ymajor ? roy : rox) - 0.5f;
+    r.sq = ((r.ymajor ? vy : vx) > 0.f) ? 1 : -1;
+    r.fq = r.q - floorf(r.q);
+    r.nrm = hypotf(vx * sx, vy * sy);
+    return true;
+}
+
+// Row-synchronous forward projection.  Block = (group of G views) x (ray
+// class: y-stepping rays on layA when blockIdx.y == 0, x-stepping rays on
+// layB when 1); thread t owns the rays of cells t, t + 1024, ... of each view
+// of the group, RPV per view.  The block walks the rows of its layout in
+// order; each padded row of pairs is copied into a 3-slot shared-memory ring
+// with 16-byte cp.async (one row ahead of use), and every ray active on row r
+// takes its sample from rows r and r + 1 there: two conflict-free 8-byte
+// shared loads and two FMAs.  A ray's row range is the reference's
+// rint(max|rd|) unit steps from its entry row; rays stepping towards smaller
+// rows are visited in the opposite order (same samples, summed backwards).
+// Rays that miss the box are written as 0 by the class-0 block.
+template <int RPV, int G>
+__global__ void __launch_bounds__(kSlabThreads, 1)
+    k_fwd2d_slab(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
+                 float *__restrict__ sino, const float2 *__restrict__ tsrc,
+                 const float2 *__restrict__ tu0, const float2 *__restrict__ tdu, int W, int H,
+                 int det, int nangles, float sx, float sy, int pa, int pb) {
+    extern __shared__ __align__(16) float2 ring[];  // kSlabRing x pitch
+    __shared__ int s_rmin, s_rmax;
+    constexpr int R = RPV * G;
+    const bool cls_y = blockIdx.y == 0;
+    const float2 *lay = cls_y ? layA : layB;
+    const int pitch = cls_y ? pa : pb;
+    const int qmax = cls_y ? H : W;   // rows of the layout run over [-kPad, qmax + 1]
+    const unsigned pcap = (unsigned)((cls_y ? W : H) + kPad);
+    const int v0 = blockIdx.x * G;
+
+    if (threadIdx.x == 0) s_rmin = INT_MAX, s_rmax = INT_MIN;
+    __syncthreads();
+
+    float p[R], V[R], alo[R], ahi[R];
+    int rlo[R], len[R];
+    int my_min = INT_MAX, my_max = INT_MIN;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int view = v0 + i / RPV, u = threadIdx.x + (i % RPV) * kSlabThreads;
+        alo[i] = ahi[i] = 0.f;
+        len[i] = 0;
+        rlo[i] = 0;
+        p[i] = V[i] = 0.f;
+        if (view >= nangles || u >= det) continue;
+        FanRay r;
+        if (!fan_ray(tsrc[view], tu0[view], tdu[view], u, W, H, sx, sy, r)) continue;
+        if (r.ymajor != cls_y) continue;
+        const int iq = (int)fminf(fmaxf(floorf(r.q), -(float)kPad), (float)qmax);
+        const int n = min(r.n, r.sq > 0 ? qmax - iq + 1 : iq + kPad + 1);
+        if (n <= 0) continue;
+        const int lo = r.sq > 0 ? iq : iq - (n - 1);
+        V[i] = r.sq > 0 ? r.vp : -r.vp;
+        // position at row `lo`: the entry point for forward-stepping rays,
+        // the last sample for backward-stepping ones
+        p[i] = r.sq > 0 ? r.p : fmaf((float)(n - 1), r.vp, r.p);
+        rlo[i] = lo;
+        len[i] = n;
+        my_min = min(my_min, lo);
+        my_max = max(my_max, lo + n - 1);
+    }
+    if (my_min <= my_max) {
+        atomicMin(&s_rmin, my_min);
+        atomicMax(&s_rmax, my_max);
+    }
+    __syncthreads();
+    const int rmin = s_rmin, rmax = s_rmax;
+
+    if (rmin <= rmax) {
+        // rows rmin .. rmax + 1 are read; row index q lives at padded q + kPad
+        const int chunks = pitch / 2;  // 16-byte chunks per row
+        auto stage = [&](int row) {
+            if (row > qmax + 1) return;
+            const float4 *src =
+                reinterpret_cast<const float4 *>(lay + (size_t)(row + kPad) * pitch);
+            float4 *dst = reinterpret_cast<float4 *>(ring + ((row - rmin) % kSlabRing) * pitch);
+            for (int c = threadIdx.x; c < chunks; c += kSlabThreads) {
+                const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + c);
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa),
+                             "l"(src + c));
+            }
+        };
+        stage(rmin);
+        stage(rmin + 1);
+        asm volatile("cp.async.commit_group;\n" ::);
+        for (int r = rmin; r <= rmax; ++r) {
+            asm volatile("cp.async.wait_group 0;\n" ::);
+            __syncthreads();
+            stage(r + 2);
+            asm volatile("cp.async.commit_group;\n" ::);
+            const float2 *rowlo = ring + ((r - rmin) % kSlabRing) * pitch;
+            const float2 *rowhi = ring + ((r + 1 - rmin) % kSlabRing) * pitch;
+#pragma unroll
+            for (int i = 0; i < R; ++i) {
+                if ((unsigned)(r - rlo[i]) < (unsigned)len[i]) {
+                    const float pf = floorf(p[i]);
+                    const float fp = p[i] - pf;
+                    const unsigned ip = min((unsigned)((int)pf + kPad), pcap);
+                    const float2 lo = rowlo[ip], hi = rowhi[ip];
+                    alo[i] += fmaf(fp, lo.y, lo.x);
+                    ahi[i] += fmaf(fp, hi.y, hi.x);
+                    p[i] += V[i];
+                }
+            }
+        }
+        asm volatile("cp.async.wait_group 0;\n" ::);
+    }
+
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int view = v0 + i / RPV, u = threadIdx.x + (i % RPV) * kSlabThreads;
+        if (view >= nangles || u >= det) continue;
+        FanRay r;
+        float out;
+        if (!fan_ray(tsrc[view], tu0[view], tdu[view], u, W, H, sx, sy, r)) {
+            if (!cls_y) continue;
+            out = 0.f;
+        } else {
+            if (r.ymajor != cls_y) continue;
+            out = fmaf(r.fq, ahi[i] - alo[i], alo[i]) * r.nrm;
+        }
+        sino[(size_t)view * det + u] = out;
+    }
+}
+
+template <int RPV, int G>
+int launch_slab(const Plan2d &p, float *sino, cudaStream_t s) {
+    const int pitch = max(p.pitchA(), p.pitchB());
+    const size_t smem = sizeof(float2) * (size_t)kSlabRing * pitch;
+    CG_TRY_CUDA(cudaFuncSetAttribute(k_fwd2d_slab<RPV, G>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid(ceil_div(p.nangles, G), 2);
+    k_fwd2d_slab<RPV, G><<<grid, kSlabThreads, smem, s>>>(
+        p.d_layA, p.d_layB, sino, p.d_src, p.d_u0, p.d_du, p.W, p.H, p.det, p.nangles, p.sx,
+        p.sy, p.pitchA(), p.pitchB());
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
+}  // namespace
+
+// True when the slab forward supports the plan's sizes.
+bool slab_supported(const Plan2d &p) {
+    const size_t smem = sizeof(float2) * kSlabRing * (size_t)std::max(p.pitchA(), p.pitchB());
+    return p.det <= 6 * kSlabThreads && smem <= 200 * 1024;
+}
+
+int launch_forward2d_slab(const Plan2d &p, float *sino, cudaStream_t s) {
+    const int rpv = ceil_div(p.det, kSlabThreads);
+    switch (rpv) {
+        case 1: return launch_slab<1, 4>(p, sino, s);
+        case 2: return launch_slab<2, 3>(p, sino, s);
+        case 3: return launch_slab<3, 2>(p, sino, s);
+        case 4: return launch_slab<4, 1>(p, sino, s);
+        case 5: return launch_slab<5, 1>(p, sino, s);
+        case 6: return launch_slab<6, 1>(p, sino, s);
+        default: return set_error(CG_ERR_INVALID, "detector too wide for the slab forward");
+    }
+}
+
+namespace {
 
 // ------------------------------------------------------------ backward
 
@@ -382,7 +592,8 @@ int launch_plan2d_tables(Plan2d &p, cudaStream_t s) {
 
 int launch_relayout2d(const Plan2d &p, const float *vol, cudaStream_t s) {
     dim3 grid(ceil_div(p.W + 2 * kPad, kTile), ceil_div(p.H + 2 * kPad, kTile));
-    k_relayout2d<<<grid, dim3(32, 8), 0, s>>>(vol, p.W, p.H, p.d_layA, p.d_layB);
+    k_relayout2d<<<grid, dim3(32, 8), 0, s>>>(vol, p.W, p.H, p.d_layA, p.d_layB, p.pitchA(),
+                                              p.pitchB());
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }
@@ -392,7 +603,7 @@ int launch_forward2d(const Plan2d &p, float *sino, cudaStream_t s) {
     dim3 grid(ceil_div(p.det, p.fwd_bx), ceil_div(p.nangles, p.fwd_by));
     if (grid.y > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     k_fwd2d<<<grid, block, 0, s>>>(p.d_layA, p.d_layB, sino, p.d_src, p.d_u0, p.d_du, p.W, p.H,
-                                   p.det, p.nangles, p.sx, p.sy);
+                                   p.det, p.nangles, p.sx, p.sy, p.pitchA(), p.pitchB());
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }

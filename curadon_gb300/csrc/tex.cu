@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(256)
                 const float2 *__restrict__ layB, float *__restrict__ sino,
                 const float2 *__restrict__ tsrc, const float2 *__restrict__ tu0,
                 const float2 *__restrict__ tdu, int W, int H, int det, int nangles, float sx,
-                float sy, int tex_eighths) {
+                float sy, int tex_eighths, int pa, int pb) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     const int view = blockIdx.y * blockDim.y + threadIdx.y;
     if (u >= det || view >= nangles) return;
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(256)
         const float q = (ymajor ? roy : rox) - 0.5f;
         const int sq = ((ymajor ? vy : vx) > 0.f) ? 1 : -1;
         const float2 *lay = ymajor ? layA : layB;
-        const int pitch = (ymajor ? W : H) + 2 * kPad;
+        const int pitch = ymajor ? pa : pb;
         const float pmax = (float)(ymajor ? W : H);
         const int qmax = ymajor ? H : W;
         const float qf = floorf(q);
@@ -180,8 +180,8 @@ __global__ void __launch_bounds__(256)
             const int ip = (int)pf;
             const float2 lo = __ldg(row + ip);
             const float2 hi = __ldg(row + pitch + ip);
-            acc_lo += fmaf(fp, lo.y - lo.x, lo.x);
-            acc_hi += fmaf(fp, hi.y - hi.x, hi.x);
+            acc_lo += fmaf(fp, lo.y, lo.x);
+            acc_hi += fmaf(fp, hi.y, hi.x);
             p += vp;
             row += rstep;
         }
@@ -393,7 +393,7 @@ int launch_forward2d_hyb(Plan2d &p, const float *vol, float *sino, cudaStream_t 
     if (grid.y > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     k_fwd2d_hyb<<<grid, block, 0, s>>>(p.tex_vol, p.d_layA, p.d_layB, sino, p.d_src, p.d_u0,
                                        p.d_du, p.W, p.H, p.det, p.nangles, p.sx, p.sy,
-                                       p.tex_eighths);
+                                       p.tex_eighths, p.pitchA(), p.pitchB());
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }

@@ -115,6 +115,7 @@ class FanGeometry:
         self.vol_prec = int(vol_prec)
         self.sino_prec = int(sino_prec)
         self._plan = None
+        self._exact_plan = None
 
     @staticmethod
     def _scalar(v, name, default):
@@ -124,18 +125,29 @@ class FanGeometry:
             raise TypeError(f"Expected {name} to be float, got {type(v)}")
         return float(v)
 
+    def _make_plan(self):
+        from .backend import plan_2d
+
+        # COR is ignored by the reference's 2D path (geometry.py:226-228)
+        return plan_2d(self.device, self.vol_prec, self.vol_shape, self.vol_spacing,
+                       self.vol_offset, self.sino_prec, self.det_shape, self.det_spacing,
+                       self.det_offset, self.DSO, self.DSD, self.angles, self.det_rotation, 0)
+
     @property
     def plan(self):
         """The device plan (``backend.plan_2d``), built on first use."""
         if self._plan is None:
-            from .backend import plan_2d
-
-            # COR is ignored by the reference's 2D path (geometry.py:226-228)
-            self._plan = plan_2d(self.device, self.vol_prec, self.vol_shape, self.vol_spacing,
-                                 self.vol_offset, self.sino_prec, self.det_shape,
-                                 self.det_spacing, self.det_offset, self.DSO, self.DSD,
-                                 self.angles, self.det_rotation, 0)
+            self._plan = self._make_plan()
         return self._plan
+
+    @property
+    def exact_plan(self):
+        """A second plan whose forward filters in FP32 (algorithm "registers"),
+        so that it and ``adjoint`` are exact transposes (matched gradients)."""
+        if self._exact_plan is None:
+            self._exact_plan = self._make_plan()
+            self._exact_plan.set_algorithm(forward="registers")
+        return self._exact_plan
 
     def to_vec(self):
         """ASTRA-like per-view vectors [src.x, src.y, det.x, det.y, u.x, u.y]
@@ -233,6 +245,7 @@ class ConeGeometry:
         self.vol_offset = self._vec(vol_offset, "vol_offset", 3, np.zeros(3))
         self.device = int(device)
         self._plan = None
+        self._exact_plan = None
 
     @staticmethod
     def _vec(v, name, n, default):
@@ -244,16 +257,28 @@ class ConeGeometry:
             raise AttributeError(f"{name} must be {word} values, got {str(a.shape)}")
         return a
 
+    def _make_plan(self):
+        from .backend import plan_3d
+
+        return plan_3d(self.device, self.vol_shape, self.vol_spacing, self.vol_offset,
+                       self.angles, self.det_shape, self.det_spacing, self.det_offset,
+                       self.det_rotation, self.DSO, self.DSD, self.COR)
+
     @property
     def plan(self):
         """The device plan (``backend.plan_3d``), built on first use."""
         if self._plan is None:
-            from .backend import plan_3d
-
-            self._plan = plan_3d(self.device, self.vol_shape, self.vol_spacing, self.vol_offset,
-                                 self.angles, self.det_shape, self.det_spacing, self.det_offset,
-                                 self.det_rotation, self.DSO, self.DSD, self.COR)
+            self._plan = self._make_plan()
         return self._plan
+
+    @property
+    def exact_plan(self):
+        """A second plan whose forward filters in FP32 (algorithm "registers"),
+        the exact transpose partner of ``adjoint`` (matched gradients)."""
+        if self._exact_plan is None:
+            self._exact_plan = self._make_plan()
+            self._exact_plan.set_algorithm(forward="registers")
+        return self._exact_plan
 
     def sinogram_shape(self):
         return (self.nangles, *self.det_shape)

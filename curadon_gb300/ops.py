@@ -24,12 +24,14 @@ from .geometry import ConeGeometry, FanGeometry
 __all__ = ["forward", "backward", "adjoint", "TorchForward", "TorchBackprojection"]
 
 
-def forward(volume, sinogram, geom: Union[FanGeometry, ConeGeometry]):
+def forward(volume, sinogram, geom: Union[FanGeometry, ConeGeometry], exact: bool = False):
+    """Forward projection into ``sinogram``.  ``exact=True`` uses the
+    geometry's FP32-filtering plan, whose transpose ``adjoint`` is exactly."""
     if isinstance(geom, FanGeometry):
-        _C.forward_2d(volume, sinogram, geom.plan)
+        _C.forward_2d(volume, sinogram, geom.exact_plan if exact else geom.plan)
         return sinogram
     if isinstance(geom, ConeGeometry):
-        geom.plan.forward(volume, sinogram)
+        (geom.exact_plan if exact else geom.plan).forward(volume, sinogram)
         return sinogram
     raise ValueError("Unknown geometry type")
 
@@ -45,13 +47,14 @@ def backward(sinogram, volume, geom: Union[FanGeometry, ConeGeometry]):
 
 
 def adjoint(sinogram, volume, geom: Union[FanGeometry, ConeGeometry]):
-    """Adds the matched adjoint A^T sinogram (exact transpose of ``forward``)
-    to ``volume`` and returns it.  An addition beside the reference's API."""
+    """Adds the matched adjoint A^T sinogram -- the exact transpose of
+    ``forward(..., exact=True)`` -- to ``volume`` and returns it.  An addition
+    beside the reference's API."""
     if isinstance(geom, FanGeometry):
-        _C.adjoint_2d(volume, sinogram, geom.plan)
+        _C.adjoint_2d(volume, sinogram, geom.exact_plan)
         return volume
     if isinstance(geom, ConeGeometry):
-        geom.plan.adjoint(volume, sinogram)
+        geom.exact_plan.adjoint(volume, sinogram)
         return volume
     raise ValueError("Unknown geometry type")
 
@@ -65,13 +68,13 @@ class TorchForward(Function):
 
     ``TorchForward.apply(volume, geom)``: the gradient is the reference's
     voxel-driven backprojector (as in diffable.py:21-24).
-    ``TorchForward.apply(volume, geom, True)``: the gradient is the matched
-    adjoint, so it is the exact gradient of the forward."""
+    ``TorchForward.apply(volume, geom, True)``: the forward filters in FP32
+    and the gradient is its matched adjoint, so it is the exact gradient."""
 
     @staticmethod
     def forward(ctx, volume, geom, matched=False):
         sino = torch.zeros(geom.sinogram_shape(), device=volume.device, dtype=torch.float32)
-        forward(volume.detach().contiguous(), sino, geom)
+        forward(volume.detach().contiguous(), sino, geom, exact=bool(matched))
         ctx.geom = geom
         ctx.matched = bool(matched)
         return sino

@@ -14,11 +14,11 @@ def dot_test(geom, x, y, dev):
     x = torch.as_tensor(x, device=dev).contiguous()
     y = torch.as_tensor(y, device=dev).contiguous()
     ax = torch.zeros(geom.sinogram_shape(), device=dev)
-    forward(x, ax, geom)
+    forward(x, ax, geom, exact=True)
     if isinstance(geom, ConeGeometry):
         # rays that miss are left unwritten: they are zero rows of A
         ax0 = torch.full_like(ax, 123.0)
-        forward(x, ax0, geom)
+        forward(x, ax0, geom, exact=True)
         ax = torch.where(ax0 == 123.0, torch.zeros_like(ax), ax)
     aty = torch.zeros_like(x)
     adjoint(y, aty, geom)
@@ -64,7 +64,7 @@ def test_matched_gradient_finite_differences(cuda_device):
     geom = FanGeometry(**g)
     x0 = ellipses_2d(64, 2, device=cuda_device).double()
     target = torch.zeros(geom.sinogram_shape(), device=cuda_device)
-    forward(ellipses_2d(64, 9, device=cuda_device), target, geom)
+    forward(ellipses_2d(64, 9, device=cuda_device), target, geom, exact=True)
 
     def loss(x):
         s = TorchForward.apply(x.float(), geom, True)
@@ -79,6 +79,18 @@ def test_matched_gradient_finite_differences(cuda_device):
     fd = (float(loss(x0 + eps * d)) - float(loss(x0 - eps * d))) / (2 * eps)
     an = float((grad.double() * d).sum())
     assert abs(fd - an) / abs(fd) < 1e-3
+
+
+@pytest.mark.parametrize("algo", ["registers", "slab"])
+def test_dot_product_2d_per_forward_algorithm(cuda_device, algo):
+    """The FP32-weight forwards (registers, slab) share the adjoint."""
+    g = fan_config(200, 150)
+    geom = FanGeometry(**g)
+    geom.exact_plan.set_algorithm(forward=algo)
+    rng = np.random.default_rng(5)
+    x = rng.uniform(0, 1, (200, 200)).astype(np.float32)
+    y = rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32)
+    assert dot_test(geom, x, y, cuda_device) < 1e-5
 
 
 def test_adjoint_accumulates(cuda_device):
