@@ -39,8 +39,8 @@ import numpy as np  # noqa: E402
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
 # the ncu captures summarised in profiles/; None where not captured.
 NCU_TRAFFIC = {
-    ("fan2048", "forward"): None,
-    ("fan2048", "backward"): None,
+    ("fan2048", "forward"): 17_007_744,    # k_fwd2d_tex, profiles/dram_fan2048.md
+    ("fan2048", "backward"): 62_407_168,   # k_bwd2d_smem
 }
 
 

@@ -93,6 +93,18 @@ def test_dot_product_2d_per_forward_algorithm(cuda_device, algo):
     assert dot_test(geom, x, y, cuda_device) < 1e-5
 
 
+@pytest.mark.parametrize("algo", ["registers", "slab"])
+def test_dot_product_3d_per_forward_algorithm(cuda_device, algo):
+    """The FP32-weight 3D forwards (registers, slab) share the adjoint."""
+    g = cone_config(40, 36, 64)
+    geom = ConeGeometry(**g)
+    geom.exact_plan.set_algorithm(forward=algo)
+    rng = np.random.default_rng(6)
+    x = rng.uniform(0, 1, (40, 40, 40)).astype(np.float32)
+    y = rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32)
+    assert dot_test(geom, x, y, cuda_device) < 1e-5
+
+
 def test_adjoint_accumulates(cuda_device):
     g = cone_config(24, 12, 40)
     geom = ConeGeometry(**g)
