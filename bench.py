@@ -195,6 +195,19 @@ def reduce_max(values, world: int, device="cpu"):
 
 # ------------------------------------------------------------ ours
 
+def kernels_per_step(wl, geom) -> int:
+    """Kernels of this library launched by one forward + one backprojection
+    with the plan's algorithms (texture-unit paths copy the input into a
+    CUDA array with a memcpy, which is not a kernel)."""
+    fwd, bwd = geom.plan.algorithm()
+    if wl["kind"] == "fan":
+        nv = len(wl["geom"]["angles"])
+        f = 1 if fwd == "texture" else 2
+        b = -(-nv // 2048) if bwd == "texture" else 2
+        return f + b
+    f = 1 if fwd == "texture" else 3 if fwd in ("registers", "slab") else 2
+    return f + 2
+
 def run_ours(args, rank, world, local_rank):
     import torch
 
@@ -217,7 +230,7 @@ def run_ours(args, rank, world, local_rank):
     vbp = torch.zeros_like(vol)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
-    launches_per_step = 4  # re-layout + forward, re-layout + backprojection
+    launches_per_step = kernels_per_step(wl, geom)
 
     def step():
         cg.forward(vol, sino, geom)

@@ -39,9 +39,9 @@ def _stream(t: torch.Tensor) -> C.c_void_p:
     return C.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
 
 
-FORWARD_2D = ("registers", "texture", "hybrid", "slab")
+FORWARD_2D = ("registers", "texture", "hybrid", "slab", "chunked")
 BACKWARD_2D = ("registers", "texture", "shared")
-FORWARD_3D = ("registers", "texture", "layered")
+FORWARD_3D = ("registers", "texture", "layered", "slab")
 BACKWARD_3D = ("registers",)
 
 

@@ -63,6 +63,13 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
         if (has("fwd2d=alu")) p2->algo_fwd = 0;
         if (has("fwd2d=tex")) p2->algo_fwd = 1;
         if (has("fwd2d=slab")) p2->algo_fwd = 3;
+        if (has("fwd2d=cslab")) p2->algo_fwd = 4;
+        // chunk shapes: 4 (rows) x 512 (pairs) or 8 x 384 for 256-cell
+        // bundles, 104 / 108: 4 or 8 x 256 for 128-cell bundles
+        for (int k : {4, 104, 108, 204, 304, 308}) {
+            const std::string key = "fwd2d=cslab" + std::to_string(k);
+            if (has(key.c_str())) p2->algo_fwd = 4, p2->fwd_chunk_rows = k;
+        }
         for (int k = 1; k < 8; ++k) {
             const std::string key = "fwd2d=hyb" + std::to_string(k);
             if (has(key.c_str())) p2->algo_fwd = 2, p2->tex_eighths = k;
@@ -75,6 +82,7 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
         if (has("fwd3d=alu")) p3->algo_fwd = 0;
         if (has("fwd3d=tex3")) p3->algo_fwd = 1;
         if (has("fwd3d=tex2l")) p3->algo_fwd = 2;
+        if (has("fwd3d=slab")) p3->algo_fwd = 3;
         const size_t at = e.find("fwd3d_block=");
         if (at != std::string::npos) {
             int bx = 0, by = 0, bz = 0;
@@ -413,7 +421,7 @@ int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by) {
 int cg_plan2d_set_algorithm(cg_plan2d *plan, int forward, int backward) {
     clear_error();
     CG_REQUIRE(plan, "plan is NULL");
-    CG_REQUIRE(forward >= -1 && forward <= 3, "2D forward algorithm must be -1..3");
+    CG_REQUIRE(forward >= -1 && forward <= 4, "2D forward algorithm must be -1..4");
     CG_REQUIRE(backward >= -1 && backward <= 2, "2D backward algorithm must be -1..2");
     if (forward >= 0) plan->algo_fwd = forward;
     if (backward >= 0) plan->algo_bwd = backward;
@@ -451,6 +459,7 @@ int cg_forward_2d(cg_plan2d *plan, const float *volume, float *sinogram, void *s
     if (rc) return rc;
     if (plan->algo_fwd == 3 && slab_supported(*plan))
         return launch_forward2d_slab(*plan, sinogram, s);
+    if (plan->algo_fwd == 4) return launch_forward2d_cslab(*plan, sinogram, s, plan->fwd_chunk_rows);
     return launch_forward2d(*plan, sinogram, s);
 }
 
@@ -462,7 +471,7 @@ int cg_backward_2d(cg_plan2d *plan, float *volume, const float *sinogram, void *
     CG_REQUIRE(guard.ok(), "cannot select the plan's device");
     cudaStream_t s = (cudaStream_t)stream;
     if (plan->algo_bwd == 1) return launch_backward2d_tex(*plan, volume, sinogram, s);
-    int rc = launch_relayout_sino2d(*plan, sinogram, s);
+    int rc = launch_relayout_sino2d(*plan, sinogram, s, plan->algo_bwd == 2);
     if (rc) return rc;
     if (plan->algo_bwd == 2) return launch_backward2d_smem(*plan, volume, s);
     return launch_backward2d(*plan, volume, s);
@@ -491,7 +500,7 @@ int cg_plan3d_create(cg_plan3d **plan, int device, const uint64_t vol_shape[3],
 int cg_plan3d_set_algorithm(cg_plan3d *plan, int forward, int backward) {
     clear_error();
     CG_REQUIRE(plan, "plan is NULL");
-    CG_REQUIRE(forward >= -1 && forward <= 2, "3D forward algorithm must be -1..2");
+    CG_REQUIRE(forward >= -1 && forward <= 3, "3D forward algorithm must be -1..3");
     CG_REQUIRE(backward >= -1 && backward <= 0, "3D backward algorithm must be -1..0");
     if (forward >= 0) plan->algo_fwd = forward;
     if (backward >= 0) plan->algo_bwd = backward;
@@ -522,6 +531,7 @@ int cg_forward_3d_plan(cg_plan3d *plan, const float *volume, float *sinogram, vo
     CG_REQUIRE(volume && sinogram, "volume and sinogram must be device pointers");
     DeviceGuard guard(plan->device);
     CG_REQUIRE(guard.ok(), "cannot select the plan's device");
+    if (plan->algo_fwd == 3) return launch_forward3d_slab(*plan, volume, sinogram, (cudaStream_t)stream);
     if (plan->algo_fwd != 0) return launch_forward3d_tex(*plan, volume, sinogram, (cudaStream_t)stream);
     int rc = ensure_plan3d_scratch(*plan, true, false);
     if (rc) return rc;
@@ -568,7 +578,9 @@ int cg_forward_3d(const float *x, const uint64_t vol_shape[3], const float vol_s
     rc = make_plan3d(&p, dev, vol_shape, vol_spacing, vol_offset, phi, theta, psi, nangles,
                      det_shape, det_spacing, det_offset, det_rotation, DSO, DSD, COR);
     if (rc) return rc;
-    if (p->algo_fwd != 0) {
+    if (p->algo_fwd == 3) {
+        rc = launch_forward3d_slab(*p, x, sinogram, (cudaStream_t)stream);
+    } else if (p->algo_fwd != 0) {
         rc = launch_forward3d_tex(*p, x, sinogram, (cudaStream_t)stream);
     } else {
         rc = ensure_plan3d_scratch(*p, true, false);

@@ -87,11 +87,13 @@ struct Plan2d {
     cudaTextureObject_t tex_vol = 0, tex_sino = 0;
 
     // algorithm per operator: forward 0 = registers, 1 = texture unit,
-    // 2 = texture + registers, 3 = shared-memory row slabs;
+    // 2 = texture + registers, 3 = shared-memory row slabs, 4 = chunked
+    // shared-memory slabs;
     // backprojection 0 = registers, 1 = texture unit, 2 = shared-memory rows.
     // Defaults: the fastest measured on GB300 (2D n-sweep).
     int algo_fwd = 1, algo_bwd = 2;
     int tex_eighths = 4;              // hybrid forward: share of warps on the texture unit
+    int fwd_chunk_rows = 4;           // chunked forward: chunk shape
 
     // row pitches of layA / layB in pairs, even so every row starts on 16 bytes
     int pitchA() const { return (W + 2 * kPad + 1) & ~1; }
@@ -123,7 +125,8 @@ struct Plan3d {
     cudaTextureObject_t tex3 = 0, texA = 0, texB = 0;
     float *d_volT = nullptr;          // x<->z transposed volume for arrB
 
-    // forward 0 = registers, 1 = tex3D, 2 = layered bilinear + lerp;
+    // forward 0 = registers, 1 = tex3D, 2 = layered bilinear + lerp,
+    // 3 = shared-memory slabs;
     // defaults: the fastest measured on GB300 (256^3 and 512^3 workloads)
     int algo_fwd = 1, algo_bwd = 0;
     // texture forwards: detector cells (u, v) x views per thread block
@@ -138,11 +141,13 @@ void free_plan3d(Plan3d *p);
 int launch_plan2d_tables(Plan2d &p, cudaStream_t s);
 int launch_relayout2d(const Plan2d &p, const float *vol, cudaStream_t s);
 int launch_forward2d(const Plan2d &p, float *sino, cudaStream_t s);
-int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s);
+// scaled: rows multiplied by the view's DSD (the staged backprojector's input)
+int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s, bool scaled);
 int launch_backward2d(const Plan2d &p, float *vol, cudaStream_t s);
 
 int ensure_plan3d_scratch(Plan3d &p, bool fwd, bool bwd);
 int launch_forward3d(const Plan3d &p, const float *vol, float *sino, cudaStream_t s);
+int launch_forward3d_slab(Plan3d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s);
 
 int launch_adjoint2d(const Plan2d &p, float *vol, const float *sino, cudaStream_t s);
@@ -151,6 +156,11 @@ int launch_adjoint3d(const Plan3d &p, float *vol, const float *sino, cudaStream_
 int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s);
 bool slab_supported(const Plan2d &p);
 int launch_forward2d_slab(const Plan2d &p, float *sino, cudaStream_t s);
+// rows: chunk shape (4, 8: rows of 256-cell bundles; 104, 108: 4 or 8 rows
+// of 128-cell bundles)
+int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int rows);
+// Copies the volume into the plan's 2D texture array.
+int load_vol_texture(Plan2d &p, const float *vol, cudaStream_t s);
 int launch_forward2d_tex(Plan2d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_forward2d_hyb(Plan2d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t s);

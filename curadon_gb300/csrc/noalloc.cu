@@ -122,7 +122,7 @@ extern "C" int cg_backward_2d_static(float *volume, const float *sinogram,
     CG_TRY_CUDA(cudaMemcpyAsync(p.d_DSO, DSO, 4 * n, cudaMemcpyHostToDevice, s));
     CG_TRY_CUDA(cudaMemcpyAsync(p.d_DSD, DSD, 4 * n, cudaMemcpyHostToDevice, s));
     if ((rc = launch_plan2d_tables(p, s))) return rc;
-    if ((rc = launch_relayout_sino2d(p, sinogram, s))) return rc;
+    if ((rc = launch_relayout_sino2d(p, sinogram, s, p.algo_bwd == 2))) return rc;
     if (p.algo_bwd == 2) return launch_backward2d_smem(p, volume, s);
     return launch_backward2d(p, volume, s);
 }

@@ -99,15 +99,19 @@ __global__ void __launch_bounds__(256)
 }
 
 __global__ void k_relayout_sino2d(const float *__restrict__ sino, int det, int nangles,
-                                  float2 *__restrict__ S) {
+                                  float2 *__restrict__ S, const float4 *__restrict__ meta) {
     const int pitch = det + 2 * kPad;
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)pitch * nangles) return;
     const int a = (int)(idx / pitch);
     const int k = (int)(idx % pitch) - kPad;
     const float *row = sino + (size_t)a * det;
-    const float t0 = (k >= 0 && k < det) ? row[k] : 0.f;
-    const float t1 = (k + 1 >= 0 && k + 1 < det) ? row[k + 1] : 0.f;
+    float t0 = (k >= 0 && k < det) ? row[k] : 0.f;
+    float t1 = (k + 1 >= 0 && k + 1 < det) ? row[k + 1] : 0.f;
+    if (meta) {  // rows pre-scaled by the view's DSD
+        const float dsd = meta[a].z;
+        t0 *= dsd, t1 *= dsd;
+    }
     S[idx] = make_float2(t0, t1 - t0);
 }
 
@@ -393,6 +397,265 @@ int launch_forward2d_slab(const Plan2d &p, float *sino, cudaStream_t s) {
 
 namespace {
 
+// ------------------------------------------------------------ forward, chunked slab
+
+constexpr int kCs2G = 4;             // views per bundle
+constexpr int kCs2MaxChunks = 1024;  // chunk windows kept in shared memory
+
+// Bundle = kCs2G views x T adjacent detector cells x ray class (blockIdx.z:
+// 0 = y-stepping rays on layA, 1 = x-stepping rays on layB); thread t owns
+// cell u0 + t of every view.  The block walks its layout's rows in chunks of
+// K.  A chunk's window -- the pair columns the bundle's rays can touch on its
+// rows -- is bounded by lines through each view's source: a ray's column is
+// linear in the row with slope b = dp/dq, and the rays of this class have
+// |b| <= 1.  Over a detector interval on which dq keeps its sign b is
+// monotone, so the slopes at the bundle's end cells clamped to [-1, 1] bound
+// every ray of the class; where dq changes sign the bound is b = -1 .. 1.
+// All windows are computed up front.  Windows are
+// staged for rows r0 .. r0 + K (row stride S pairs) with 16-byte cp.async
+// into two alternating buffers, the next chunk's copy running while the
+// current chunk is sampled, one barrier per chunk.  Every ray then takes its
+// samples of the chunk from shared memory: two 8-byte loads at fixed row
+// offsets and two FMAs each.  Samples and their order per ray are those of the
+// register forward (the reference's positions; rays stepping towards smaller
+// rows are summed in reverse), so the matched adjoint is this forward's
+// exact transpose too.  A chunk whose window does not fit reads global memory.
+// Row-sum accumulation of one sample's two pairs.  Scalar: alo += lo.x +
+// fp lo.y (same operations as the register forward).  Packed: the terms are
+// kept apart, (sum lo.x, sum fp lo.y), one packed FP32 FMA per row.
+template <bool PK>
+struct RowAcc {
+    float2 lo, hi;
+    __device__ __forceinline__ void zero() { lo = hi = make_float2(0.f, 0.f); }
+    __device__ __forceinline__ void add(float fp, float2 a, float2 b) {
+        if constexpr (PK) {
+            const float2 w = make_float2(1.f, fp);
+            lo = __ffma2_rn(w, a, lo);
+            hi = __ffma2_rn(w, b, hi);
+        } else {
+            lo.x += fmaf(fp, a.y, a.x);
+            hi.x += fmaf(fp, b.y, b.x);
+        }
+    }
+    __device__ __forceinline__ float sum_lo() const { return PK ? lo.x + lo.y : lo.x; }
+    __device__ __forceinline__ float sum_hi() const { return PK ? hi.x + hi.y : hi.x; }
+};
+
+template <int K, int S, int T, bool PK>
+__global__ void __launch_bounds__(T)
+    k_fwd2d_cslab(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
+                  float *__restrict__ sino, const float2 *__restrict__ tsrc,
+                  const float2 *__restrict__ tu0, const float2 *__restrict__ tdu, int W, int H,
+                  int det, int nangles, float sx, float sy, int pa, int pb) {
+    static_assert(S % 2 == 0, "rows of the window buffers must stay 16-byte aligned");
+    constexpr int kBuf = (K + 1) * S;               // pairs per buffer
+    extern __shared__ __align__(16) float2 cwin[];  // 2 buffers
+    __shared__ float s_cor[2 * kCs2G][2];            // column = a + b * row
+    __shared__ int s_win[kCs2MaxChunks];             // (first column << 16) | width, or -1
+    __shared__ int s_rmin, s_rmax;
+    const bool cls_y = blockIdx.z == 0;
+    const float2 *lay = cls_y ? layA : layB;
+    const int pitch = cls_y ? pa : pb;
+    const int qmax = cls_y ? H : W;
+    const int pmaxi = cls_y ? W : H;
+    const int u0 = blockIdx.x * T, v0 = blockIdx.y * kCs2G;
+    const int u = u0 + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+    if (threadIdx.x == 0) s_rmin = INT_MAX, s_rmax = INT_MIN;
+    __syncthreads();
+    if (threadIdx.x < 2 * kCs2G) {  // lanes 2g, 2g + 1: the end cells of view g
+        const int view = min(v0 + (threadIdx.x >> 1), nangles - 1);
+        const int cu = (threadIdx.x & 1) ? min(u0 + T - 1, det - 1) : u0;
+        const float2 sv = tsrc[view], o = tu0[view], d = tdu[view];
+        const float dx = fmaf(d.x, (float)cu, o.x), dy = fmaf(d.y, (float)cu, o.y);
+        // column p (texel coordinate - 1/2) of the ray on row q (the same)
+        const float dp = cls_y ? dx : dy, dq = cls_y ? dy : dx;
+        const float sp = (cls_y ? sv.x : sv.y) - 0.5f, sq = (cls_y ? sv.y : sv.x) - 0.5f;
+        const float dq_other = __shfl_xor_sync(0xffu, dq, 1);
+        const float b = (dq > 0.f) != (dq_other > 0.f) ? ((threadIdx.x & 1) ? 1.f : -1.f)
+                                                        : fminf(fmaxf(dp / dq, -1.f), 1.f);
+        s_cor[threadIdx.x][0] = sp - sq * b;
+        s_cor[threadIdx.x][1] = b;
+    }
+    // per ray: column at its first row (p), step per row (V), row sums
+    float p[kCs2G], V[kCs2G];
+    RowAcc<PK> acc[kCs2G];
+    int rlo[kCs2G], len[kCs2G];
+    int my_min = INT_MAX, my_max = INT_MIN;
+#pragma unroll
+    for (int g = 0; g < kCs2G; ++g) {
+        const int view = v0 + g;
+        acc[g].zero(), len[g] = 0, rlo[g] = 0, p[g] = V[g] = 0.f;
+        if (view >= nangles || u >= det) continue;
+        FanRay r;
+        if (!fan_ray(tsrc[view], tu0[view], tdu[view], u, W, H, sx, sy, r)) continue;
+        if (r.ymajor != cls_y) continue;
+        const int iq = (int)fminf(fmaxf(floorf(r.q), -(float)kPad), (float)qmax);
+        const int n = min(r.n, r.sq > 0 ? qmax - iq + 1 : iq + kPad + 1);
+        if (n <= 0) continue;
+        const int lo = r.sq > 0 ? iq : iq - (n - 1);
+        V[g] = r.sq > 0 ? r.vp : -r.vp;
+        p[g] = r.sq > 0 ? r.p : fmaf((float)(n - 1), r.vp, r.p);
+        rlo[g] = lo, len[g] = n;
+        my_min = min(my_min, lo), my_max = max(my_max, lo + n - 1);
+    }
+    if (my_min <= my_max) {
+        atomicMin(&s_rmin, my_min);
+        atomicMax(&s_rmax, my_max);
+    }
+    __syncthreads();
+    const int rmin = s_rmin, rmax = s_rmax;
+    const int nch = rmin <= rmax ? (rmax - rmin) / K + 1 : 0;
+    {
+        for (int ci = threadIdx.x; ci < min(nch, kCs2MaxChunks); ci += T) {
+            const float ra = (float)(rmin + ci * K), rb = ra + (float)K;
+            float lo = FLT_MAX, hi = -FLT_MAX;
+#pragma unroll
+            for (int c = 0; c < 2 * kCs2G; ++c) {
+                const float c0 = fmaf(s_cor[c][1], ra, s_cor[c][0]);
+                const float c1 = fmaf(s_cor[c][1], rb, s_cor[c][0]);
+                lo = fminf(lo, fminf(c0, c1));
+                hi = fmaxf(hi, fmaxf(c0, c1));
+            }
+            int win = -1;
+            if (lo > -1e6f && hi < 1e6f) {
+                // first column even (16-byte aligned rows), even width
+                const int a0 = max((int)floorf(lo) - 1, -kPad) & ~1;
+                const int a1 = min((int)floorf(hi) + 1, pmaxi + 1);
+                const int wx = (a1 - a0 + 2) & ~1;
+                if (a1 >= a0 && wx <= S) win = ((a0 + kPad) << 16) | wx;
+            }
+            s_win[ci] = win;
+        }
+    }
+    __syncthreads();
+
+    // copies chunk ci's window into buffer `buf`
+    auto stage = [&](int ci, int buf) {
+        const int win = ci < kCs2MaxChunks ? s_win[ci] : -1;
+        if (win < 0) return;
+        const int c0 = win >> 16, wx = win & 0xffff, r0 = rmin + ci * K;
+        float2 *base = cwin + buf * kBuf;
+        for (int row = warp; row <= K; row += T / 32) {
+            const int q = min(r0 + row, qmax + 1);
+            const float2 *src = lay + (size_t)(q + kPad) * pitch + c0;
+            float2 *dst = base + row * S;
+            for (int c = 2 * lane; c < wx; c += 64) {
+                const unsigned d = (unsigned)__cvta_generic_to_shared(dst + c);
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src + c));
+            }
+        }
+    };
+
+    if (nch > 0) stage(0, 0);
+    asm volatile("cp.async.commit_group;\n" ::);
+    for (int ci = 0; ci < nch; ++ci) {
+        asm volatile("cp.async.wait_group 0;\n" ::);
+        __syncthreads();
+        if (ci + 1 < nch) stage(ci + 1, (ci + 1) & 1);
+        asm volatile("cp.async.commit_group;\n" ::);
+        const int r0 = rmin + ci * K;
+        const int win = ci < kCs2MaxChunks ? s_win[ci] : -1;
+        if (win >= 0) {
+            const int c0 = (win >> 16) - kPad, wx = win & 0xffff;
+            const unsigned cmax = (unsigned)(wx - 1);
+            const float2 *b0 = cwin + (ci & 1) * kBuf;
+#pragma unroll
+            for (int g = 0; g < kCs2G; ++g) {
+                const int rel = r0 - rlo[g];
+                if (rel >= 0 && rel + K <= len[g]) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) {
+                        const float pf = floorf(p[g]);
+                        const float fp = p[g] - pf;
+                        const unsigned c = min((unsigned)((int)pf - c0), cmax);
+                        const float2 lo = b0[k * S + c], hi = b0[(k + 1) * S + c];
+                        acc[g].add(fp, lo, hi);
+                        p[g] += V[g];
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < K; ++k) {
+                        if ((unsigned)(rel + k) < (unsigned)len[g]) {
+                            const float pf = floorf(p[g]);
+                            const float fp = p[g] - pf;
+                            const unsigned c = min((unsigned)((int)pf - c0), cmax);
+                            const float2 lo = b0[k * S + c], hi = b0[(k + 1) * S + c];
+                            acc[g].add(fp, lo, hi);
+                            p[g] += V[g];
+                        }
+                    }
+                }
+            }
+        } else {
+            const unsigned gcap = (unsigned)(pmaxi + kPad);
+#pragma unroll
+            for (int g = 0; g < kCs2G; ++g) {
+                const int ra = max(r0, rlo[g]), rb = min(r0 + K - 1, rlo[g] + len[g] - 1);
+                for (int r = ra; r <= rb; ++r) {
+                    const float pf = floorf(p[g]);
+                    const float fp = p[g] - pf;
+                    const unsigned c = min((unsigned)((int)pf + kPad), gcap);
+                    const float2 *rowp = lay + (size_t)(r + kPad) * pitch;
+                    const float2 lo = __ldg(rowp + c), hi = __ldg(rowp + pitch + c);
+                    acc[g].add(fp, lo, hi);
+                    p[g] += V[g];
+                }
+            }
+        }
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::);
+
+#pragma unroll
+    for (int g = 0; g < kCs2G; ++g) {
+        const int view = v0 + g;
+        if (view >= nangles || u >= det) continue;
+        FanRay r;
+        float out;
+        if (!fan_ray(tsrc[view], tu0[view], tdu[view], u, W, H, sx, sy, r)) {
+            if (!cls_y) continue;
+            out = 0.f;
+        } else {
+            if (r.ymajor != cls_y) continue;
+            const float alo = acc[g].sum_lo(), ahi = acc[g].sum_hi();
+            out = fmaf(r.fq, ahi - alo, alo) * r.nrm;
+        }
+        sino[(size_t)view * det + u] = out;
+    }
+}
+
+}  // namespace
+
+int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int rows) {
+    const int groups = ceil_div(p.nangles, kCs2G);
+    if (groups > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
+    if (std::max(p.pitchA(), p.pitchB()) >= 32768)
+        return set_error(CG_ERR_INVALID, "volume too wide for the chunked forward");
+    auto go = [&](auto kernel, int k, int stride, int threads) -> int {
+        const size_t smem = 2 * sizeof(float2) * (k + 1) * stride;
+        CG_TRY_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem));
+        dim3 grid(ceil_div(p.det, threads), groups, 2);
+        kernel<<<grid, threads, smem, s>>>(p.d_layA, p.d_layB, sino, p.d_src, p.d_u0, p.d_du,
+                                           p.W, p.H, p.det, p.nangles, p.sx, p.sy, p.pitchA(),
+                                           p.pitchB());
+        CG_TRY_CUDA(cudaGetLastError());
+        return CG_OK;
+    };
+    switch (rows) {
+        case 4: return go(k_fwd2d_cslab<4, 512, 256, false>, 4, 512, 256);
+        case 104: return go(k_fwd2d_cslab<4, 256, 128, false>, 4, 256, 128);
+        case 108: return go(k_fwd2d_cslab<8, 256, 128, false>, 8, 256, 128);
+        case 204: return go(k_fwd2d_cslab<4, 512, 256, true>, 4, 512, 256);
+        case 304: return go(k_fwd2d_cslab<4, 256, 128, true>, 4, 256, 128);
+        case 308: return go(k_fwd2d_cslab<8, 256, 128, true>, 8, 256, 128);
+        default: return set_error(CG_ERR_INVALID, "unknown chunk shape");
+    }
+}
+
+namespace {
+
 // ------------------------------------------------------------ backward
 
 constexpr int kBwdRows = 4;        // pixels per thread, 8 rows apart
@@ -471,7 +734,9 @@ constexpr int kSmWin = 128;   // pairs of one view's row staged for a tile
 // (backward_2d.hpp:61-96) are formed with the per-view terms hoisted:
 //   x' + DSO = -cos Y + (-sin X + DSO),  yi = -sin SY + cos SX,
 //   w = DSD / (x' + DSO),  u = w yi + det/2,
-// then one 8-byte shared load and two FMAs.
+// then one 8-byte shared load and two FMAs.  The rows were pre-scaled by
+// DSD, so the weight is the reciprocal 1 / (x' + DSO) and u = (DSD yi) / (x' +
+// DSO) + det/2 with DSD folded into the per-view terms.
 __global__ void __launch_bounds__(256)
     k_bwd2d_smem(float *__restrict__ vol, const float2 *__restrict__ S,
                  const float4 *__restrict__ meta, int W, int H, int det, int nangles, float sx,
@@ -532,17 +797,19 @@ __global__ void __launch_bounds__(256)
             srow[j][i] = S[(size_t)(v0 + j) * pitch + kPad + k];
         }
         __syncthreads();
+#pragma unroll 2
         for (int j = 0; j < nv; ++j) {
             const float4 m = smeta[j];
             const int k0 = skmin[j];
-            const float A = fmaf(m.x, X, m.w), B = m.y * SX, nc = -m.y;
+            const float A = fmaf(m.x, X, m.w), nc = -m.y;
+            const float mx = m.x * m.z, B = (m.y * m.z) * SX;
             if (k0 != INT_MIN) {
                 const float2 *sr = srow[j];
 #pragma unroll
                 for (int r = 0; r < kSmRows; ++r) {
                     const float den = fmaf(nc, Y[r], A);
-                    const float yi = fmaf(m.x, SY[r], B);
-                    const float w = __fdividef(m.z, den);
+                    const float yi = fmaf(mx, SY[r], B);
+                    const float w = __fdividef(1.0f, den);
                     const float ub = fmaf(w, yi, edm);
                     const float kf = floorf(ub);
                     const float a = ub - kf;
@@ -555,8 +822,8 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
                 for (int r = 0; r < kSmRows; ++r) {
                     const float den = fmaf(nc, Y[r], A);
-                    const float yi = fmaf(m.x, SY[r], B);
-                    const float w = __fdividef(m.z, den);
+                    const float yi = fmaf(mx, SY[r], B);
+                    const float w = __fdividef(1.0f, den);
                     const float ub = fmaf(w, yi, edm);
                     const float kf = floorf(ub);
                     const float a = ub - kf;
@@ -608,9 +875,10 @@ int launch_forward2d(const Plan2d &p, float *sino, cudaStream_t s) {
     return CG_OK;
 }
 
-int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s) {
+int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s, bool scaled) {
     const long long n = (long long)p.pitchS() * p.nangles;
-    k_relayout_sino2d<<<ceil_div(n, 256), 256, 0, s>>>(sino, p.det, p.nangles, p.d_sinoP);
+    k_relayout_sino2d<<<ceil_div(n, 256), 256, 0, s>>>(sino, p.det, p.nangles, p.d_sinoP,
+                                                       scaled ? p.d_bmeta : nullptr);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }

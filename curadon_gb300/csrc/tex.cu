@@ -378,7 +378,7 @@ int launch_forward2d_tex(Plan2d &p, const float *vol, float *sino, cudaStream_t 
     return CG_OK;
 }
 
-int launch_forward2d_hyb(Plan2d &p, const float *vol, float *sino, cudaStream_t s) {
+int load_vol_texture(Plan2d &p, const float *vol, cudaStream_t s) {
     if (!p.arr_vol) {
         int rc = alloc_array(&p.arr_vol, p.W, p.H, 0, cudaArrayDefault);
         if (rc) return rc;
@@ -386,7 +386,13 @@ int launch_forward2d_hyb(Plan2d &p, const float *vol, float *sino, cudaStream_t 
     }
     CG_TRY_CUDA(cudaMemcpy2DToArrayAsync(p.arr_vol, 0, 0, vol, sizeof(float) * p.W,
                                          sizeof(float) * p.W, p.H, cudaMemcpyDeviceToDevice, s));
-    int rc = launch_relayout2d(p, vol, s);
+    return CG_OK;
+}
+
+int launch_forward2d_hyb(Plan2d &p, const float *vol, float *sino, cudaStream_t s) {
+    int rc = load_vol_texture(p, vol, s);
+    if (rc) return rc;
+    rc = launch_relayout2d(p, vol, s);
     if (rc) return rc;
     dim3 block(p.fwd_bx, p.fwd_by);
     dim3 grid(ceil_div(p.det, p.fwd_bx), ceil_div(p.nangles, p.fwd_by));

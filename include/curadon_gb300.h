@@ -76,11 +76,12 @@ int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by);
 /* Algorithm of each operator of a plan; -1 leaves one unchanged.
  *   forward:  0 registers (FP32 filtering of pair-packed copies, gathered
  *               through L1), 1 texture unit, 2 texture unit + registers on
- *               alternate warps, 3 shared-memory row slabs
+ *               alternate warps, 3 shared-memory row slabs, 4 chunked
+ *               shared-memory slabs
  *   backward: 0 registers, 1 texture unit, 2 shared-memory detector windows
  * The texture unit filters with 8-bit weight fractions, exactly as the
  * reference does; the other algorithms filter in FP32, and cg_adjoint_2d is
- * the exact transpose of forward algorithms 0 and 3.  A new plan starts at
+ * the exact transpose of forward algorithms 0, 3 and 4.  A new plan starts at
  * the fastest measured combination. */
 int cg_plan2d_set_algorithm(cg_plan2d *plan, int forward, int backward);
 int cg_plan2d_get_algorithm(const cg_plan2d *plan, int *forward, int *backward);
@@ -132,9 +133,9 @@ int cg_plan3d_destroy(cg_plan3d *plan);
 /* Algorithm of each 3D operator; -1 leaves one unchanged.
  *   forward:  0 registers (FP32 trilinear from pair-packed copies),
  *             1 texture unit (tex3D), 2 texture unit bilinear per layer +
- *             FP32 lerp across layers
+ *             FP32 lerp across layers, 3 shared-memory slabs (FP32)
  *   backward: 0 registers
- * cg_adjoint_3d_plan is the exact transpose of forward algorithm 0. */
+ * cg_adjoint_3d_plan is the exact transpose of forward algorithms 0 and 3. */
 int cg_plan3d_set_algorithm(cg_plan3d *plan, int forward, int backward);
 int cg_plan3d_get_algorithm(const cg_plan3d *plan, int *forward, int *backward);
 

@@ -81,9 +81,9 @@ def test_matched_gradient_finite_differences(cuda_device):
     assert abs(fd - an) / abs(fd) < 1e-3
 
 
-@pytest.mark.parametrize("algo", ["registers", "slab"])
+@pytest.mark.parametrize("algo", ["registers", "slab", "chunked"])
 def test_dot_product_2d_per_forward_algorithm(cuda_device, algo):
-    """The FP32-weight forwards (registers, slab) share the adjoint."""
+    """The FP32-weight forwards (registers, slab, chunked) share the adjoint."""
     g = fan_config(200, 150)
     geom = FanGeometry(**g)
     geom.exact_plan.set_algorithm(forward=algo)
