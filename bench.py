@@ -37,10 +37,22 @@ sys.path.insert(0, str(ROOT))
 import numpy as np  # noqa: E402
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
-# the ncu captures summarised in profiles/; None where not captured.
+# the ncu captures summarised in profiles/, by workload and kernel; None
+# where not captured.
 NCU_TRAFFIC = {
-    ("fan2048", "forward"): 17_007_744,    # k_fwd2d_tex, profiles/dram_fan2048.md
-    ("fan2048", "backward"): 62_407_168,   # k_bwd2d_smem
+    ("fan2048", "k_fwd2d_tex"): 17_007_744,    # profiles/dram_fan2048.md
+    ("fan2048", "k_bwd2d_smem"): 62_407_168,
+}
+
+# Main kernel of each operator by the plan's algorithm name.
+KERNELS = {
+    ("fan", "forward", "texture"): "k_fwd2d_tex", ("fan", "forward", "chunked"): "k_fwd2d_cslab",
+    ("fan", "forward", "registers"): "k_fwd2d", ("fan", "forward", "hybrid"): "k_fwd2d_hyb",
+    ("fan", "forward", "slab"): "k_fwd2d_slab", ("fan", "backward", "shared"): "k_bwd2d_smem",
+    ("fan", "backward", "registers"): "k_bwd2d", ("fan", "backward", "texture"): "k_bwd2d_tex",
+    ("cone", "forward", "texture"): "k_fwd3d_tex3", ("cone", "forward", "layered"): "k_fwd3d_tex2l",
+    ("cone", "forward", "registers"): "k_fwd3d", ("cone", "forward", "slab"): "k_fwd3d_slab",
+    ("cone", "backward", "registers"): "k_bwd3d",
 }
 
 
@@ -325,6 +337,8 @@ def run_ours(args, rank, world, local_rank):
     b_alg = {"forward": 4 * (nvox + nrays), "backward": 4 * (nrays + 2 * nvox)}
     dom = "forward" if ms_fwd >= ms_bwd else "backward"
     t_dom = (ms_fwd if dom == "forward" else ms_bwd) / 1e3
+    algos = dict(zip(("forward", "backward"), geom.plan.algorithm()))
+    kernel = KERNELS.get((wl["kind"], dom, algos[dom]), dom)
     peaks = {}
     try:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -335,8 +349,9 @@ def run_ours(args, rank, world, local_rank):
     peak = peak or 6800.0
     achieved = b_alg[dom] / t_dom / 1e9
     samples = s_fwd if dom == "forward" else s_bwd
-    traffic = NCU_TRAFFIC.get((wl["name"], dom))
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 3), "peak": peak,
+    traffic = NCU_TRAFFIC.get((wl["name"], kernel))
+    roofline = {"bound": "hbm", "kernel": kernel, "operator": dom,
+                "achieved": round(achieved, 3), "peak": peak,
                 "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "algorithmic_bytes": b_alg[dom],
                 "samples_per_s": samples / t_dom,

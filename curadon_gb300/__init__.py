@@ -10,13 +10,13 @@ there is no CPU fallback.
 """
 from . import backend
 from .backend import (adjoint_2d, backward_2d, backward_3d, forward_2d, forward_3d, plan_2d,
-                      plan_3d)
-from .geometry import ConeGeometry, FanGeometry, geom_to_str
+                      plan_2d_vec, plan_3d)
+from .geometry import ConeGeometry, FanGeometry, FanVecGeometry, geom_to_str
 from .ops import TorchBackprojection, TorchForward, adjoint, backward, forward
 
 __all__ = [
-    "FanGeometry", "ConeGeometry", "geom_to_str", "forward", "backward", "adjoint", "TorchForward",
-    "TorchBackprojection", "plan_2d", "plan_3d", "forward_2d", "backward_2d", "forward_3d",
-    "backward_3d", "backend",
+    "FanGeometry", "FanVecGeometry", "ConeGeometry", "geom_to_str", "forward", "backward",
+    "adjoint", "TorchForward", "TorchBackprojection", "plan_2d", "plan_2d_vec", "plan_3d",
+    "forward_2d", "backward_2d", "forward_3d", "backward_3d", "backend",
 ]
 __version__ = "1.0.0"

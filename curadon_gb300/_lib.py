@@ -21,6 +21,9 @@ SIGNATURES = [
     ("cg_plan2d_create", C.c_int,
      [C.POINTER(C.c_void_p), C.c_int, C.c_uint32, u64p, f32p, f32p, C.c_uint32, C.c_uint64,
       C.c_float, C.c_float, f32p, f32p, f32p, C.c_uint64, C.c_float, C.c_float]),
+    ("cg_plan2d_create_vec", C.c_int,
+     [C.POINTER(C.c_void_p), C.c_int, C.c_uint32, u64p, f32p, f32p, C.c_uint32, C.c_uint64,
+      f32p, C.c_uint64]),
     ("cg_plan2d_destroy", C.c_int, [C.c_void_p]),
     ("cg_plan2d_get_forward_block", C.c_int, [C.c_void_p, u64p, u64p]),
     ("cg_plan2d_set_forward_block", C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64]),
@@ -29,6 +32,8 @@ SIGNATURES = [
     ("cg_plan2d_tables", C.c_int, [C.c_void_p, f32p, f32p, f32p]),
     ("cg_forward_2d", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cg_backward_2d", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("cg_forward_2d_ex", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    ("cg_backward_2d_ex", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("cg_adjoint_2d", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("cg_plan3d_create", C.c_int,
      [C.POINTER(C.c_void_p), C.c_int, u64p, f32p, f32p, f32p, f32p, f32p, C.c_uint64, u64p, f32p,
@@ -51,6 +56,12 @@ SIGNATURES = [
     ("cg_filter_rows", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint64, C.c_float,
       C.c_void_p]),
+    ("cg_batch2d_create", C.c_int,
+     [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+      C.POINTER(C.c_void_p), C.c_int]),
+    ("cg_batch2d_destroy", C.c_int, [C.c_void_p]),
+    ("cg_batch2d_forward", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("cg_batch2d_backward", C.c_int, [C.c_void_p, C.c_void_p]),
 ]
 
 CG_OK, CG_ERR_INVALID, CG_ERR_CUDA, CG_ERR_NOMEM, CG_ERR_UNSUPPORTED = range(5)

@@ -2,15 +2,18 @@
 
 Same names, argument order and meaning as the reference's bindings
 (python/standalone/src/bind.cpp:58-66, plan.cu:34-58, forward.cu:138-143,
-backward.cu:279-284).  Tensors are torch CUDA tensors, C-contiguous, float32;
-work is enqueued on torch's current stream of the tensors' device.
+backward.cu:279-284).  Tensors are torch CUDA tensors, C-contiguous; 2D
+volumes and sinograms are float32 or float16 (the volume's as the plan's
+vol_prec), 3D ones float32.  Work is enqueued on torch's current stream of
+the tensors' device.
 
 Error behaviour follows the reference's: mismatched devices raise
-``AttributeError`` (forward.cu:95-105), a dtype other than float32/float16
-raises ``TypeError`` (forward.cu:133-135), and precisions other than 16/32
-raise ``AttributeError`` (plan.cu:20-28); float16 plans raise
-``NotImplementedError`` here.  Unlike the reference, shapes are checked
-against the plan (the reference writes out of bounds instead).
+``AttributeError`` (forward.cu:95-105), a volume whose dtype differs from the
+plan's precision raises ``AttributeError`` (forward.cu:107-122), a dtype other
+than float32/float16 raises ``TypeError`` (forward.cu:133-135), and
+precisions other than 16/32 raise ``AttributeError`` (plan.cu:20-28).  Unlike
+the reference, shapes are checked against the plan (the reference writes out
+of bounds instead).
 """
 from __future__ import annotations
 
@@ -21,8 +24,8 @@ import torch
 
 from ._lib import check, load
 
-__all__ = ["plan_2d", "plan_3d", "forward_2d", "backward_2d", "adjoint_2d", "forward_3d",
-           "backward_3d"]
+__all__ = ["plan_2d", "plan_2d_vec", "plan_3d", "forward_2d", "backward_2d", "adjoint_2d",
+           "forward_3d", "backward_3d"]
 
 
 def _u64(a):
@@ -53,7 +56,7 @@ def _algo_index(name, names, what):
     return names.index(name)
 
 
-def _check_tensor(t, name: str, ndim: int | None = None):
+def _check_tensor(t, name: str, ndim: int | None = None, half: bool = False):
     if not isinstance(t, torch.Tensor):
         raise TypeError(f"{name} must be a torch.Tensor")
     if not t.is_cuda:
@@ -62,10 +65,14 @@ def _check_tensor(t, name: str, ndim: int | None = None):
         raise TypeError(f"{name} must be C-contiguous")
     if ndim is not None and t.dim() != ndim:
         raise TypeError(f"{name} must have {ndim} dimensions, got {t.dim()}")
-    if t.dtype == torch.float16:
-        raise NotImplementedError(f"{name}: float16 is not built (float32 only)")
-    if t.dtype != torch.float32:
+    if t.dtype == torch.float16 and not half:
+        raise NotImplementedError(f"{name}: float16 is only built for the 2D operators")
+    if t.dtype not in (torch.float32, torch.float16):
         raise TypeError("Only float32 is supported")
+
+
+def _bits(t: torch.Tensor) -> int:
+    return 16 if t.dtype == torch.float16 else 32
 
 
 class plan_2d:
@@ -95,6 +102,8 @@ class plan_2d:
         self._h = h
         self._L = L
         self.device_id = int(device)
+        self.vol_prec = int(vol_prec)
+        self.det_prec = int(det_prec)
         self.vol_shape = (int(shape_a[0]), int(shape_a[1]))
         self.det_count = int(det_count)
         self.nangles = n
@@ -151,13 +160,47 @@ class plan_2d:
         return [o.reshape(self.nangles, 2) for o in out]
 
 
+class plan_2d_vec(plan_2d):
+    """Fan-beam plan from per-view vectors (``cg_plan2d_create_vec``):
+    ``vecs`` is (nangles, 6) = [source.x, source.y, detector.x, detector.y,
+    u.x, u.y] as FanGeometry.to_vec returns them (geometry.py:54-80)."""
+
+    def __init__(self, device, vol_prec, vol_shape, vol_spacing, vol_offset, det_prec, det_count,
+                 vecs):
+        L = load()
+        if int(vol_prec) not in (16, 32) or int(det_prec) not in (16, 32):
+            raise AttributeError("Precision must either be f32 or f16")
+        v = np.ascontiguousarray(np.asarray(vecs, np.float32).reshape(-1, 6))
+        n = v.shape[0]
+        shape_a, shape_p = _u64(vol_shape)
+        sp_a, sp_p = _f32(vol_spacing)
+        off_a, off_p = _f32(vol_offset)
+        if shape_a.size != 2 or sp_a.size != 2 or off_a.size != 2:
+            raise TypeError("vol_shape, vol_spacing and vol_offset must have 2 entries")
+        h = C.c_void_p()
+        check(L.cg_plan2d_create_vec(C.byref(h), int(device), int(vol_prec), shape_p, sp_p, off_p,
+                                     int(det_prec), int(det_count),
+                                     v.ctypes.data_as(C.POINTER(C.c_float)), n))
+        self._h = h
+        self._L = L
+        self.device_id = int(device)
+        self.vol_prec = int(vol_prec)
+        self.det_prec = int(det_prec)
+        self.vol_shape = (int(shape_a[0]), int(shape_a[1]))
+        self.det_count = int(det_count)
+        self.nangles = n
+
+
 def _check_2d(vol, sino, plan: plan_2d):
-    _check_tensor(vol, "volume", 2)
-    _check_tensor(sino, "sinogram", 2)
+    _check_tensor(vol, "volume", 2, half=True)
+    _check_tensor(sino, "sinogram", 2, half=True)
     if vol.device != sino.device:
         raise AttributeError("Volume and sinogram must be on the same device")
     if vol.device.index != plan.device_id:
         raise AttributeError("Volume and plan are not on the same device")
+    if _bits(vol) != plan.vol_prec:
+        kind = "f16" if vol.dtype == torch.float16 else "f32"
+        raise AttributeError(f"Plan precision does not match volume precision ({kind})")
     if tuple(vol.shape) != plan.vol_shape:
         raise ValueError(f"volume shape {tuple(vol.shape)} != plan {plan.vol_shape}")
     if tuple(sino.shape) != (plan.nangles, plan.det_count):
@@ -168,21 +211,25 @@ def _check_2d(vol, sino, plan: plan_2d):
 def forward_2d(volume, sinogram, plan: plan_2d):
     """Overwrites ``sinogram`` (nangles, det) with the projection of ``volume``."""
     _check_2d(volume, sinogram, plan)
-    check(plan._L.cg_forward_2d(plan.handle, C.c_void_p(volume.data_ptr()),
-                                C.c_void_p(sinogram.data_ptr()), _stream(volume)))
+    check(plan._L.cg_forward_2d_ex(plan.handle, C.c_void_p(volume.data_ptr()),
+                                   C.c_void_p(sinogram.data_ptr()), _bits(sinogram),
+                                   _stream(volume)))
 
 
 def backward_2d(volume, sinogram, plan: plan_2d):
     """Adds the backprojection of ``sinogram`` to ``volume``."""
     _check_2d(volume, sinogram, plan)
-    check(plan._L.cg_backward_2d(plan.handle, C.c_void_p(volume.data_ptr()),
-                                 C.c_void_p(sinogram.data_ptr()), _stream(volume)))
+    check(plan._L.cg_backward_2d_ex(plan.handle, C.c_void_p(volume.data_ptr()),
+                                    C.c_void_p(sinogram.data_ptr()), _bits(sinogram),
+                                    _stream(volume)))
 
 
 def adjoint_2d(volume, sinogram, plan: plan_2d):
     """Adds the matched adjoint (exact transpose of ``forward_2d``) of
-    ``sinogram`` to ``volume``."""
+    ``sinogram`` to ``volume`` (float32 only)."""
     _check_2d(volume, sinogram, plan)
+    if volume.dtype != torch.float32 or sinogram.dtype != torch.float32:
+        raise TypeError("the matched adjoint takes float32 tensors")
     check(plan._L.cg_adjoint_2d(plan.handle, C.c_void_p(volume.data_ptr()),
                                 C.c_void_p(sinogram.data_ptr()), _stream(volume)))
 

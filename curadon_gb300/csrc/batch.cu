@@ -1,0 +1,138 @@
+// batch.cu -- many 2D problems per launch.
+//
+// Serving and iterative reconstruction run many small and medium problems
+// (n = 128 .. 1024) whose single launches leave most of the 152 SMs idle and
+// pay a launch each.  A batch binds a list of 2D plans to their volumes and
+// sinograms once; then each direction of the whole batch is two launches
+// (re-layout + operator) over a (problem, tile) work list, whatever the
+// number, sizes and geometries of the problems.  Bound buffers make the
+// calls stream-ordered and capturable in a CUDA graph (an iteration loop is
+// captured once and replayed).
+//
+// The batched forward is the register ray march (algorithm 0) and the
+// batched backprojection the staged one (algorithm 2), the FP32 algorithms
+// that need no per-problem texture; each problem uses its own plan's scratch,
+// so a plan may appear in one batch only once, and a batch must not overlap
+// on the GPU with other calls on its plans.
+#include <memory>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+struct cg_batch2d {
+    int device = 0;
+    int count = 0;
+    std::vector<cg::Plan2d *> plans;
+    cg::Prob2d *d_probs = nullptr;
+    int *d_starts = nullptr;  // 4 stages x (count + 1)
+    int totals[4] = {0, 0, 0, 0};
+};
+
+using namespace cg;
+
+namespace {
+
+void free_batch(cg_batch2d *b) {
+    if (b->d_probs) cudaFree(b->d_probs);
+    if (b->d_starts) cudaFree(b->d_starts);
+}
+
+}  // namespace
+
+extern "C" {
+
+int cg_batch2d_create(cg_batch2d **batch, cg_plan2d *const *plans, float *const *volumes,
+                      float *const *sinograms, int count) {
+    clear_error();
+    CG_REQUIRE(batch, "batch output pointer is NULL");
+    *batch = nullptr;
+    CG_REQUIRE(plans && volumes && sinograms, "plan, volume and sinogram lists must be given");
+    CG_REQUIRE(count > 0 && count <= (1 << 20), "count out of range");
+    std::set<const cg_plan2d *> seen;
+    for (int i = 0; i < count; ++i) {
+        CG_REQUIRE(plans[i] && volumes[i] && sinograms[i], "NULL plan or buffer in the batch");
+        CG_REQUIRE(plans[i]->device == plans[0]->device, "all plans of a batch share one device");
+        CG_REQUIRE(plans[i]->vol_bits == 32, "batches take float32 plans");
+        CG_REQUIRE(seen.insert(plans[i]).second, "a plan appears twice in one batch");
+    }
+    DeviceGuard guard(plans[0]->device);
+    CG_REQUIRE(guard.ok(), "cannot select the plans' device");
+
+    std::vector<Prob2d> probs(count);
+    std::vector<int> starts(4 * (count + 1), 0);
+    long long totals[4] = {0, 0, 0, 0};
+    for (int i = 0; i < count; ++i) {
+        const Plan2d &p = *plans[i];
+        Prob2d &q = probs[i];
+        q.vol = volumes[i], q.sino = sinograms[i];
+        q.src = p.d_src, q.u0 = p.d_u0, q.du = p.d_du, q.bproj = p.d_bproj;
+        q.layA = p.d_layA, q.layB = p.d_layB, q.sinoP = p.d_sinoP;
+        q.W = p.W, q.H = p.H, q.det = p.det, q.nangles = p.nangles;
+        q.pa = p.pitchA(), q.pb = p.pitchB();
+        q.sx = p.sx, q.sy = p.sy, q.ox = p.ox, q.oy = p.oy, q.ds = p.ds;
+        int blocks[4];
+        batch_blocks(p, blocks);
+        for (int st = 0; st < 4; ++st) {
+            starts[st * (count + 1) + i] = (int)totals[st];
+            totals[st] += blocks[st];
+            starts[st * (count + 1) + i + 1] = (int)totals[st];
+        }
+    }
+    for (long long t : totals)
+        CG_REQUIRE(t > 0 && t < (1ll << 31), "batch too large for one launch");
+
+    std::unique_ptr<cg_batch2d> b(new cg_batch2d());
+    b->device = plans[0]->device;
+    b->count = count;
+    b->plans.assign(plans, plans + count);
+    for (int st = 0; st < 4; ++st) b->totals[st] = (int)totals[st];
+    auto fail = [&](cudaError_t e) {
+        free_batch(b.get());
+        return set_error(e == cudaErrorMemoryAllocation ? CG_ERR_NOMEM : CG_ERR_CUDA,
+                         std::string("batch set-up: ") + cudaGetErrorString(e));
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&b->d_probs, sizeof(Prob2d) * count)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_starts, sizeof(int) * starts.size())) != cudaSuccess) return fail(e);
+    if ((e = cudaMemcpy(b->d_probs, probs.data(), sizeof(Prob2d) * count,
+                        cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail(e);
+    if ((e = cudaMemcpy(b->d_starts, starts.data(), sizeof(int) * starts.size(),
+                        cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail(e);
+    *batch = b.release();
+    return CG_OK;
+}
+
+int cg_batch2d_destroy(cg_batch2d *batch) {
+    clear_error();
+    if (!batch) return CG_OK;
+    {
+        DeviceGuard guard(batch->device);
+        free_batch(batch);
+    }
+    delete batch;
+    return CG_OK;
+}
+
+int cg_batch2d_forward(cg_batch2d *batch, void *stream) {
+    clear_error();
+    CG_REQUIRE(batch, "batch is NULL");
+    DeviceGuard guard(batch->device);
+    CG_REQUIRE(guard.ok(), "cannot select the batch's device");
+    return launch_batch2d(batch->d_probs, batch->d_starts, batch->totals, batch->count, true,
+                          (cudaStream_t)stream);
+}
+
+int cg_batch2d_backward(cg_batch2d *batch, void *stream) {
+    clear_error();
+    CG_REQUIRE(batch, "batch is NULL");
+    DeviceGuard guard(batch->device);
+    CG_REQUIRE(guard.ok(), "cannot select the batch's device");
+    return launch_batch2d(batch->d_probs, batch->d_starts, batch->totals, batch->count, false,
+                          (cudaStream_t)stream);
+}
+
+}  // extern "C"

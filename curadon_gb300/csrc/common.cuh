@@ -76,11 +76,21 @@ struct Plan2d {
     float *d_angles = nullptr, *d_DSO = nullptr, *d_DSD = nullptr;
     float2 *d_src = nullptr, *d_u0 = nullptr, *d_du = nullptr;
     float4 *d_bmeta = nullptr;        // (-sin, cos, DSD, DSO)
+    // backprojection as a projective map per view, 2 x nangles entries:
+    // [i] = (ax, ay, a0, -), [n + i] = (bx, by, b0, -); for the pixel's world
+    // position (X, Y): w = 1 / (ax X + ay Y + a0), u = (bx X + by Y + b0) w + det/2
+    float4 *d_bproj = nullptr;
+    bool vec = false;                 // per-view vectors (no angles / DSO / DSD)
 
     // scratch (device)
     float2 *d_layA = nullptr;         // (H+2P) rows x pitchA() pairs along x
     float2 *d_layB = nullptr;         // (W+2P) rows x pitchB() pairs along y
     float2 *d_sinoP = nullptr;        // nangles x (det+2P) pairs along u
+
+    // FP16 storage: precisions of the volume (plan) and FP32 staging of half
+    // data (allocated on first use)
+    int vol_bits = 32, det_bits = 32;
+    float *d_vol32 = nullptr, *d_sino32 = nullptr;
 
     // texture-unit variants (allocated on first use)
     cudaArray_t arr_vol = nullptr, arr_sino = nullptr;
@@ -90,15 +100,27 @@ struct Plan2d {
     // 2 = texture + registers, 3 = shared-memory row slabs, 4 = chunked
     // shared-memory slabs;
     // backprojection 0 = registers, 1 = texture unit, 2 = shared-memory rows.
-    // Defaults: the fastest measured on GB300 (2D n-sweep).
+    // Defaults: the fastest measured on GB300 (2D n-sweep); the forward
+    // becomes chunked for volumes of 1536^2 pixels and more (cg_plan2d_create).
     int algo_fwd = 1, algo_bwd = 2;
     int tex_eighths = 4;              // hybrid forward: share of warps on the texture unit
-    int fwd_chunk_rows = 4;           // chunked forward: chunk shape
+    int fwd_chunk_rows = 308;         // chunked forward: chunk shape
 
     // row pitches of layA / layB in pairs, even so every row starts on 16 bytes
     int pitchA() const { return (W + 2 * kPad + 1) & ~1; }
     int pitchB() const { return (H + 2 * kPad + 1) & ~1; }
     int pitchS() const { return det + 2 * kPad; }
+};
+
+// One problem of a 2D batch as the batched kernels see it.
+struct Prob2d {
+    float *vol;    // volume: forward input, backprojection accumulator
+    float *sino;   // sinogram: forward output, backprojection input
+    const float2 *src, *u0, *du;
+    const float4 *bproj;
+    float2 *layA, *layB, *sinoP;
+    int W, H, det, nangles, pa, pb;
+    float sx, sy, ox, oy, ds;
 };
 
 struct Plan3d {
@@ -141,8 +163,18 @@ void free_plan3d(Plan3d *p);
 int launch_plan2d_tables(Plan2d &p, cudaStream_t s);
 int launch_relayout2d(const Plan2d &p, const float *vol, cudaStream_t s);
 int launch_forward2d(const Plan2d &p, float *sino, cudaStream_t s);
-// scaled: rows multiplied by the view's DSD (the staged backprojector's input)
-int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s, bool scaled);
+// FP16 storage (half.cu)
+int ensure_half_scratch(Plan2d &p, bool vol, bool sino);
+int widen_half(const void *in, float *out, long long n, cudaStream_t s);
+int narrow_to_half(const float *in, void *out, long long n, cudaStream_t s);
+int add_into_half(void *vol, const float *add, long long n, cudaStream_t s);
+
+int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s);
+// batches (proj2d.cu): blocks of each stage of one problem, and the launch of
+// one direction over a batch whose starts hold 4 x (count + 1) block starts
+void batch_blocks(const Plan2d &p, int blocks[4]);
+int launch_batch2d(const Prob2d *probs, const int *starts, const int totals[4], int count,
+                   bool forward, cudaStream_t s);
 int launch_backward2d(const Plan2d &p, float *vol, cudaStream_t s);
 
 int ensure_plan3d_scratch(Plan3d &p, bool fwd, bool bwd);

@@ -86,13 +86,14 @@ extern "C" int cg_backward_2d_static(float *volume, const float *sinogram,
     const size_t off_u0 = align256(off_src + 8 * n);
     const size_t off_du = align256(off_u0 + 8 * n);
     const size_t off_meta = align256(off_du + 8 * n);
-    const size_t off_sino = align256(off_meta + 16 * n);
+    const size_t off_proj = align256(off_meta + 16 * n);
+    const size_t off_sino = align256(off_proj + 32 * n);
     const size_t total = off_sino + 8 * n * (det_count + 2 * kPad);
     if (total > kStaticScratchBytes)
         return set_error(CG_ERR_INVALID,
                          "problem needs " + std::to_string(total) + " bytes of scratch; the "
                          "static scratch holds " + std::to_string(kStaticScratchBytes) +
-                         " (nangles x (det_count + 4) x 8 bytes plus 60 bytes per view)");
+                         " (nangles x (det_count + 4) x 8 bytes plus 92 bytes per view)");
 
     void *base = nullptr;
     int rc = static_scratch(&base);
@@ -114,6 +115,7 @@ extern "C" int cg_backward_2d_static(float *volume, const float *sinogram,
     p.d_u0 = reinterpret_cast<float2 *>(b + off_u0);
     p.d_du = reinterpret_cast<float2 *>(b + off_du);
     p.d_bmeta = reinterpret_cast<float4 *>(b + off_meta);
+    p.d_bproj = reinterpret_cast<float4 *>(b + off_proj);
     p.d_sinoP = reinterpret_cast<float2 *>(b + off_sino);
     apply_algo_env(&p, nullptr);
 
@@ -122,7 +124,7 @@ extern "C" int cg_backward_2d_static(float *volume, const float *sinogram,
     CG_TRY_CUDA(cudaMemcpyAsync(p.d_DSO, DSO, 4 * n, cudaMemcpyHostToDevice, s));
     CG_TRY_CUDA(cudaMemcpyAsync(p.d_DSD, DSD, 4 * n, cudaMemcpyHostToDevice, s));
     if ((rc = launch_plan2d_tables(p, s))) return rc;
-    if ((rc = launch_relayout_sino2d(p, sinogram, s, p.algo_bwd == 2))) return rc;
+    if ((rc = launch_relayout_sino2d(p, sinogram, s))) return rc;
     if (p.algo_bwd == 2) return launch_backward2d_smem(p, volume, s);
     return launch_backward2d(p, volume, s);
 }

@@ -44,7 +44,7 @@ __global__ void k_plan2d_tables(int n, const float *__restrict__ ang,
                                 const float *__restrict__ DSO, const float *__restrict__ DSD,
                                 float det_ext, float ds, float doff, float sx, float sy,
                                 float ox, float oy, float extx, float exty, float2 *src,
-                                float2 *u0, float2 *du, float4 *bmeta) {
+                                float2 *u0, float2 *du, float4 *bmeta, float4 *bproj) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float a = ang[i], dso = DSO[i], dsd = DSD[i];
@@ -65,18 +65,23 @@ __global__ void k_plan2d_tables(int n, const float *__restrict__ ang,
     // (-sin, cos, DSD, DSO) as the backprojector's shared table
     // (backward_2d.hpp:45-55), with the same intrinsics.
     bmeta[i] = make_float4(-__sinf(a), __cosf(a), dsd, dso);
+    // the same map as a projective table: den = (x' + DSO) / DSD, so that
+    // w = 1 / den, and yi = (cos X - sin Y) / ds, so that u = yi w + det/2
+    const float rd = 1.0f / dsd, rs = 1.0f / ds;
+    bproj[i] = make_float4(-sn * rd, -cs * rd, dso * rd, 0.f);
+    bproj[n + i] = make_float4(cs * rs, -sn * rs, 0.f, 0.f);
 }
 
 // ------------------------------------------------------------ re-layouts
 
 constexpr int kTile = 32;
 
-// Writes layA and layB for one 32 x 32 tile of padded texel space.
-__global__ void __launch_bounds__(256)
-    k_relayout2d(const float *__restrict__ vol, int W, int H, float2 *__restrict__ A,
-                 float2 *__restrict__ B, int pa, int pb) {
+// Writes layA and layB for the 32 x 32 tile (bx, by) of padded texel space.
+__device__ __forceinline__ void relayout2d_tile(const float *__restrict__ vol, int W, int H,
+                                                float2 *__restrict__ A, float2 *__restrict__ B,
+                                                int pa, int pb, int bx, int by) {
     __shared__ float tile[kTile + 1][kTile + 1];
-    const int x0 = blockIdx.x * kTile - kPad, y0 = blockIdx.y * kTile - kPad;
+    const int x0 = bx * kTile - kPad, y0 = by * kTile - kPad;
     for (int j = threadIdx.y; j < kTile + 1; j += blockDim.y)
         for (int i = threadIdx.x; i < kTile + 1; i += blockDim.x) {
             const int x = x0 + i, y = y0 + j;
@@ -98,21 +103,28 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-__global__ void k_relayout_sino2d(const float *__restrict__ sino, int det, int nangles,
-                                  float2 *__restrict__ S, const float4 *__restrict__ meta) {
+__global__ void __launch_bounds__(256)
+    k_relayout2d(const float *__restrict__ vol, int W, int H, float2 *__restrict__ A,
+                 float2 *__restrict__ B, int pa, int pb) {
+    relayout2d_tile(vol, W, H, A, B, pa, pb, blockIdx.x, blockIdx.y);
+}
+
+__device__ __forceinline__ void relayout_sino2d_elem(const float *__restrict__ sino, int det,
+                                                     int nangles, float2 *__restrict__ S,
+                                                     long long idx) {
     const int pitch = det + 2 * kPad;
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)pitch * nangles) return;
     const int a = (int)(idx / pitch);
     const int k = (int)(idx % pitch) - kPad;
     const float *row = sino + (size_t)a * det;
-    float t0 = (k >= 0 && k < det) ? row[k] : 0.f;
-    float t1 = (k + 1 >= 0 && k + 1 < det) ? row[k + 1] : 0.f;
-    if (meta) {  // rows pre-scaled by the view's DSD
-        const float dsd = meta[a].z;
-        t0 *= dsd, t1 *= dsd;
-    }
+    const float t0 = (k >= 0 && k < det) ? row[k] : 0.f;
+    const float t1 = (k + 1 >= 0 && k + 1 < det) ? row[k + 1] : 0.f;
     S[idx] = make_float2(t0, t1 - t0);
+}
+
+__global__ void k_relayout_sino2d(const float *__restrict__ sino, int det, int nangles,
+                                  float2 *__restrict__ S) {
+    relayout_sino2d_elem(sino, det, nangles, S, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ------------------------------------------------------------ forward
@@ -122,13 +134,14 @@ __global__ void k_relayout_sino2d(const float *__restrict__ sino, int det, int n
 // then rint(max|rd|) unit steps along the dominant axis.  Along that axis the
 // step is exactly +-1, so the row index advances by one and the vertical
 // filter weight stays fixed; the two row sums are blended once at the end.
-__global__ void __launch_bounds__(256)
-    k_fwd2d(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
-            float *__restrict__ sino, const float2 *__restrict__ tsrc,
-            const float2 *__restrict__ tu0, const float2 *__restrict__ tdu, int W, int H,
-            int det, int nangles, float sx, float sy, int pa, int pb) {
-    const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    const int view = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void fwd2d_ray(const float2 *__restrict__ layA,
+                                          const float2 *__restrict__ layB,
+                                          float *__restrict__ sino,
+                                          const float2 *__restrict__ tsrc,
+                                          const float2 *__restrict__ tu0,
+                                          const float2 *__restrict__ tdu, int W, int H, int det,
+                                          int nangles, float sx, float sy, int pa, int pb, int u,
+                                          int view) {
     if (u >= det || view >= nangles) return;
     const float2 s = tsrc[view], o = tu0[view], du = tdu[view];
     const float fu = (float)u;
@@ -190,6 +203,15 @@ __global__ void __launch_bounds__(256)
     }
     const float acc = fmaf(fq, acc_hi - acc_lo, acc_lo);
     *out = acc * hypotf(vx * sx, vy * sy);
+}
+
+__global__ void __launch_bounds__(256)
+    k_fwd2d(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
+            float *__restrict__ sino, const float2 *__restrict__ tsrc,
+            const float2 *__restrict__ tu0, const float2 *__restrict__ tdu, int W, int H,
+            int det, int nangles, float sx, float sy, int pa, int pb) {
+    fwd2d_ray(layA, layB, sino, tsrc, tu0, tdu, W, H, det, nangles, sx, sy, pa, pb,
+              blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
 }
 
 // ------------------------------------------------------------ forward, slab
@@ -731,33 +753,32 @@ constexpr int kSmWin = 128;   // pairs of one view's row staged for a tile
 // the block stages that window of the difference-encoded pair row, and every
 // pixel samples it there; a view whose window exceeds kSmWin pairs is read
 // from global memory instead.  Per (pixel, view) the reference's quantities
-// (backward_2d.hpp:61-96) are formed with the per-view terms hoisted:
-//   x' + DSO = -cos Y + (-sin X + DSO),  yi = -sin SY + cos SX,
-//   w = DSD / (x' + DSO),  u = w yi + det/2,
-// then one 8-byte shared load and two FMAs.  The rows were pre-scaled by
-// DSD, so the weight is the reciprocal 1 / (x' + DSO) and u = (DSD yi) / (x' +
-// DSO) + det/2 with DSD folded into the per-view terms.
-__global__ void __launch_bounds__(256)
-    k_bwd2d_smem(float *__restrict__ vol, const float2 *__restrict__ S,
-                 const float4 *__restrict__ meta, int W, int H, int det, int nangles, float sx,
-                 float sy, float ox, float oy, float ds) {
+// (backward_2d.hpp:61-96) come from the view's projective table
+// (den, yi affine in the pixel's world position X, Y):
+//   w = 1 / den = DSD / (x' + DSO),  u = yi w + det/2,
+// with the per-view terms of each thread's column hoisted, then one
+// reciprocal, one 8-byte shared load and two FMAs.  The same table describes
+// an arbitrary per-view source / detector placement (vector geometry).
+__device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
+                                                const float2 *__restrict__ S,
+                                                const float4 *__restrict__ proj, int W, int H,
+                                                int det, int nangles, float sx, float sy, float ox,
+                                                float oy, float ds, int bx, int by) {
     __shared__ float2 srow[kSmViews][kSmWin];
-    __shared__ float4 smeta[kSmViews];
+    __shared__ float4 sA[kSmViews], sB[kSmViews];
     __shared__ int skmin[kSmViews];
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int xt = blockIdx.x * 32, yt = blockIdx.y * (8 * kSmRows);
+    const int xt = bx * 32, yt = by * (8 * kSmRows);
     const int x = xt + threadIdx.x;
     const int y0 = yt + threadIdx.y;
     const float ex = (float)W / 2.0f, ey = (float)H / 2.0f;
     const float edm = (float)det / 2.0f - 0.5f;
     const float inv = __fdividef(1.0f, ds);
     const float X = ((float)x - ex) * sx + ox + 0.5f;
-    const float SX = X * inv;
-    float Y[kSmRows], SY[kSmRows], acc[kSmRows];
+    float Y[kSmRows], acc[kSmRows];
 #pragma unroll
     for (int r = 0; r < kSmRows; ++r) {
         Y[r] = ((float)(y0 + 8 * r) - ey) * sy + oy + 0.5f;
-        SY[r] = Y[r] * inv;
         acc[r] = 0.f;
     }
     const int pitch = det + 2 * kPad;
@@ -765,26 +786,26 @@ __global__ void __launch_bounds__(256)
         const int nv = min(kSmViews, nangles - v0);
         __syncthreads();
         if (tid < nv) {
-            const float4 m = meta[v0 + tid];  // (-sin, cos, DSD, DSO)
-            smeta[tid] = m;
+            const float4 a = proj[v0 + tid], b = proj[nangles + v0 + tid];
+            sA[tid] = a, sB[tid] = b;
             float lo = FLT_MAX, hi = -FLT_MAX, dmin = FLT_MAX;
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 const float cX = ((float)(xt + (c & 1) * 31) - ex) * sx + ox + 0.5f;
                 const float cY = ((float)(yt + (c >> 1) * (8 * kSmRows - 1)) - ey) * sy + oy + 0.5f;
-                const float den = fmaf(-m.y, cY, fmaf(m.x, cX, m.w));
-                const float yi = fmaf(m.x, cY * inv, m.y * (cX * inv));
-                const float ub = fmaf(__fdividef(m.z, den), yi, edm);
+                const float den = fmaf(a.y, cY, fmaf(a.x, cX, a.z));
+                const float yi = fmaf(b.y, cY, fmaf(b.x, cX, b.z));
+                const float ub = fmaf(__fdividef(1.0f, den), yi, edm);
                 lo = fminf(lo, ub);
                 hi = fmaxf(hi, ub);
                 dmin = fminf(dmin, den);
             }
             // the window bound holds when the tile lies wholly in front of the
-            // source (x' + DSO > 0 at every corner, hence on the whole tile)
+            // source (den > 0 at every corner, hence on the whole tile)
             int k0 = INT_MIN;
             if (dmin > 0.f && lo >= -1e6f && hi <= 1e6f) {
-                const int a = (int)floorf(lo) - 1, b = (int)floorf(hi) + 1;
-                if (b - a + 1 <= kSmWin) k0 = a;
+                const int a0 = (int)floorf(lo) - 1, a1 = (int)floorf(hi) + 1;
+                if (a1 - a0 + 1 <= kSmWin) k0 = a0;
             }
             skmin[tid] = k0;
         }
@@ -799,37 +820,36 @@ __global__ void __launch_bounds__(256)
         __syncthreads();
 #pragma unroll 2
         for (int j = 0; j < nv; ++j) {
-            const float4 m = smeta[j];
+            const float4 a = sA[j], b = sB[j];
             const int k0 = skmin[j];
-            const float A = fmaf(m.x, X, m.w), nc = -m.y;
-            const float mx = m.x * m.z, B = (m.y * m.z) * SX;
+            const float A = fmaf(a.x, X, a.z), B = fmaf(b.x, X, b.z);
             if (k0 != INT_MIN) {
                 const float2 *sr = srow[j];
 #pragma unroll
                 for (int r = 0; r < kSmRows; ++r) {
-                    const float den = fmaf(nc, Y[r], A);
-                    const float yi = fmaf(mx, SY[r], B);
+                    const float den = fmaf(a.y, Y[r], A);
+                    const float yi = fmaf(b.y, Y[r], B);
                     const float w = __fdividef(1.0f, den);
                     const float ub = fmaf(w, yi, edm);
                     const float kf = floorf(ub);
-                    const float a = ub - kf;
+                    const float f = ub - kf;
                     const unsigned li = min((unsigned)((int)kf - k0), (unsigned)(kSmWin - 1));
                     const float2 t = sr[li];
-                    acc[r] = fmaf(fmaf(a, t.y, t.x), w, acc[r]);
+                    acc[r] = fmaf(fmaf(f, t.y, t.x), w, acc[r]);
                 }
             } else {
                 const float2 *row = S + (size_t)(v0 + j) * pitch;
 #pragma unroll
                 for (int r = 0; r < kSmRows; ++r) {
-                    const float den = fmaf(nc, Y[r], A);
-                    const float yi = fmaf(mx, SY[r], B);
+                    const float den = fmaf(a.y, Y[r], A);
+                    const float yi = fmaf(b.y, Y[r], B);
                     const float w = __fdividef(1.0f, den);
                     const float ub = fmaf(w, yi, edm);
                     const float kf = floorf(ub);
-                    const float a = ub - kf;
+                    const float f = ub - kf;
                     const unsigned col = min((unsigned)((int)kf + kPad), (unsigned)(det + kPad));
                     const float2 t = __ldg(row + col);
-                    acc[r] = fmaf(fmaf(a, t.y, t.x), w, acc[r]);
+                    acc[r] = fmaf(fmaf(f, t.y, t.x), w, acc[r]);
                 }
             }
         }
@@ -843,7 +863,97 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+__global__ void __launch_bounds__(256)
+    k_bwd2d_smem(float *__restrict__ vol, const float2 *__restrict__ S,
+                 const float4 *__restrict__ proj, int W, int H, int det, int nangles, float sx,
+                 float sy, float ox, float oy, float ds) {
+    bwd2d_smem_tile(vol, S, proj, W, H, det, nangles, sx, sy, ox, oy, ds, blockIdx.x, blockIdx.y);
+}
+
 }  // namespace
+
+namespace {
+
+// ------------------------------------------------------------ batches
+
+// A batch runs every stage of many 2D problems (any sizes, geometries) as
+// one launch over a work list: stage s of problem i owns the blocks
+// [start[s][i], start[s][i + 1]) of the launch, and each block finds its
+// problem by binary search over those starts, then runs the single-problem
+// tile or ray code on it.
+__device__ __forceinline__ int batch_problem(const int *__restrict__ start, int count, int b) {
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {  // last i with start[i] <= b
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256)
+    k_batch_relayout2d(const Prob2d *__restrict__ probs, const int *__restrict__ start, int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob2d &q = probs[i];
+    const int local = blockIdx.x - start[i];
+    const int gx = (q.W + 2 * kPad + kTile - 1) / kTile;
+    relayout2d_tile(q.vol, q.W, q.H, q.layA, q.layB, q.pa, q.pb, local % gx, local / gx);
+}
+
+__global__ void __launch_bounds__(256)
+    k_batch_fwd2d(const Prob2d *__restrict__ probs, const int *__restrict__ start, int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob2d &q = probs[i];
+    const int local = blockIdx.x - start[i];
+    const int gx = (q.det + 31) / 32;
+    fwd2d_ray(q.layA, q.layB, q.sino, q.src, q.u0, q.du, q.W, q.H, q.det, q.nangles, q.sx, q.sy,
+              q.pa, q.pb, (local % gx) * 32 + threadIdx.x, (local / gx) * 8 + threadIdx.y);
+}
+
+__global__ void __launch_bounds__(256)
+    k_batch_relayout_sino2d(const Prob2d *__restrict__ probs, const int *__restrict__ start,
+                            int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob2d &q = probs[i];
+    const long long idx = (long long)(blockIdx.x - start[i]) * blockDim.x + threadIdx.x;
+    relayout_sino2d_elem(q.sino, q.det, q.nangles, q.sinoP, idx);
+}
+
+__global__ void __launch_bounds__(256)
+    k_batch_bwd2d(const Prob2d *__restrict__ probs, const int *__restrict__ start, int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob2d &q = probs[i];
+    const int local = blockIdx.x - start[i];
+    const int gx = (q.W + 31) / 32;
+    bwd2d_smem_tile(q.vol, q.sinoP, q.bproj, q.W, q.H, q.det, q.nangles, q.sx, q.sy, q.ox, q.oy,
+                    q.ds, local % gx, local / gx);
+}
+
+}  // namespace
+
+// Blocks of each batched stage for one problem (the launch shapes of the
+// single-problem kernels above).
+void batch_blocks(const Plan2d &p, int blocks[4]) {
+    blocks[0] = ceil_div(p.W + 2 * kPad, kTile) * ceil_div(p.H + 2 * kPad, kTile);
+    blocks[1] = ceil_div(p.det, 32) * ceil_div(p.nangles, 8);
+    blocks[2] = (int)ceil_div((long long)p.pitchS() * p.nangles, 256);
+    blocks[3] = ceil_div(p.W, 32) * ceil_div(p.H, 8 * kSmRows);
+}
+
+int launch_batch2d(const Prob2d *probs, const int *starts, const int totals[4], int count,
+                   bool forward, cudaStream_t s) {
+    const dim3 tile(32, 8);
+    if (forward) {
+        k_batch_relayout2d<<<totals[0], tile, 0, s>>>(probs, starts, count);
+        CG_TRY_CUDA(cudaGetLastError());
+        k_batch_fwd2d<<<totals[1], tile, 0, s>>>(probs, starts + (count + 1), count);
+    } else {
+        k_batch_relayout_sino2d<<<totals[2], 256, 0, s>>>(probs, starts + 2 * (count + 1), count);
+        CG_TRY_CUDA(cudaGetLastError());
+        k_batch_bwd2d<<<totals[3], tile, 0, s>>>(probs, starts + 3 * (count + 1), count);
+    }
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
 
 // ------------------------------------------------------------ launchers
 
@@ -852,7 +962,7 @@ int launch_plan2d_tables(Plan2d &p, cudaStream_t s) {
     const float extx = (float)p.W * p.sx, exty = (float)p.H * p.sy;
     k_plan2d_tables<<<ceil_div(p.nangles, 128), 128, 0, s>>>(
         p.nangles, p.d_angles, p.d_DSO, p.d_DSD, det_ext, p.ds, p.doff, p.sx, p.sy, p.ox, p.oy,
-        extx, exty, p.d_src, p.d_u0, p.d_du, p.d_bmeta);
+        extx, exty, p.d_src, p.d_u0, p.d_du, p.d_bmeta, p.d_bproj);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }
@@ -875,17 +985,16 @@ int launch_forward2d(const Plan2d &p, float *sino, cudaStream_t s) {
     return CG_OK;
 }
 
-int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s, bool scaled) {
+int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s) {
     const long long n = (long long)p.pitchS() * p.nangles;
-    k_relayout_sino2d<<<ceil_div(n, 256), 256, 0, s>>>(sino, p.det, p.nangles, p.d_sinoP,
-                                                       scaled ? p.d_bmeta : nullptr);
+    k_relayout_sino2d<<<ceil_div(n, 256), 256, 0, s>>>(sino, p.det, p.nangles, p.d_sinoP);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }
 
 int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s) {
     dim3 grid(ceil_div(p.W, 32), ceil_div(p.H, 8 * kSmRows));
-    k_bwd2d_smem<<<grid, dim3(32, 8), 0, s>>>(vol, p.d_sinoP, p.d_bmeta, p.W, p.H, p.det,
+    k_bwd2d_smem<<<grid, dim3(32, 8), 0, s>>>(vol, p.d_sinoP, p.d_bproj, p.W, p.H, p.det,
                                               p.nangles, p.sx, p.sy, p.ox, p.oy, p.ds);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;

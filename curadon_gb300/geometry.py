@@ -17,7 +17,8 @@ from typing import Any, List, Optional, Tuple, Union
 
 import numpy as np
 
-__all__ = ["FanGeometry", "ConeGeometry", "geom_to_str", "is_convertible_to_float"]
+__all__ = ["FanGeometry", "FanVecGeometry", "ConeGeometry", "geom_to_str",
+           "is_convertible_to_float"]
 
 
 def is_convertible_to_float(val: Any) -> bool:
@@ -163,9 +164,14 @@ class FanGeometry:
         return vecs
 
     @staticmethod
-    def from_vec(vol_shape: Tuple[int, int], det_shape: int, vecs: List[List[float]], **kwargs):
+    def from_vec(vol_shape: Tuple[int, int], det_shape: int, vecs: List[List[float]],
+                 lossless: bool = False, **kwargs):
         """FanGeometry from ASTRA-like vectors (geometry.py:84-134): keeps the
-        angle, |src| and |src - det| of each view and one detector spacing."""
+        angle, |src| and |src - det| of each view and one detector spacing.
+        ``lossless=True`` (an addition) keeps the vectors themselves instead
+        (``FanVecGeometry``)."""
+        if lossless:
+            return FanVecGeometry(vol_shape, det_shape, vecs, **kwargs)
         vecs = np.asarray(vecs, dtype=np.float64)
         det_spacing = float(np.linalg.norm(vecs[0][-2:]))
         dsd, dso, angles = [], [], []
@@ -186,6 +192,42 @@ class FanGeometry:
 
     def __str__(self):
         return geom_to_str(self)
+
+
+class FanVecGeometry(FanGeometry):
+    """2D fan-beam geometry given by per-view vectors, kept as given.
+
+    ``vecs`` is (nangles, 6): [source.x, source.y, detector.x, detector.y,
+    u.x, u.y] in the world frame of ``FanGeometry.to_vec`` (x along the
+    volume's width), with ``u`` the step from one detector cell centre to the
+    next (its length is the detector spacing, equal for all views).  The
+    reference's ``from_vec`` reduces such vectors to angles / DSO / DSD and so
+    loses per-view shifts of source and detector (e.g. calibrated or jittered
+    trajectories); here the plan uses the vectors themselves
+    (``cg_plan2d_create_vec``).  ``angles``, ``DSO``, ``DSD`` and
+    ``det_spacing`` hold that reduction for information."""
+
+    def __init__(self, vol_shape: Tuple[int, int], det_shape: int, vecs,
+                 vol_spacing: Optional[Tuple[float, float]] = None,
+                 vol_offset: Optional[Tuple[float, float]] = None, device: int = 0,
+                 vol_prec: int = 32, sino_prec: int = 32):
+        v = np.asarray(vecs, dtype=np.float64)
+        if v.ndim != 2 or v.shape[1] != 6 or v.shape[0] == 0:
+            raise AttributeError(f"vecs must be (nangles, 6), got {v.shape}")
+        reduced = FanGeometry.from_vec(vol_shape, det_shape, v, vol_spacing=vol_spacing,
+                                       vol_offset=vol_offset, device=device, vol_prec=vol_prec,
+                                       sino_prec=sino_prec)
+        self.__dict__.update(reduced.__dict__)
+        self.vecs = v
+
+    def _make_plan(self):
+        from .backend import plan_2d_vec
+
+        return plan_2d_vec(self.device, self.vol_prec, self.vol_shape, self.vol_spacing,
+                           self.vol_offset, self.sino_prec, self.det_shape, self.vecs)
+
+    def to_vec(self):
+        return self.vecs.tolist()
 
 
 class ConeGeometry:

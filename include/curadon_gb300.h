@@ -38,7 +38,7 @@ extern "C" {
 #define CG_ERR_INVALID 1     /* bad argument: null pointer, shape, size      */
 #define CG_ERR_CUDA 2        /* a CUDA runtime call or launch failed         */
 #define CG_ERR_NOMEM 3       /* device allocation failed                     */
-#define CG_ERR_UNSUPPORTED 4 /* valid in the reference, not built here (f16) */
+#define CG_ERR_UNSUPPORTED 4 /* valid in the reference, not built here       */
 
 /* Message of the last failed call on this thread ("" if none). */
 const char *cg_last_error(void);
@@ -55,7 +55,9 @@ typedef struct cg_plan2d cg_plan2d;
  * and detector step are precomputed on the device exactly as
  * plan_2d::precompute does (plan_2d.hpp:189-241), and the scratch the
  * operators need is allocated here, once.  vol_prec / det_prec are bit widths
- * (32; 16 is valid in the reference and returns CG_ERR_UNSUPPORTED here).
+ * (32 or 16, plan.cu:20-28): vol_prec is the element type of every volume
+ * passed with this plan (float or IEEE half); det_prec is recorded, and the
+ * sinogram's type is given per call, as the reference reads it from the array.
  * vol_shape / vol_spacing / vol_offset are in Python order (y, x).
  * det_pitch and COR are accepted and, as in the reference, unused. */
 int cg_plan2d_create(cg_plan2d **plan, int device, uint32_t vol_prec,
@@ -63,6 +65,23 @@ int cg_plan2d_create(cg_plan2d **plan, int device, uint32_t vol_prec,
                      const float vol_offset[2], uint32_t det_prec, uint64_t det_count,
                      float det_spacing, float det_offset, const float *DSO, const float *DSD,
                      const float *angles, uint64_t nangles, float det_pitch, float COR);
+
+/* Fan-beam plan from per-view vectors: vecs holds nangles x 6 floats
+ * [source.x, source.y, detector_centre.x, detector_centre.y, u.x, u.y] in
+ * the layout of the reference's FanGeometry.to_vec / from_vec
+ * (geometry.py:54-134; x along the volume's width, u the step from one
+ * detector cell centre to the next).  The reference reduces such vectors to
+ * angles / DSO / DSD (from_vec, losing per-view shifts of source and
+ * detector); this plan keeps them: the forward marches the rays the vectors
+ * define and the backprojection maps each pixel through the view's own
+ * projective map.  For vectors made by to_vec from a circular geometry the
+ * results equal cg_plan2d_create's within FP32 rounding.  All views must
+ * share one |u| (the detector spacing).  The backprojection uses the staged
+ * algorithm (2).  No counterpart call in the reference. */
+int cg_plan2d_create_vec(cg_plan2d **plan, int device, uint32_t vol_prec,
+                         const uint64_t vol_shape[2], const float vol_spacing[2],
+                         const float vol_offset[2], uint32_t det_prec, uint64_t det_count,
+                         const float *vecs, uint64_t nangles);
 
 /* Frees the plan and its device memory (plan_2d destructor). */
 int cg_plan2d_destroy(cg_plan2d *plan);
@@ -93,19 +112,32 @@ int cg_plan2d_get_algorithm(const cg_plan2d *plan, int *forward, int *backward);
 int cg_plan2d_tables(const cg_plan2d *plan, float *sources, float *u_origins, float *delta_us);
 
 /* 2D ray-driven forward projection.  Replaces `forward_2d(volume, sinogram,
- * plan)` (forward.cu:92-139 -> fp::forward_2d, forward_2d.hpp:135-139). */
+ * plan)` (forward.cu:92-139 -> fp::forward_2d, forward_2d.hpp:135-139) for a
+ * float32 sinogram; `volume` holds the plan's vol_prec. */
 int cg_forward_2d(cg_plan2d *plan, const float *volume, float *sinogram, void *stream);
 
 /* 2D voxel-driven backprojection, accumulating into `volume`.  Replaces
  * `backward_2d(volume, sinogram, plan)` (backward.cu:233-280 ->
- * bp::backproject_2d, backward_2d.hpp:302-306). */
+ * bp::backproject_2d, backward_2d.hpp:302-306) for a float32 sinogram. */
 int cg_backward_2d(cg_plan2d *plan, float *volume, const float *sinogram, void *stream);
+
+/* The same two operators with the sinogram's element type given: sino_bits
+ * 32 (float) or 16 (IEEE half); the volume's is the plan's vol_prec.  These
+ * are the four typed instantiations of forward_2d_cuda_typed /
+ * backward_2d_cuda_typed (forward.cu:77-135, backward.cu:75-135).  Half data
+ * is widened to FP32, every computation is FP32, a half sinogram gets each
+ * ray sum rounded to nearest and a half volume gets half(acc / ds) added in
+ * half arithmetic, as the reference's kernels store to __half. */
+int cg_forward_2d_ex(cg_plan2d *plan, const void *volume, void *sinogram, int sino_bits,
+                     void *stream);
+int cg_backward_2d_ex(cg_plan2d *plan, void *volume, const void *sinogram, int sino_bits,
+                      void *stream);
 
 /* Matched adjoint of cg_forward_2d, accumulating A^T sinogram into `volume`:
  * the exact transpose of the ray-driven interpolation (same rays, sample
  * points and weights), for gradients and solvers that need <Ax,y> = <x,A^T y>.
  * No counterpart call in the reference, whose backward of the forward is the
- * voxel-driven backprojector (diffable.py:21-24). */
+ * voxel-driven backprojector (diffable.py:21-24).  float32 plans only. */
 int cg_adjoint_2d(cg_plan2d *plan, float *volume, const float *sinogram, void *stream);
 
 /* ------------------------------------------------------------------ 3D -- */
@@ -179,7 +211,7 @@ int cg_backward_3d(float *x, const uint64_t vol_shape[3], const float vol_spacin
  * det_offset, which the backprojection does not use), accumulating into
  * `volume`; all scratch lives in one 16 MiB device array that the library
  * holds on every GPU that loads it, so problems needing more --
- * nangles * (det_count + 4) * 8 bytes plus 60 bytes per view -- are rejected
+ * nangles * (det_count + 4) * 8 bytes plus 92 bytes per view -- are rejected
  * with CG_ERR_INVALID.  The first call on a device looks the array up (make
  * it before any stream capture).  All calls share the array: calls that
  * overlap on the GPU race and must be ordered by the caller. */
@@ -200,6 +232,27 @@ int cg_backward_2d_static(float *volume, const float *sinogram, const uint64_t v
  * device pointers; out must not alias in.  ncols <= 29056. */
 int cg_filter_rows(const float *in, float *out, const float *h, const float *pre, uint64_t nrows,
                    uint64_t ncols, float scale, void *stream);
+
+/* ------------------------------------------------------------- batches -- */
+
+/* A batch binds `count` float32 2D plans (any sizes and geometries, each
+ * plan at most once) to their device volumes and sinograms.  Each direction
+ * of the whole batch then runs as two launches over a (problem, tile) work
+ * list instead of two launches per problem: the serving / many-problem entry
+ * point, capturable in a CUDA graph because the buffers are bound.  The
+ * batched forward is the register ray march (algorithm 0), the batched
+ * backprojection the staged one (algorithm 2); results equal cg_forward_2d /
+ * cg_backward_2d with those algorithms bit for bit.  A batch must not run
+ * concurrently with other calls on its plans.  No counterpart call in the
+ * reference, which runs one problem per call. */
+typedef struct cg_batch2d cg_batch2d;
+int cg_batch2d_create(cg_batch2d **batch, cg_plan2d *const *plans, float *const *volumes,
+                      float *const *sinograms, int count);
+int cg_batch2d_destroy(cg_batch2d *batch);
+/* sinogram_i = A_i volume_i for every problem (overwrites the sinograms) */
+int cg_batch2d_forward(cg_batch2d *batch, void *stream);
+/* volume_i += A_i^T sinogram_i for every problem */
+int cg_batch2d_backward(cg_batch2d *batch, void *stream);
 
 #ifdef __cplusplus
 }

@@ -79,6 +79,10 @@ def lib():
             f.argtypes = [C.POINTER(Cone3d), _f32p, _f64p, C.c_int, C.c_int]
             f.restype = C.c_int
         L.or_fan2d_tables.argtypes = [C.POINTER(Fan2d), _f64p, _f64p, _f64p]
+        L.or_fan2d_vec_tables.argtypes = [C.POINTER(Fan2d), _f64p, _f64p, _f64p, _f64p]
+        L.or_fwd2d_vec.argtypes = [C.POINTER(Fan2d), _f64p, _f32p, _f64p, C.c_int, C.c_int]
+        L.or_bwd2d_vec.argtypes = [C.POINTER(Fan2d), _f64p, _f32p, _f64p, C.c_int, C.c_int]
+        L.or_fwd2d_vec.restype = L.or_bwd2d_vec.restype = C.c_int
         L.or_cone3d_fwd_tables.argtypes = [C.POINTER(Cone3d), _f64p, _f64p, _f64p, _f64p]
         L.or_cone3d_bwd_tables.argtypes = [C.POINTER(Cone3d)] + [_f64p] * 5
         _lib = L
@@ -162,6 +166,55 @@ def bwd2d(g, sino, vol0=None, quant: int = 0, nthreads: int | None = None) -> np
     return out
 
 
+def _vec_struct(g, vecs):
+    """Fan struct for per-view vectors (nangles, 6); det_spacing = |u| of view 0."""
+    v = np.ascontiguousarray(np.asarray(vecs, np.float64).reshape(-1, 6))
+    n = v.shape[0]
+    h = dict(g)
+    h["angles"] = np.zeros(n, np.float32)
+    h["DSO"] = np.ones(n, np.float32)
+    h["DSD"] = np.full(n, 2.0, np.float32)
+    h["det_spacing"] = float(np.hypot(v[0, 4], v[0, 5]))
+    h["det_offset"] = 0.0
+    s, keep = fan_struct(h)
+    return s, keep, v
+
+
+def fan_vec_tables(g, vecs):
+    """FP64 (sources, u_origins, delta_us) of a vector geometry, each (nangles, 2)."""
+    s, keep, v = _vec_struct(g, vecs)
+    n = s.nangles
+    src, u0, du = (np.zeros(2 * n) for _ in range(3))
+    lib().or_fan2d_vec_tables(C.byref(s), v, src, u0, du)
+    del keep
+    return src.reshape(n, 2), u0.reshape(n, 2), du.reshape(n, 2)
+
+
+def fwd2d_vec(g, vecs, vol, quant: int = 0, nthreads: int | None = None) -> np.ndarray:
+    """Forward projection of a (H, W) volume through per-view vectors
+    [S.x, S.y, C.x, C.y, U.x, U.y]; g supplies vol_shape, det_shape and the
+    voxel spacing / offset."""
+    s, keep, v = _vec_struct(g, vecs)
+    vv = np.ascontiguousarray(vol, dtype=np.float32)
+    out = np.zeros((s.nangles, s.det_count), np.float64)
+    lib().or_fwd2d_vec(C.byref(s), v, vv, out, quant, nthreads or default_threads())
+    del keep
+    return out
+
+
+def bwd2d_vec(g, vecs, sino, vol0=None, quant: int = 0,
+              nthreads: int | None = None) -> np.ndarray:
+    """Backprojection through per-view vectors (direct ray / detector-line
+    intersection per pixel and view)."""
+    s, keep, v = _vec_struct(g, vecs)
+    sg = np.ascontiguousarray(sino, dtype=np.float32)
+    out = (np.zeros((s.H, s.W), np.float64) if vol0 is None
+           else np.array(vol0, dtype=np.float64, copy=True))
+    lib().or_bwd2d_vec(C.byref(s), v, sg, out, quant, nthreads or default_threads())
+    del keep
+    return out
+
+
 def fwd3d(g, vol, sino0=None, quant: int = 0, nthreads: int | None = None) -> np.ndarray:
     """Sinogram (nangles, V, U) float64; rays that miss keep sino0 (default 0)."""
     s, keep = cone_struct(g)
@@ -212,11 +265,13 @@ class RefOps:
         L.ref_plan2d_create.restype = C.c_void_p
         L.ref_plan2d_create.argtypes = [C.c_uint64, u64p, f32p, f32p, C.c_uint64, C.c_float,
                                         C.c_float, f32p, f32p, f32p, C.c_uint64, C.c_float,
-                                        C.c_float]
+                                        C.c_float, C.c_uint32, C.c_uint32]
         L.ref_plan2d_destroy.argtypes = [C.c_void_p]
         L.ref_plan2d_tables.argtypes = [C.c_void_p, f32p, f32p, f32p]
         L.ref_forward2d.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.ref_backward2d.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ref_forward2d_t.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+        L.ref_backward2d_t.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int]
         args3 = [C.c_void_p, u64p, f32p, f32p, C.c_void_p, f32p, f32p, f32p, C.c_uint64, u64p,
                  f32p, f32p, f32p, C.c_float, C.c_float, C.c_float]
         L.ref_forward3d.argtypes = args3
@@ -229,7 +284,7 @@ class RefOps:
         a = np.ascontiguousarray(np.asarray(a, dtype=dt).ravel())
         return a, a.ctypes.data_as(C.POINTER(ct))
 
-    def plan2d(self, g):
+    def plan2d(self, g, vol_prec: int = 32, det_prec: int = 32):
         H, W = (int(v) for v in _get(g, "vol_shape"))
         keep = []
 
@@ -246,7 +301,7 @@ class RefOps:
             0, a([H, W], C.c_uint64, np.uint64), a(_opt(g, "vol_spacing", (1.0, 1.0))),
             a(_opt(g, "vol_offset", (0.0, 0.0))), int(_get(g, "det_shape")),
             float(_opt(g, "det_spacing", 1.0)), float(_opt(g, "det_offset", 0.0)), a(DSO), a(DSD),
-            a(angles), n, float(_opt(g, "det_rotation", 0.0)), 0.0)
+            a(angles), n, float(_opt(g, "det_rotation", 0.0)), 0.0, vol_prec, det_prec)
         return h, n
 
     def plan2d_tables(self, h, n):
@@ -259,6 +314,15 @@ class RefOps:
 
     def backward2d(self, h, vol_ptr, sino_ptr):
         self.L.ref_backward2d(h, vol_ptr, sino_ptr)
+
+    def forward2d_typed(self, h, vol, sino):
+        """Forward with the tensors' element types (float32 / float16)."""
+        bits = lambda t: 16 if t.element_size() == 2 else 32  # noqa: E731
+        self.L.ref_forward2d_t(h, vol.data_ptr(), sino.data_ptr(), bits(vol), bits(sino))
+
+    def backward2d_typed(self, h, vol, sino):
+        bits = lambda t: 16 if t.element_size() == 2 else 32  # noqa: E731
+        self.L.ref_backward2d_t(h, vol.data_ptr(), sino.data_ptr(), bits(vol), bits(sino))
 
     def destroy2d(self, h):
         self.L.ref_plan2d_destroy(h)

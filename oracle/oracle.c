@@ -227,6 +227,84 @@ int or_fwd2d(const or_fan2d_t *g, const float *vol, double *sino, int quant, int
     return 0;
 }
 
+/* ------------------------------------------------- 2D vector geometry */
+
+/* Per-view vectors [S.x, S.y, C.x, C.y, U.x, U.y] (source, detector centre,
+ * step between detector cell centres) in the circular plan's world frame,
+ * the layout of FanGeometry.to_vec (geometry.py:54-80).  Forward tables as
+ * plan_2d::precompute defines them: the source in voxel index units, the
+ * direction from it to the centre of cell 0, C - (det - 1)/2 U, and the
+ * per-cell step, both divided by the voxel spacing. */
+void or_fan2d_vec_tables(const or_fan2d_t *g, const double *vecs, double *src, double *u0,
+                         double *du) {
+    for (int64_t i = 0; i < g->nangles; ++i) {
+        const double *v = vecs + 6 * i;
+        const double d0x = v[2] - 0.5 * (double)(g->det_count - 1) * v[4];
+        const double d0y = v[3] - 0.5 * (double)(g->det_count - 1) * v[5];
+        src[2 * i] = (v[0] - g->ox) / g->sx + 0.5 * (double)g->W;
+        src[2 * i + 1] = (v[1] - g->oy) / g->sy + 0.5 * (double)g->H;
+        u0[2 * i] = (d0x - v[0]) / g->sx;
+        u0[2 * i + 1] = (d0y - v[1]) / g->sy;
+        du[2 * i] = v[4] / g->sx;
+        du[2 * i + 1] = v[5] / g->sy;
+    }
+}
+
+int or_fwd2d_vec(const or_fan2d_t *g, const double *vecs, const float *vol, double *sino,
+                 int quant, int nthreads) {
+    const int64_t n = g->nangles;
+    double *tab = (double *)malloc(sizeof(double) * 6 * (size_t)(n > 0 ? n : 1));
+    if (!tab) return -1;
+    or_fan2d_vec_tables(g, vecs, tab, tab + 2 * n, tab + 4 * n);
+    or_fwd2d_ctx c = {g, vol, sino, quant, tab, tab + 2 * n, tab + 4 * n};
+    or_parallel_for(n * g->det_count, nthreads, or_fwd2d_body, &c);
+    free(tab);
+    return 0;
+}
+
+typedef struct {
+    const or_fan2d_t *g;
+    const double *vecs;
+    const float *sino;
+    double *vol;
+    int quant;
+} or_bwd2d_vec_ctx;
+
+/* Pixel P (the backprojector's world position, unscaled +1/2 as in
+ * backward_2d.hpp:41-44): per view the ray S + s (P - S) meets the detector
+ * line C + t U where [P - S, -U] (s, t)^T = C - S (Cramer's rule); the sample
+ * of the view's row at t + det/2 is weighted by the magnification s, which is
+ * DSD / (x' + DSO) for a circular view; the sum times 1/|U| is added. */
+static void or_bwd2d_vec_body(void *ctx, int64_t b, int64_t e) {
+    or_bwd2d_vec_ctx *c = (or_bwd2d_vec_ctx *)ctx;
+    const or_fan2d_t *g = c->g;
+    const double inv = 1.0 / g->det_spacing;
+    const double half_det = (double)g->det_count / 2.0;
+    for (int64_t p = b; p < e; ++p) {
+        const int64_t ix = p % g->W, iy = p / g->W;
+        const double X = ((double)ix - (double)g->W / 2.0) * g->sx + g->ox + 0.5;
+        const double Y = ((double)iy - (double)g->H / 2.0) * g->sy + g->oy + 0.5;
+        double acc = 0.0;
+        for (int64_t v = 0; v < g->nangles; ++v) {
+            const double *q = c->vecs + 6 * v;
+            const double a11 = X - q[0], a21 = Y - q[1], a12 = -q[4], a22 = -q[5];
+            const double b1 = q[2] - q[0], b2 = q[3] - q[1];
+            const double det = a11 * a22 - a12 * a21;
+            const double s = (b1 * a22 - a12 * b2) / det;
+            const double t = (a11 * b2 - b1 * a21) / det;
+            acc += or_lerp1(c->sino + v * g->det_count, g->det_count, t + half_det, c->quant) * s;
+        }
+        c->vol[p] += acc * inv;
+    }
+}
+
+int or_bwd2d_vec(const or_fan2d_t *g, const double *vecs, const float *sino, double *vol,
+                 int quant, int nthreads) {
+    or_bwd2d_vec_ctx c = {g, vecs, sino, vol, quant};
+    or_parallel_for(g->W * g->H, nthreads, or_bwd2d_vec_body, &c);
+    return 0;
+}
+
 /* ------------------------------------------------------- 2D backprojection */
 
 typedef struct {

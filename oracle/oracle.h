@@ -51,6 +51,16 @@ void or_fan2d_tables(const or_fan2d_t *g, double *src, double *u0, double *du);
 int or_fwd2d(const or_fan2d_t *g, const float *vol, double *sino, int quant, int nthreads);
 int or_bwd2d(const or_fan2d_t *g, const float *sino, double *vol, int quant, int nthreads);
 
+/* Vector geometry: vecs is nangles x 6 [S.x, S.y, C.x, C.y, U.x, U.y]; the
+ * angles / DSO / DSD / det_offset fields of g are not used, det_spacing must
+ * be |U|. */
+void or_fan2d_vec_tables(const or_fan2d_t *g, const double *vecs, double *src, double *u0,
+                         double *du);
+int or_fwd2d_vec(const or_fan2d_t *g, const double *vecs, const float *vol, double *sino,
+                 int quant, int nthreads);
+int or_bwd2d_vec(const or_fan2d_t *g, const double *vecs, const float *sino, double *vol,
+                 int quant, int nthreads);
+
 void or_cone3d_fwd_tables(const or_cone3d_t *g, double *org, double *du, double *dv,
                           double *src);
 void or_cone3d_bwd_tables(const or_cone3d_t *g, double *org, double *dx, double *dy,

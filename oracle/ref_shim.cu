@@ -10,6 +10,7 @@
 //   ref_plan2d_create  <- plan.cu:34-56   (axis swap, thrust vectors)
 //   ref_forward2d      <- forward.cu:77-90 (spans {W,H}, {det, nangles})
 //   ref_backward2d     <- backward.cu:218-231
+//   ref_forward2d_t / ref_backward2d_t  <- the f16 instantiations of both
 //   ref_forward3d      <- forward.cu:23-75 (axis swaps, psi/phi naming swap)
 //   ref_backward3d     <- backward.cu:164-216
 #include <cstdint>
@@ -23,22 +24,42 @@
 #include "curadon/image.hpp"
 #include "curadon/measurement.hpp"
 
+// The typed instantiations of forward.cu:77-90 / backward.cu:75-87: T is the
+// volume's element type, U the sinogram's (float or __half).
+template <class T, class U>
+static void fwd2d_typed(curad::plan_2d &p, void *vol, void *sino) {
+    curad::device_span_2d<T> vol_span(p.device_id(), (T *)vol, p.vol_shape());
+    curad::device_span_2d<U> sino_span(p.device_id(), (U *)sino, {p.det_count(), p.nangles()});
+    curad::fp::forward_2d<T, U>(vol_span, sino_span, p);
+}
+
+template <class T, class U>
+static void bwd2d_typed(curad::plan_2d &p, void *vol, void *sino) {
+    curad::device_span_2d<T> vol_span(p.device_id(), (T *)vol, p.vol_shape());
+    curad::device_span_2d<U> sino_span(p.device_id(), (U *)sino, {p.det_count(), p.nangles()});
+    curad::bp::backproject_2d(vol_span, sino_span, p);
+}
+
 extern "C" {
+
+static curad::precision prec_of(uint32_t bits) {
+    return bits == 16 ? curad::precision::HALF : curad::precision::SINGLE;
+}
 
 void *ref_plan2d_create(uint64_t device, const uint64_t py_vol_shape[2],
                         const float py_vol_spacing[2], const float py_vol_offset[2],
                         uint64_t det_count, float det_spacing, float det_offset, const float *DSO,
                         const float *DSD, const float *angles, uint64_t n, float det_pitch,
-                        float COR) {
+                        float COR, uint32_t vol_prec, uint32_t det_prec) {
     thrust::device_vector<float> gpu_angles(angles, angles + n);
     thrust::device_vector<float> gpu_dso(DSO, DSO + n);
     thrust::device_vector<float> gpu_dsd(DSD, DSD + n);
     curad::vec2u vol_shape{py_vol_shape[1], py_vol_shape[0]};
     curad::vec2f vol_spacing{py_vol_spacing[1], py_vol_spacing[0]};
     curad::vec2f vol_offset{py_vol_offset[1], py_vol_offset[0]};
-    return new curad::plan_2d(device, curad::precision::SINGLE, vol_shape, vol_spacing, vol_offset,
-                              curad::precision::SINGLE, det_count, det_spacing, det_offset,
-                              gpu_dso, gpu_dsd, gpu_angles, det_pitch, COR);
+    return new curad::plan_2d(device, prec_of(vol_prec), vol_shape, vol_spacing, vol_offset,
+                              prec_of(det_prec), det_count, det_spacing, det_offset, gpu_dso,
+                              gpu_dsd, gpu_angles, det_pitch, COR);
 }
 
 void ref_plan2d_destroy(void *plan) { delete static_cast<curad::plan_2d *>(plan); }
@@ -63,6 +84,24 @@ void ref_backward2d(void *plan, float *vol, float *sino) {
     curad::device_span_2d<float> vol_span(p.device_id(), vol, p.vol_shape());
     curad::device_span_2d<float> sino_span(p.device_id(), sino, {p.det_count(), p.nangles()});
     curad::bp::backproject_2d(vol_span, sino_span, p);
+}
+
+void ref_forward2d_t(void *plan, void *vol, void *sino, int vol_bits, int sino_bits) {
+    auto &p = *static_cast<curad::plan_2d *>(plan);
+    using curad::f16;
+    if (vol_bits == 16)
+        sino_bits == 16 ? fwd2d_typed<f16, f16>(p, vol, sino) : fwd2d_typed<f16, float>(p, vol, sino);
+    else
+        sino_bits == 16 ? fwd2d_typed<float, f16>(p, vol, sino) : fwd2d_typed<float, float>(p, vol, sino);
+}
+
+void ref_backward2d_t(void *plan, void *vol, void *sino, int vol_bits, int sino_bits) {
+    auto &p = *static_cast<curad::plan_2d *>(plan);
+    using curad::f16;
+    if (vol_bits == 16)
+        sino_bits == 16 ? bwd2d_typed<f16, f16>(p, vol, sino) : bwd2d_typed<f16, float>(p, vol, sino);
+    else
+        sino_bits == 16 ? bwd2d_typed<float, f16>(p, vol, sino) : bwd2d_typed<float, float>(p, vol, sino);
 }
 
 static curad::device_measurement<float>

@@ -72,9 +72,14 @@ def test_invalid_precision_is_rejected(lib):
     assert b"Precision" in lib.cg_last_error()
 
 
-def test_f16_is_reported_unsupported(lib):
-    rc, _ = _create(lib, _plan_args(det_prec=16))
-    assert rc == _lib.CG_ERR_UNSUPPORTED
+def test_precisions(lib):
+    """16 and 32 pass argument validation (without a GPU the device check is
+    what fails), any other width is rejected (plan.cu:20-28)."""
+    for prec in (16, 32):
+        rc, _ = _create(lib, _plan_args(det_prec=prec))
+        assert rc != _lib.CG_ERR_INVALID or b"device" in lib.cg_last_error()
+    rc, _ = _create(lib, _plan_args(det_prec=8))
+    assert rc == _lib.CG_ERR_INVALID and b"f32 or f16" in lib.cg_last_error()
 
 
 def test_nonfinite_geometry_is_rejected(lib):
@@ -92,6 +97,8 @@ def test_zero_views_rejected(lib):
 def test_null_plan_calls_fail_cleanly(lib):
     assert lib.cg_forward_2d(None, None, None, None) == _lib.CG_ERR_INVALID
     assert lib.cg_backward_2d(None, None, None, None) == _lib.CG_ERR_INVALID
+    assert lib.cg_forward_2d_ex(None, None, None, 16, None) == _lib.CG_ERR_INVALID
+    assert lib.cg_backward_2d_ex(None, None, None, 16, None) == _lib.CG_ERR_INVALID
     assert lib.cg_forward_3d_plan(None, None, None, None) == _lib.CG_ERR_INVALID
     assert lib.cg_plan2d_destroy(None) == _lib.CG_OK
 

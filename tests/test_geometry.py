@@ -79,3 +79,20 @@ def test_str():
     assert "DSD" in geom_to_str(fan())
     assert "vol_shape" in str(ConeGeometry(DSD=3, DSO=2, angles=[0.0], vol_shape=(8, 8, 8),
                                            det_shape=(10, 12)))
+
+
+def test_vec_geometry_keeps_the_vectors():
+    from curadon_gb300 import FanVecGeometry
+
+    g = FanGeometry(DSD=300.0, DSO=[200.0] * 4, angles=[0.0, 0.5, 1.0, 2.0], vol_shape=(32, 32),
+                    det_shape=40, det_spacing=1.0)
+    vecs = np.asarray(g.to_vec())
+    vecs[:, 0] += 0.25  # a source shift the angle/DSO/DSD reduction cannot hold
+    vg = FanGeometry.from_vec((32, 32), 40, vecs, lossless=True)
+    assert isinstance(vg, FanVecGeometry) and isinstance(vg, FanGeometry)
+    assert np.array_equal(np.asarray(vg.to_vec()), vecs)
+    assert vg.sinogram_shape() == (4, 40) and vg.det_spacing == 1.0
+    lossy = FanGeometry.from_vec((32, 32), 40, vecs)
+    assert not isinstance(lossy, FanVecGeometry)
+    with pytest.raises(AttributeError):
+        FanVecGeometry((32, 32), 40, vecs[:, :5])

@@ -5,6 +5,7 @@ import pytest
 
 import oracle
 from conftest import load_golden, max_abs, rel_l2
+from curadon_gb300 import FanGeometry
 from curadon_gb300.phantom import ellipses_2d, fan_config
 
 
@@ -131,3 +132,18 @@ def test_oracle_matches_reference_cone(case):
     assert rel_l2(s[~missed], sref[~missed]) < 1e-3, rel_l2(s[~missed], sref[~missed])
     b = oracle.bwd3d(g, z["bwd_in"], vol0=np.ones(z["volume"].shape), quant=1)
     assert rel_l2(b, z["bwd_ref"]) < 1e-3, rel_l2(b, z["bwd_ref"])
+
+
+def test_vector_oracle_matches_circular():
+    """The vector-geometry oracle (direct ray / detector-line intersection)
+    reproduces the circular oracle for vectors of a circular geometry."""
+    g = fan_config(64, 90, 91, 1.5, 256, 384)
+    geom = FanGeometry(**g)
+    vecs = np.asarray(geom.to_vec())
+    vecs[:, 4:] *= g["det_spacing"]  # u as the cell step
+    ph = ellipses_2d(64, 3).numpy()
+    a, b = oracle.fwd2d(g, ph), oracle.fwd2d_vec(g, vecs, ph)
+    assert np.abs(a - b).max() < 1e-5 * np.abs(a).max()
+    s = a.astype(np.float32)
+    c, d = oracle.bwd2d(g, s), oracle.bwd2d_vec(g, vecs, s)
+    assert np.abs(c - d).max() < 1e-5 * np.abs(c).max()
