@@ -63,7 +63,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference", "reference-gpu"])
     p.add_argument("--workload", default="fan2048",
-                   help="fan<n> (n-sweep: n x n, n views) or cone256 / cone512")
+                   help="fan<n> (n-sweep: n x n, n views), cone256 / cone512, or serve "
+                        "(served reconstruction stream vs the plain loop)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="CPU work budget of the cpu_baseline sample")
@@ -521,12 +522,131 @@ def run_reference_gpu(args, rank, world, local_rank):
     }
 
 
+# ------------------------------------------------------------ serving
+
+def serve_requests(n_req: int, dev, seed: int = 4000):
+    """A seeded request mix in the proportions of the served stream: 70 %
+    2D FBP (n log-uniform over 128..2048, n views), 25 % 2D SIRT-20 (n
+    128..512), 5 % 3D CGLS-30 (n 64..128, 2n views); sizes drawn from a
+    log-spaced set so geometries repeat as in a clinic.  Sinograms are
+    projections of seeded phantoms, in pinned host memory."""
+    import torch
+
+    from curadon_gb300 import ConeGeometry, FanGeometry, forward
+    from curadon_gb300.phantom import cone_config, ellipses_2d, ellipsoids_3d, fan_config
+    from curadon_gb300.serve import Request
+
+    rng = np.random.default_rng(seed)
+    fbp_sizes = [128, 181, 256, 362, 512, 724, 1024, 1448, 2048]
+    sirt_sizes = [128, 181, 256, 362, 512]
+    cone_sizes = [64, 96, 128]
+    geoms, reqs = {}, []
+    for _ in range(n_req):
+        u = rng.random()
+        if u < 0.70:
+            kind, n = "fbp", int(rng.choice(fbp_sizes))
+        elif u < 0.95:
+            kind, n = "sirt", int(rng.choice(sirt_sizes))
+        else:
+            kind, n = "cgls", int(rng.choice(cone_sizes))
+        key = (kind == "cgls", n)
+        if key not in geoms:
+            if kind == "cgls":
+                geoms[key] = ConeGeometry(**cone_config(n, 2 * n, int(1.5 * n)))
+            else:
+                geoms[key] = FanGeometry(**fan_config(n))
+        g = geoms[key]
+        ph = (ellipsoids_3d(n, int(rng.integers(1 << 30)), device=dev) if kind == "cgls"
+              else ellipses_2d(n, int(rng.integers(1 << 30)), device=dev)).contiguous()
+        y = torch.zeros(g.sinogram_shape(), device=dev)
+        forward(ph, y, g)
+        iters = {"fbp": 0, "sirt": 20, "cgls": 30}[kind]
+        reqs.append(Request(kind, g, y.cpu().pin_memory(), iters=iters))
+    torch.cuda.synchronize()
+    return reqs
+
+
+def run_serve(args):
+    """Served solves/s with Poisson arrivals against the plain loop (one
+    problem at a time, each solved and read back before the next)."""
+    import threading
+
+    import torch
+
+    from curadon_gb300 import _build
+    from curadon_gb300.fbp import fbp
+    from curadon_gb300.serve import Server
+    from curadon_gb300.solvers import cgls, sirt
+
+    _build.build()
+    dev = torch.device("cuda", 0)
+    n_req = max(20, args.steps * 8)
+    reqs = serve_requests(n_req, dev)
+
+    def plain(r):
+        y = r.sinogram.to(dev)
+        x = (fbp(y, r.geom) if r.kind == "fbp" else
+             sirt(r.geom, y, r.iters) if r.kind == "sirt" else cgls(r.geom, y, r.iters))
+        return x.cpu()
+
+    for r in reqs[:min(len(reqs), 30)]:  # warm-up: plans and filters of the plain path
+        plain(r)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r in reqs:
+        plain(r)
+    t_plain = time.perf_counter() - t0
+
+    srv = Server(device=0, slots=8)
+    for f in [srv.submit(r) for r in reqs[:min(len(reqs), 30)]]:  # warm-up: slot residency
+        f.result()
+    srv.latencies.clear()
+    srv.completed, srv.t_first, srv.t_last = 0, None, None
+    rate = 200.0
+    rng = np.random.default_rng(7)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+    futs = []
+
+    def client():
+        t_start = time.perf_counter()
+        for r, ta in zip(reqs, arrivals):
+            delay = t_start + ta - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            futs.append(srv.submit(r))
+
+    th = threading.Thread(target=client)
+    th.start()
+    th.join()
+    for f in futs:
+        f.result()
+    srv.close()
+    st = srv.stats()
+    plain_rate = len(reqs) / t_plain
+    kinds = {k: sum(r.kind == k for r in reqs) for k in ("fbp", "sirt", "cgls")}
+    return {
+        "metric": "served solves/s", "value": st["solves_per_s"], "unit": "solves/s",
+        "n_gpus": 1, "steps": len(reqs), "warmup": 30, "ms_per_step": 1e3 / st["solves_per_s"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded phantoms, projected by the forward operator)",
+        "config": {"workload": f"served stream of {len(reqs)} requests, Poisson arrivals at "
+                               f"{rate:.0f}/s: {kinds['fbp']} 2D FBP (n 128..2048), "
+                               f"{kinds['sirt']} 2D SIRT-20 (n 128..512), {kinds['cgls']} 3D "
+                               "CGLS-30 (n 64..128, 2n views), 8 slots",
+                   "parallelism": "one GPU, concurrent streams"},
+        "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+        "plain_loop_solves_per_s": plain_rate, "speedup_vs_plain_loop": st["solves_per_s"] / plain_rate,
+    }
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
+    if args.workload == "serve":
+        line = run_serve(args) if rank == 0 else None
+    elif args.impl == "reference":
         line = run_reference_cpu(args, rank, world)
     elif args.impl == "reference-gpu":
         line = run_reference_gpu(args, rank, world, local_rank)

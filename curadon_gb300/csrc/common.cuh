@@ -163,6 +163,11 @@ void free_plan3d(Plan3d *p);
 int launch_plan2d_tables(Plan2d &p, cudaStream_t s);
 int launch_relayout2d(const Plan2d &p, const float *vol, cudaStream_t s);
 int launch_forward2d(const Plan2d &p, float *sino, cudaStream_t s);
+// Raises a kernel's dynamic shared-memory limit to `bytes` on the current
+// device, once per (device, kernel): later calls, e.g. inside a CUDA-graph
+// capture, make no runtime call.
+int ensure_smem_attr(const void *func, int bytes);
+
 // FP16 storage (half.cu)
 int ensure_half_scratch(Plan2d &p, bool vol, bool sino);
 int widen_half(const void *in, float *out, long long n, cudaStream_t s);

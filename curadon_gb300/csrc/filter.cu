@@ -77,8 +77,7 @@ template <int RB>
 int launch_rb(const float *in, float *out, const float *h, const float *pre, int nrows, int N,
               float scale, cudaStream_t s) {
     const size_t smem = sizeof(float) * (size_t)N * (RB + 1);
-    CG_TRY_CUDA(cudaFuncSetAttribute(k_filter_rows<RB>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (int rc = ensure_smem_attr((const void *)k_filter_rows<RB>, (int)smem)) return rc;
     dim3 grid(ceil_div(N, kFiltThreads * kFiltOut), ceil_div(nrows, RB));
     k_filter_rows<RB><<<grid, kFiltThreads, smem, s>>>(in, out, h, pre, nrows, N, scale);
     CG_TRY_CUDA(cudaGetLastError());

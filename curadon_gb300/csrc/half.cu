@@ -1,4 +1,4 @@
-// FP16 storage for the 2D operators (the reference's f16 paths,
+// Small runtime helpers and FP16 storage for the 2D operators (the reference's f16 paths,
 // python/standalone/src/forward.cu:107-135 and backward.cu:104-135).
 //
 // Values are stored as IEEE half and computed in FP32: a half volume or
@@ -9,6 +9,9 @@
 // backprojection as half(acc / ds) added in half arithmetic, as the
 // reference's `volume[i] += accum * inv_u_spacing` does for T = __half.
 #include <cuda_fp16.h>
+
+#include <map>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -39,6 +42,20 @@ __global__ void k_add_to_half(__half *__restrict__ vol, const float *__restrict_
 dim3 grid_for(long long n) { return dim3((unsigned)std::min<long long>(ceil_div(n, 256), 152 * 16)); }
 
 }  // namespace
+
+int ensure_smem_attr(const void *func, int bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, int> done;
+    int dev = 0;
+    CG_TRY_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    int &have = done[{dev, func}];
+    if (have < bytes) {
+        CG_TRY_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        have = bytes;
+    }
+    return CG_OK;
+}
 
 int ensure_half_scratch(Plan2d &p, bool vol, bool sino) {
     if (vol && !p.d_vol32)

@@ -386,8 +386,7 @@ template <int RPV, int G>
 int launch_slab(const Plan2d &p, float *sino, cudaStream_t s) {
     const int pitch = max(p.pitchA(), p.pitchB());
     const size_t smem = sizeof(float2) * (size_t)kSlabRing * pitch;
-    CG_TRY_CUDA(cudaFuncSetAttribute(k_fwd2d_slab<RPV, G>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (int rc = ensure_smem_attr((const void *)k_fwd2d_slab<RPV, G>, (int)smem)) return rc;
     dim3 grid(ceil_div(p.nangles, G), 2);
     k_fwd2d_slab<RPV, G><<<grid, kSlabThreads, smem, s>>>(
         p.d_layA, p.d_layB, sino, p.d_src, p.d_u0, p.d_du, p.W, p.H, p.det, p.nangles, p.sx,
@@ -656,8 +655,7 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
         return set_error(CG_ERR_INVALID, "volume too wide for the chunked forward");
     auto go = [&](auto kernel, int k, int stride, int threads) -> int {
         const size_t smem = 2 * sizeof(float2) * (k + 1) * stride;
-        CG_TRY_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem));
+        if (int rc = ensure_smem_attr((const void *)kernel, (int)smem)) return rc;
         dim3 grid(ceil_div(p.det, threads), groups, 2);
         kernel<<<grid, threads, smem, s>>>(p.d_layA, p.d_layB, sino, p.d_src, p.d_u0, p.d_du,
                                            p.W, p.H, p.det, p.nangles, p.sx, p.sy, p.pitchA(),

@@ -586,8 +586,7 @@ int launch_forward3d_slab(Plan3d &p, const float *vol, float *sino, cudaStream_t
     const long long groups = ceil_div(p.nangles, kS3G);
     if (2 * groups > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     dim3 grid(ceil_div(p.U, kS3BU), ceil_div(p.V, kS3BV), (unsigned)(2 * groups));
-    CG_TRY_CUDA(cudaFuncSetAttribute(k_fwd3d_slab, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
+    if (int rc = ensure_smem_attr((const void *)k_fwd3d_slab, (int)smem)) return rc;
     k_fwd3d_slab<<<grid, kS3Threads, smem, s>>>(p.d_volA, p.d_volB, sino, p.d_forg, p.d_fdu,
                                                 p.d_fdv, p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V,
                                                 p.nangles);

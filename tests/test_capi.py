@@ -100,6 +100,10 @@ def test_null_plan_calls_fail_cleanly(lib):
     assert lib.cg_forward_2d_ex(None, None, None, 16, None) == _lib.CG_ERR_INVALID
     assert lib.cg_backward_2d_ex(None, None, None, 16, None) == _lib.CG_ERR_INVALID
     assert lib.cg_forward_3d_plan(None, None, None, None) == _lib.CG_ERR_INVALID
+    h = C.c_void_p()
+    assert lib.cg_batch2d_create(C.byref(h), None, None, None, 1) == _lib.CG_ERR_INVALID
+    assert lib.cg_batch2d_forward(None, None) == _lib.CG_ERR_INVALID
+    assert lib.cg_batch2d_destroy(None) == _lib.CG_OK
     assert lib.cg_plan2d_destroy(None) == _lib.CG_OK
 
 

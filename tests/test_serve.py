@@ -1,0 +1,112 @@
+"""Serving with continuous admission (``curadon_gb300.serve``) and the
+fixed-iteration solvers it runs.
+
+Each result must be the same alone and in the mix: FBP and SIRT bit for bit
+(deterministic kernels, private per-slot scratch), CGLS within relative L2
+1e-3 (its matched adjoint accumulates with atomics).  The solvers must
+reduce the residual, and CUDA-graph replay must equal direct iterations."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+from curadon_gb300 import ConeGeometry, FanGeometry, forward
+from curadon_gb300.phantom import cone_config, ellipses_2d, ellipsoids_3d, fan_config
+from curadon_gb300.serve import Request, Server, solve_alone
+from curadon_gb300.solvers import CglsSolver, SirtSolver
+
+pytestmark = pytest.mark.gpu
+
+
+def fan_request(kind, n, nangles, seed, dev, iters=10):
+    g = FanGeometry(**fan_config(n, nangles), device=dev.index or 0)
+    x = ellipses_2d(n, seed, device=dev).contiguous()
+    y = torch.zeros(g.sinogram_shape(), device=dev)
+    forward(x, y, g)
+    torch.cuda.synchronize()
+    return Request(kind, g, y.cpu().pin_memory(), iters=iters)
+
+
+def cone_request(n, nangles, det, seed, dev, iters=8):
+    g = ConeGeometry(**cone_config(n, nangles, det), device=dev.index or 0)
+    x = ellipsoids_3d(n, seed, device=dev).contiguous()
+    y = torch.zeros(g.sinogram_shape(), device=dev)
+    forward(x, y, g)
+    torch.cuda.synchronize()
+    return Request("cgls", g, y.cpu().pin_memory(), iters=iters)
+
+
+def test_solvers_reduce_the_residual(cuda_device):
+    req = fan_request("sirt", 96, 120, 1, cuda_device)
+    g, y = req.geom, req.sinogram.to(cuda_device)
+    for solver in (SirtSolver(g, cuda_device), CglsSolver(g, cuda_device)):
+        x1 = solver.run(y, 1).clone()
+        x10 = solver.run(y, 10).clone()
+        r = []
+        for x in (x1, x10):
+            s = torch.zeros_like(y)
+            forward(x, s, g)
+            r.append(float(torch.linalg.norm(s - y)))
+        assert r[1] < 0.7 * r[0], r
+
+
+@pytest.mark.parametrize("kind", ["sirt", "cgls"])
+def test_graph_replay_equals_direct(cuda_device, kind):
+    req = fan_request(kind, 128, 90, 2, cuda_device)
+    g, y = req.geom, req.sinogram.to(cuda_device)
+    cls = SirtSolver if kind == "sirt" else CglsSolver
+    a = cls(g, cuda_device, graph=False).run(y, 6).clone()
+    b = cls(g, cuda_device, graph=True).run(y, 6).clone()
+    torch.cuda.synchronize()
+    e = rel_l2(a.cpu(), b.cpu())
+    print(f"{kind}: graph vs direct rel-L2 {e:.2e}")
+    # SIRT is deterministic; CGLS's matched adjoint accumulates with atomics
+    # (order-dependent rounding) and its recurrences amplify that, so any two
+    # CGLS runs agree to the parity bar, not bit for bit
+    assert e == 0.0 if kind == "sirt" else e < 1e-3
+
+
+def test_results_same_alone_and_in_the_mix(cuda_device):
+    reqs = [fan_request("fbp", 256, 256, 3, cuda_device),
+            fan_request("sirt", 128, 180, 4, cuda_device, iters=5),
+            fan_request("fbp", 384, 200, 5, cuda_device),
+            cone_request(48, 40, 72, 6, cuda_device, iters=4),
+            fan_request("fbp", 128, 90, 7, cuda_device),
+            fan_request("sirt", 192, 120, 8, cuda_device, iters=5)]
+    alone = [solve_alone(r, cuda_device.index or 0).cpu() for r in reqs]
+    srv = Server(device=cuda_device.index or 0, slots=3)
+    futs = [srv.submit(r) for r in reqs + reqs]  # every geometry twice, interleaved
+    outs = [f.result(timeout=120) for f in futs]
+    srv.close()
+    st = srv.stats()
+    print(st)
+    assert st["completed"] == len(futs)
+    for i, out in enumerate(outs):
+        ref = alone[i % len(reqs)]
+        if reqs[i % len(reqs)].kind == "cgls":
+            assert rel_l2(out, ref) < 1e-3
+        else:
+            assert torch.equal(out, ref), i
+
+
+def test_admission_respects_the_memory_budget(cuda_device):
+    """A budget below two requests' needs runs them one at a time."""
+    from curadon_gb300.serve import request_bytes
+
+    reqs = [fan_request("fbp", 256, 128, 9 + k, cuda_device) for k in range(4)]
+    budget = 1.5 * request_bytes(reqs[0])
+    srv = Server(device=cuda_device.index or 0, slots=4, hbm_budget=budget)
+    peak = []
+    orig = srv._admit
+
+    def spy():
+        r = orig()
+        peak.append(len(srv._inflight))
+        return r
+
+    srv._admit = spy
+    futs = [srv.submit(r) for r in reqs]
+    for f in futs:
+        f.result(timeout=60)
+    srv.close()
+    assert max(peak) == 1
