@@ -212,7 +212,7 @@ def kernels_per_step(wl, geom) -> int:
     """Kernels of this library launched by one forward + one backprojection
     with the plan's algorithms (texture-unit paths copy the input into a
     CUDA array with a memcpy, which is not a kernel)."""
-    fwd, bwd = geom.plan.algorithm()
+    fwd, bwd = geom.plan.algorithm
     if wl["kind"] == "fan":
         nv = len(wl["geom"]["angles"])
         f = 1 if fwd == "texture" else 2
@@ -338,7 +338,7 @@ def run_ours(args, rank, world, local_rank):
     b_alg = {"forward": 4 * (nvox + nrays), "backward": 4 * (nrays + 2 * nvox)}
     dom = "forward" if ms_fwd >= ms_bwd else "backward"
     t_dom = (ms_fwd if dom == "forward" else ms_bwd) / 1e3
-    algos = dict(zip(("forward", "backward"), geom.plan.algorithm()))
+    algos = dict(zip(("forward", "backward"), geom.plan.algorithm))
     kernel = KERNELS.get((wl["kind"], dom, algos[dom]), dom)
     peaks = {}
     try:

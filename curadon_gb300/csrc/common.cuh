@@ -105,6 +105,7 @@ struct Plan2d {
     int algo_fwd = 1, algo_bwd = 2;
     int tex_eighths = 4;              // hybrid forward: share of warps on the texture unit
     int fwd_chunk_rows = 308;         // chunked forward: chunk shape
+    int bwd_min_blocks = 4;           // staged backprojector: register bound (blocks / SM)
 
     // row pitches of layA / layB in pairs, even so every row starts on 16 bytes
     int pitchA() const { return (W + 2 * kPad + 1) & ~1; }

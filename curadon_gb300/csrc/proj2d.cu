@@ -861,7 +861,9 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
     }
 }
 
-__global__ void __launch_bounds__(256)
+// MINB: resident blocks per SM the register allocation must allow
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB)
     k_bwd2d_smem(float *__restrict__ vol, const float2 *__restrict__ S,
                  const float4 *__restrict__ proj, int W, int H, int det, int nangles, float sx,
                  float sy, float ox, float oy, float ds) {
@@ -992,8 +994,15 @@ int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s) {
 
 int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s) {
     dim3 grid(ceil_div(p.W, 32), ceil_div(p.H, 8 * kSmRows));
-    k_bwd2d_smem<<<grid, dim3(32, 8), 0, s>>>(vol, p.d_sinoP, p.d_bproj, p.W, p.H, p.det,
-                                              p.nangles, p.sx, p.sy, p.ox, p.oy, p.ds);
+    auto go = [&](auto kernel) {
+        kernel<<<grid, dim3(32, 8), 0, s>>>(vol, p.d_sinoP, p.d_bproj, p.W, p.H, p.det,
+                                            p.nangles, p.sx, p.sy, p.ox, p.oy, p.ds);
+    };
+    switch (p.bwd_min_blocks) {
+        case 3: go(k_bwd2d_smem<3>); break;
+        case 5: go(k_bwd2d_smem<5>); break;
+        default: go(k_bwd2d_smem<4>); break;
+    }
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }

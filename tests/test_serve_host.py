@@ -1,0 +1,30 @@
+"""Host-side logic of serving (no GPU): geometry keys for resident plans and
+the memory estimate admission uses."""
+import numpy as np
+import torch
+
+from curadon_gb300 import ConeGeometry, FanGeometry, FanVecGeometry
+from curadon_gb300.phantom import cone_config, fan_config
+from curadon_gb300.serve import Request, _geom_key, request_bytes
+
+
+def test_geometry_keys():
+    a = FanGeometry(**fan_config(128, 90))
+    b = FanGeometry(**fan_config(128, 90))
+    c = FanGeometry(**fan_config(128, 91))
+    assert _geom_key(a) == _geom_key(b) != _geom_key(c)
+    v = np.asarray(a.to_vec())
+    assert _geom_key(FanVecGeometry((128, 128), a.det_shape, v)) != _geom_key(a)
+    assert _geom_key(ConeGeometry(**cone_config(32, 20, 48))) != _geom_key(a)
+
+
+def test_memory_estimate_grows_with_the_problem():
+    def req(kind, n):
+        g = FanGeometry(**fan_config(n, n))
+        return Request(kind, g, torch.zeros(g.sinogram_shape()))
+
+    small, large = request_bytes(req("fbp", 128)), request_bytes(req("fbp", 1024))
+    assert 0 < small < large
+    # the volume and sinogram alone are a lower bound
+    assert large >= 4 * (1024 * 1024 + 1024 * 1449)
+    assert request_bytes(req("sirt", 256)) > request_bytes(req("fbp", 256))
