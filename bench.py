@@ -40,8 +40,9 @@ import numpy as np  # noqa: E402
 # the ncu captures summarised in profiles/, by workload and kernel; None
 # where not captured.
 NCU_TRAFFIC = {
-    ("fan2048", "k_fwd2d_tex"): 17_007_744,    # profiles/dram_fan2048.md
-    ("fan2048", "k_bwd2d_smem"): 62_407_168,
+    ("fan2048", "k_fwd2d_cslab"): 80_510_592,  # profiles/dram_fan2048.md
+    ("fan2048", "k_bwd2d_smem"): 62_522_240,
+    ("fan2048", "k_fwd2d_tex"): 17_007_744,    # the texture-unit forward (algorithm 1)
 }
 
 # Main kernel of each operator by the plan's algorithm name.

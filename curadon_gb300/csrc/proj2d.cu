@@ -757,6 +757,7 @@ constexpr int kSmWin = 128;   // pairs of one view's row staged for a tile
 // with the per-view terms of each thread's column hoisted, then one
 // reciprocal, one 8-byte shared load and two FMAs.  The same table describes
 // an arbitrary per-view source / detector placement (vector geometry).
+template <bool PK>
 __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                                                 const float2 *__restrict__ S,
                                                 const float4 *__restrict__ proj, int W, int H,
@@ -823,17 +824,41 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
             const float A = fmaf(a.x, X, a.z), B = fmaf(b.x, X, b.z);
             if (k0 != INT_MIN) {
                 const float2 *sr = srow[j];
+                if constexpr (PK) {
+                    // two rows per packed FP32 instruction (the same IEEE
+                    // operations per row as the scalar loop below)
+                    const float2 ay = make_float2(a.y, a.y), by = make_float2(b.y, b.y);
+                    const float2 A2 = make_float2(A, A), B2 = make_float2(B, B);
+                    const float2 e2 = make_float2(edm, edm);
 #pragma unroll
-                for (int r = 0; r < kSmRows; ++r) {
-                    const float den = fmaf(a.y, Y[r], A);
-                    const float yi = fmaf(b.y, Y[r], B);
-                    const float w = __fdividef(1.0f, den);
-                    const float ub = fmaf(w, yi, edm);
-                    const float kf = floorf(ub);
-                    const float f = ub - kf;
-                    const unsigned li = min((unsigned)((int)kf - k0), (unsigned)(kSmWin - 1));
-                    const float2 t = sr[li];
-                    acc[r] = fmaf(fmaf(f, t.y, t.x), w, acc[r]);
+                    for (int r = 0; r < kSmRows; r += 2) {
+                        const float2 Yr = make_float2(Y[r], Y[r + 1]);
+                        const float2 den = __ffma2_rn(ay, Yr, A2);
+                        const float2 yi = __ffma2_rn(by, Yr, B2);
+                        const float2 w = make_float2(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y));
+                        const float2 ub = __ffma2_rn(w, yi, e2);
+                        const float2 kf = make_float2(floorf(ub.x), floorf(ub.y));
+                        const float2 f = __fadd2_rn(ub, make_float2(-kf.x, -kf.y));
+                        const unsigned l0 = min((unsigned)((int)kf.x - k0), (unsigned)(kSmWin - 1));
+                        const unsigned l1 = min((unsigned)((int)kf.y - k0), (unsigned)(kSmWin - 1));
+                        const float2 t0 = sr[l0], t1 = sr[l1];
+                        const float2 v = make_float2(fmaf(f.x, t0.y, t0.x), fmaf(f.y, t1.y, t1.x));
+                        const float2 acc2 = __ffma2_rn(v, w, make_float2(acc[r], acc[r + 1]));
+                        acc[r] = acc2.x, acc[r + 1] = acc2.y;
+                    }
+                } else {
+#pragma unroll
+                    for (int r = 0; r < kSmRows; ++r) {
+                        const float den = fmaf(a.y, Y[r], A);
+                        const float yi = fmaf(b.y, Y[r], B);
+                        const float w = __fdividef(1.0f, den);
+                        const float ub = fmaf(w, yi, edm);
+                        const float kf = floorf(ub);
+                        const float f = ub - kf;
+                        const unsigned li = min((unsigned)((int)kf - k0), (unsigned)(kSmWin - 1));
+                        const float2 t = sr[li];
+                        acc[r] = fmaf(fmaf(f, t.y, t.x), w, acc[r]);
+                    }
                 }
             } else {
                 const float2 *row = S + (size_t)(v0 + j) * pitch;
@@ -862,12 +887,13 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
 }
 
 // MINB: resident blocks per SM the register allocation must allow
-template <int MINB>
+template <int MINB, bool PK>
 __global__ void __launch_bounds__(256, MINB)
     k_bwd2d_smem(float *__restrict__ vol, const float2 *__restrict__ S,
                  const float4 *__restrict__ proj, int W, int H, int det, int nangles, float sx,
                  float sy, float ox, float oy, float ds) {
-    bwd2d_smem_tile(vol, S, proj, W, H, det, nangles, sx, sy, ox, oy, ds, blockIdx.x, blockIdx.y);
+    bwd2d_smem_tile<PK>(vol, S, proj, W, H, det, nangles, sx, sy, ox, oy, ds, blockIdx.x,
+                        blockIdx.y);
 }
 
 }  // namespace
@@ -924,8 +950,8 @@ __global__ void __launch_bounds__(256)
     const Prob2d &q = probs[i];
     const int local = blockIdx.x - start[i];
     const int gx = (q.W + 31) / 32;
-    bwd2d_smem_tile(q.vol, q.sinoP, q.bproj, q.W, q.H, q.det, q.nangles, q.sx, q.sy, q.ox, q.oy,
-                    q.ds, local % gx, local / gx);
+    bwd2d_smem_tile<false>(q.vol, q.sinoP, q.bproj, q.W, q.H, q.det, q.nangles, q.sx, q.sy, q.ox,
+                           q.oy, q.ds, local % gx, local / gx);
 }
 
 }  // namespace
@@ -999,9 +1025,11 @@ int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s) {
                                             p.nangles, p.sx, p.sy, p.ox, p.oy, p.ds);
     };
     switch (p.bwd_min_blocks) {
-        case 3: go(k_bwd2d_smem<3>); break;
-        case 5: go(k_bwd2d_smem<5>); break;
-        default: go(k_bwd2d_smem<4>); break;
+        case 3: go(k_bwd2d_smem<3, false>); break;
+        case 5: go(k_bwd2d_smem<5, false>); break;
+        case 14: go(k_bwd2d_smem<4, true>); break;
+        case 15: go(k_bwd2d_smem<5, true>); break;
+        default: go(k_bwd2d_smem<4, false>); break;
     }
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
