@@ -78,7 +78,7 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
         if (has("bwd2d=alu")) p2->algo_bwd = 0;
         if (has("bwd2d=tex")) p2->algo_bwd = 1;
         if (has("bwd2d=smem")) p2->algo_bwd = 2;
-        for (int k : {3, 4, 5, 14, 15})
+        for (int k : {3, 4, 5, 14, 24})
             if (has(("bwd2d_minb=" + std::to_string(k)).c_str())) p2->bwd_min_blocks = k;
     }
     if (p3) {

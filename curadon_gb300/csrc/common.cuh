@@ -105,7 +105,10 @@ struct Plan2d {
     int algo_fwd = 1, algo_bwd = 2;
     int tex_eighths = 4;              // hybrid forward: share of warps on the texture unit
     int fwd_chunk_rows = 308;         // chunked forward: chunk shape
-    int bwd_min_blocks = 4;           // staged backprojector: register bound (blocks / SM)
+    // staged backprojector variant: 24 = 4 blocks/SM, packed FP32 pairs of
+    // rows, floor taken by FP32 adds (default, measured fastest); 14 = the
+    // same with the conversion unit's floor; 3, 4, 5 = scalar at 3..5 blocks/SM
+    int bwd_min_blocks = 24;
 
     // row pitches of layA / layB in pairs, even so every row starts on 16 bytes
     int pitchA() const { return (W + 2 * kPad + 1) & ~1; }
@@ -212,6 +215,25 @@ int launch_filter_rows(const float *in, float *out, const float *h, const float 
                        int N, float scale, cudaStream_t s);
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// floor(x) with two FP32 adds instead of the conversion unit (which runs
+// floor and float<->int conversions at a fraction of the FMA rate):
+// x - 1/2 + 1.5 * 2^23 rounds to the nearest integer, which is floor(x); at
+// an exact integer it may be x - 1 with fraction 1, which gives the same
+// linear interpolation of a difference-encoded pair (v, next - v).  frac =
+// x - floor(x); idx = floor(x) - base as an unsigned offset for the caller to
+// clamp: for |x| >= 2^22, infinities and NaN it lands far outside any buffer
+// and the clamp sends it to the zero padding.
+struct FloorSplit {
+    float frac;
+    unsigned idx;
+};
+__device__ __forceinline__ FloorSplit floor_split(float x, int base) {
+    constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+    const float t = __fadd_rn(__fadd_rn(x, -0.5f), kMagic);
+    const float k = __fadd_rn(t, -kMagic);
+    return {__fadd_rn(x, -k), __float_as_uint(t) - (0x4B400000u + (unsigned)base)};
+}
 
 }  // namespace cg
 

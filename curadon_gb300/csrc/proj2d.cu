@@ -423,24 +423,6 @@ namespace {
 constexpr int kCs2G = 4;             // views per bundle
 constexpr int kCs2MaxChunks = 1024;  // chunk windows kept in shared memory
 
-// Bundle = kCs2G views x T adjacent detector cells x ray class (blockIdx.z:
-// 0 = y-stepping rays on layA, 1 = x-stepping rays on layB); thread t owns
-// cell u0 + t of every view.  The block walks its layout's rows in chunks of
-// K.  A chunk's window -- the pair columns the bundle's rays can touch on its
-// rows -- is bounded by lines through each view's source: a ray's column is
-// linear in the row with slope b = dp/dq, and the rays of this class have
-// |b| <= 1.  Over a detector interval on which dq keeps its sign b is
-// monotone, so the slopes at the bundle's end cells clamped to [-1, 1] bound
-// every ray of the class; where dq changes sign the bound is b = -1 .. 1.
-// All windows are computed up front.  Windows are
-// staged for rows r0 .. r0 + K (row stride S pairs) with 16-byte cp.async
-// into two alternating buffers, the next chunk's copy running while the
-// current chunk is sampled, one barrier per chunk.  Every ray then takes its
-// samples of the chunk from shared memory: two 8-byte loads at fixed row
-// offsets and two FMAs each.  Samples and their order per ray are those of the
-// register forward (the reference's positions; rays stepping towards smaller
-// rows are summed in reverse), so the matched adjoint is this forward's
-// exact transpose too.  A chunk whose window does not fit reads global memory.
 // Row-sum accumulation of one sample's two pairs.  Scalar: alo += lo.x +
 // fp lo.y (same operations as the register forward).  Packed: the terms are
 // kept apart, (sum lo.x, sum fp lo.y), one packed FP32 FMA per row.
@@ -462,6 +444,26 @@ struct RowAcc {
     __device__ __forceinline__ float sum_hi() const { return PK ? hi.x + hi.y : hi.x; }
 };
 
+// Bundle = kCs2G views x T adjacent detector cells x ray class (blockIdx.z:
+// 0 = y-stepping rays on layA, 1 = x-stepping rays on layB); thread t owns
+// cell u0 + t of every view.  The block walks its layout's rows in chunks of
+// K.  A chunk's window -- the pair columns the bundle's rays can touch on its
+// rows -- is bounded by lines through each view's source: a ray's column is
+// linear in the row with slope b = dp/dq, and the rays of this class have
+// |b| <= 1.  Over a detector interval on which dq keeps its sign b is
+// monotone, so the slopes at the bundle's end cells clamped to [-1, 1] bound
+// every ray of the class; where dq changes sign the bound is b = -1 .. 1.
+// All windows are computed up front.  Windows are staged for rows r0 .. r0 +
+// K (row stride S pairs) with 16-byte cp.async into two alternating buffers,
+// the next chunk's copy running while the current chunk is sampled, one
+// barrier per chunk.  Every ray then takes its samples of the chunk from
+// shared memory: two 8-byte loads at fixed row offsets and two FMAs each
+// (bound by the shared-memory data path, so the conversion unit's floor
+// costs nothing here: the FP32-add floor measured slower).  Samples and
+// weights are those of the register forward (the reference's positions; rays
+// stepping towards smaller rows are summed in reverse), so the matched
+// adjoint is this forward's transpose up to the order of summation.  A chunk
+// whose window does not fit reads global memory.
 template <int K, int S, int T, bool PK>
 __global__ void __launch_bounds__(T)
     k_fwd2d_cslab(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
@@ -757,7 +759,7 @@ constexpr int kSmWin = 128;   // pairs of one view's row staged for a tile
 // with the per-view terms of each thread's column hoisted, then one
 // reciprocal, one 8-byte shared load and two FMAs.  The same table describes
 // an arbitrary per-view source / detector placement (vector geometry).
-template <bool PK>
+template <bool PK, bool MAGIC = false>
 __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                                                 const float2 *__restrict__ S,
                                                 const float4 *__restrict__ proj, int W, int H,
@@ -837,10 +839,26 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                         const float2 yi = __ffma2_rn(by, Yr, B2);
                         const float2 w = make_float2(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y));
                         const float2 ub = __ffma2_rn(w, yi, e2);
-                        const float2 kf = make_float2(floorf(ub.x), floorf(ub.y));
-                        const float2 f = __fadd2_rn(ub, make_float2(-kf.x, -kf.y));
-                        const unsigned l0 = min((unsigned)((int)kf.x - k0), (unsigned)(kSmWin - 1));
-                        const unsigned l1 = min((unsigned)((int)kf.y - k0), (unsigned)(kSmWin - 1));
+                        float2 f;
+                        unsigned l0, l1;
+                        if constexpr (MAGIC) {
+                            // floor without the conversion unit: ub - 1/2 + 1.5 * 2^23
+                            // rounds to the nearest integer, i.e. floor(ub) (at an exact
+                            // integer possibly one less, with fraction 1: the same lerp);
+                            // |ub| >= 2^22 lands outside the window and is clamped
+                            const float2 t = __fadd2_rn(__fadd2_rn(ub, make_float2(-0.5f, -0.5f)),
+                                                        make_float2(12582912.0f, 12582912.0f));
+                            const float2 kf = __fadd2_rn(t, make_float2(-12582912.0f, -12582912.0f));
+                            f = __fadd2_rn(ub, make_float2(-kf.x, -kf.y));
+                            const unsigned base = 0x4B400000u + (unsigned)k0;
+                            l0 = min(__float_as_uint(t.x) - base, (unsigned)(kSmWin - 1));
+                            l1 = min(__float_as_uint(t.y) - base, (unsigned)(kSmWin - 1));
+                        } else {
+                            const float2 kf = make_float2(floorf(ub.x), floorf(ub.y));
+                            f = __fadd2_rn(ub, make_float2(-kf.x, -kf.y));
+                            l0 = min((unsigned)((int)kf.x - k0), (unsigned)(kSmWin - 1));
+                            l1 = min((unsigned)((int)kf.y - k0), (unsigned)(kSmWin - 1));
+                        }
                         const float2 t0 = sr[l0], t1 = sr[l1];
                         const float2 v = make_float2(fmaf(f.x, t0.y, t0.x), fmaf(f.y, t1.y, t1.x));
                         const float2 acc2 = __ffma2_rn(v, w, make_float2(acc[r], acc[r + 1]));
@@ -887,13 +905,13 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
 }
 
 // MINB: resident blocks per SM the register allocation must allow
-template <int MINB, bool PK>
+template <int MINB, bool PK, bool MAGIC = false>
 __global__ void __launch_bounds__(256, MINB)
     k_bwd2d_smem(float *__restrict__ vol, const float2 *__restrict__ S,
                  const float4 *__restrict__ proj, int W, int H, int det, int nangles, float sx,
                  float sy, float ox, float oy, float ds) {
-    bwd2d_smem_tile<PK>(vol, S, proj, W, H, det, nangles, sx, sy, ox, oy, ds, blockIdx.x,
-                        blockIdx.y);
+    bwd2d_smem_tile<PK, MAGIC>(vol, S, proj, W, H, det, nangles, sx, sy, ox, oy, ds, blockIdx.x,
+                               blockIdx.y);
 }
 
 }  // namespace
@@ -1026,10 +1044,10 @@ int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s) {
     };
     switch (p.bwd_min_blocks) {
         case 3: go(k_bwd2d_smem<3, false>); break;
+        case 4: go(k_bwd2d_smem<4, false>); break;
         case 5: go(k_bwd2d_smem<5, false>); break;
         case 14: go(k_bwd2d_smem<4, true>); break;
-        case 15: go(k_bwd2d_smem<5, true>); break;
-        default: go(k_bwd2d_smem<4, false>); break;
+        default: go(k_bwd2d_smem<4, true, true>); break;
     }
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;

@@ -137,21 +137,21 @@ __global__ void __launch_bounds__(256)
     const float2 *L = xmajor ? B : A;
     const int Na = xmajor ? Z : X, Nc = xmajor ? X : Z;
     const int pa = Na + 2 * kP3, pb = Y + 2 * kP3;
-    const float amax = (float)Na, bmax = (float)Y, cmax = (float)Nc;
-    const float lo = -(float)kP3;
+    const unsigned acap = (unsigned)(Na + kP3), bcap = (unsigned)(Y + kP3),
+                   ccap = (unsigned)(Nc + kP3);
 
     float acc = 0.f;
     float t = tmin;
     for (int k = 0; k <= nsteps + 1; ++k) {
         if (!(t <= tmax)) break;
         const float pa_ = fmaf(da, t, sa), pb_ = fmaf(dy, t, s.y), pc_ = fmaf(dc, t, sc);
-        // texture coordinate p + 0.5 filtered at (p + 0.5) - 0.5 = p
-        const float fa = fminf(fmaxf(floorf(pa_), lo), amax);
-        const float fb = fminf(fmaxf(floorf(pb_), lo), bmax);
-        const float fc = fminf(fmaxf(floorf(pc_), lo), cmax);
-        const float wa = pa_ - fa, wb = pb_ - fb, wc = pc_ - fc;
-        const float2 *p00 =
-            L + ((size_t)((int)fc + kP3) * pb + ((int)fb + kP3)) * pa + ((int)fa + kP3);
+        // texture coordinate p + 0.5 filtered at (p + 0.5) - 0.5 = p; indices
+        // past the padded box clamp onto its zero border
+        const FloorSplit fa = floor_split(pa_, -kP3), fb = floor_split(pb_, -kP3),
+                         fc = floor_split(pc_, -kP3);
+        const float wa = fa.frac, wb = fb.frac, wc = fc.frac;
+        const float2 *p00 = L + ((size_t)min(fc.idx, ccap) * pb + min(fb.idx, bcap)) * pa +
+                            min(fa.idx, acap);
         const float2 t00 = __ldg(p00);
         const float2 t10 = __ldg(p00 + pa);
         const float2 t01 = __ldg(p00 + (size_t)pa * pb);

@@ -100,8 +100,10 @@ int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by);
  *   backward: 0 registers, 1 texture unit, 2 shared-memory detector windows
  * The texture unit filters with 8-bit weight fractions, exactly as the
  * reference does; the other algorithms filter in FP32, and cg_adjoint_2d is
- * the exact transpose of forward algorithms 0, 3 and 4.  A new plan starts at
- * the fastest measured combination. */
+ * the transpose of forward algorithms 0, 3 and 4 (exact for 0 and 3; 4 takes
+ * the same samples and weights, summed in another order).  A new plan starts
+ * at the fastest measured combination: forward 4 from 1536^2 pixels, else 1;
+ * backward 2. */
 int cg_plan2d_set_algorithm(cg_plan2d *plan, int forward, int backward);
 int cg_plan2d_get_algorithm(const cg_plan2d *plan, int *forward, int *backward);
 
@@ -167,7 +169,8 @@ int cg_plan3d_destroy(cg_plan3d *plan);
  *             1 texture unit (tex3D), 2 texture unit bilinear per layer +
  *             FP32 lerp across layers, 3 shared-memory slabs (FP32)
  *   backward: 0 registers
- * cg_adjoint_3d_plan is the exact transpose of forward algorithms 0 and 3. */
+ * cg_adjoint_3d_plan is the transpose of forward algorithms 0 and 3 (the
+ * same samples and trilinear weights, up to FP32 rounding). */
 int cg_plan3d_set_algorithm(cg_plan3d *plan, int forward, int backward);
 int cg_plan3d_get_algorithm(const cg_plan3d *plan, int *forward, int *backward);
 
