@@ -67,7 +67,7 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
         if (has("fwd2d=cslab")) p2->algo_fwd = 4;
         // chunk shapes: 4 (rows) x 512 (pairs) or 8 x 384 for 256-cell
         // bundles, 104 / 108: 4 or 8 x 256 for 128-cell bundles
-        for (int k : {4, 104, 108, 204, 304, 308}) {
+        for (int k : {4, 104, 108, 204, 304, 308, 404, 408}) {
             const std::string key = "fwd2d=cslab" + std::to_string(k);
             if (has(key.c_str())) p2->algo_fwd = 4, p2->fwd_chunk_rows = k;
         }
@@ -86,6 +86,8 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
         if (has("fwd3d=tex3")) p3->algo_fwd = 1;
         if (has("fwd3d=tex2l")) p3->algo_fwd = 2;
         if (has("fwd3d=slab")) p3->algo_fwd = 3;
+        if (has("bwd3d=pk")) p3->bwd_packed = true;
+        if (has("bwd3d=scalar")) p3->bwd_packed = false;
         const size_t at = e.find("fwd3d_block=");
         if (at != std::string::npos) {
             int bx = 0, by = 0, bz = 0;

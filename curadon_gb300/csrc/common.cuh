@@ -104,7 +104,8 @@ struct Plan2d {
     // becomes chunked for volumes of 1536^2 pixels and more (cg_plan2d_create).
     int algo_fwd = 1, algo_bwd = 2;
     int tex_eighths = 4;              // hybrid forward: share of warps on the texture unit
-    int fwd_chunk_rows = 308;         // chunked forward: chunk shape
+    int fwd_chunk_rows = 408;         // chunked forward: chunk shape (8 rows, 128-cell
+                                      // bundles, packed sums, pair reuse)
     // staged backprojector variant: 24 = 4 blocks/SM, packed FP32 pairs of
     // rows, floor taken by FP32 adds (default, measured fastest); 14 = the
     // same with the conversion unit's floor; 3, 4, 5 = scalar at 3..5 blocks/SM
@@ -155,6 +156,7 @@ struct Plan3d {
     // 3 = shared-memory slabs;
     // defaults: the fastest measured on GB300 (256^3 and 512^3 workloads)
     int algo_fwd = 1, algo_bwd = 0;
+    bool bwd_packed = true;  // backprojection: two voxels per packed FP32 instruction
     // texture forwards: detector cells (u, v) x views per thread block
     int fwd_bx = 8, fwd_by = 4, fwd_bz = 8;
 };

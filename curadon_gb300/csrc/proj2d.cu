@@ -464,7 +464,7 @@ struct RowAcc {
 // stepping towards smaller rows are summed in reverse), so the matched
 // adjoint is this forward's transpose up to the order of summation.  A chunk
 // whose window does not fit reads global memory.
-template <int K, int S, int T, bool PK>
+template <int K, int S, int T, bool PK, bool REUSE = false>
 __global__ void __launch_bounds__(T)
     k_fwd2d_cslab(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
                   float *__restrict__ sino, const float2 *__restrict__ tsrc,
@@ -588,13 +588,22 @@ __global__ void __launch_bounds__(T)
             for (int g = 0; g < kCs2G; ++g) {
                 const int rel = r0 - rlo[g];
                 if (rel >= 0 && rel + K <= len[g]) {
+                    // REUSE: row k's lower pair is row k-1's upper pair when the
+                    // column did not change (|step| <= 1 column per row), so
+                    // only the lanes whose column moved load it
+                    unsigned c_prev = 0xffffffffu;
+                    float2 hi_prev = make_float2(0.f, 0.f);
 #pragma unroll
                     for (int k = 0; k < K; ++k) {
                         const float pf = floorf(p[g]);
                         const float fp = p[g] - pf;
                         const unsigned c = min((unsigned)((int)pf - c0), cmax);
-                        const float2 lo = b0[k * S + c], hi = b0[(k + 1) * S + c];
+                        const float2 hi = b0[(k + 1) * S + c];
+                        float2 lo;
+                        if (REUSE && c == c_prev) lo = hi_prev;
+                        else lo = b0[k * S + c];
                         acc[g].add(fp, lo, hi);
+                        if (REUSE) c_prev = c, hi_prev = hi;
                         p[g] += V[g];
                     }
                 } else {
@@ -672,6 +681,8 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
         case 204: return go(k_fwd2d_cslab<4, 512, 256, true>, 4, 512, 256);
         case 304: return go(k_fwd2d_cslab<4, 256, 128, true>, 4, 256, 128);
         case 308: return go(k_fwd2d_cslab<8, 256, 128, true>, 8, 256, 128);
+        case 408: return go(k_fwd2d_cslab<8, 256, 128, true, true>, 8, 256, 128);
+        case 404: return go(k_fwd2d_cslab<4, 256, 128, true, true>, 4, 256, 128);
         default: return set_error(CG_ERR_INVALID, "unknown chunk shape");
     }
 }
