@@ -40,9 +40,11 @@ import numpy as np  # noqa: E402
 # the ncu captures summarised in profiles/, by workload and kernel; None
 # where not captured.
 NCU_TRAFFIC = {
-    ("fan2048", "k_fwd2d_cslab"): 80_510_592,  # profiles/dram_fan2048.md
-    ("fan2048", "k_bwd2d_smem"): 62_522_240,
+    ("fan2048", "k_fwd2d_cslab"): 80_521_088,  # profiles/dram_fan2048.md
+    ("fan2048", "k_bwd2d_smem"): 62_423_552,
     ("fan2048", "k_fwd2d_tex"): 17_007_744,    # the texture-unit forward (algorithm 1)
+    ("cone256", "k_fwd3d_tex3"): 172_266_542,  # profiles/k_bwd3d_cone256.md
+    ("cone256", "k_bwd3d"): 51_088_249,
 }
 
 # Main kernel of each operator by the plan's algorithm name.
