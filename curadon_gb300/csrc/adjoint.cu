@@ -93,8 +93,13 @@ __global__ void k_fold2d(float *__restrict__ vol, const float2 *__restrict__ A,
 
 // ------------------------------------------------------------ 3D
 
+// QUAD: the accumulators hold, per (a, b, c), the four contributions to
+// voxels (a, b), (a + 1, b), (a, b + 1), (a + 1, b + 1) of slice c as one
+// float4, so a sample is two 16-byte atomics instead of four 8-byte ones
+// (the scatter is bound by the L2's atomic operations).
+template <bool QUAD>
 __global__ void __launch_bounds__(256)
-    k_adj3d(float2 *__restrict__ A, float2 *__restrict__ B, const float *__restrict__ sino,
+    k_adj3d(void *__restrict__ A, void *__restrict__ B, const float *__restrict__ sino,
             const float4 *__restrict__ torg, const float4 *__restrict__ tdu,
             const float4 *__restrict__ tdv, const float4 *__restrict__ tsrc, int X, int Y, int Z,
             int U, int V) {
@@ -136,7 +141,7 @@ __global__ void __launch_bounds__(256)
     const bool xmajor = fabsf(dx) > fabsf(dz);
     const float sa = xmajor ? s.z : s.x, da = xmajor ? dz : dx;
     const float sc = xmajor ? s.x : s.z, dc = xmajor ? dx : dz;
-    float2 *L = xmajor ? B : A;
+    void *L = xmajor ? B : A;
     const int Na = xmajor ? Z : X, Nc = xmajor ? X : Z;
     const int pa = Na + 2 * kPad, pb = Y + 2 * kPad;
     const float amax = (float)Na, bmax = (float)Y, cmax = (float)Nc;
@@ -149,13 +154,21 @@ __global__ void __launch_bounds__(256)
         const float fb = fminf(fmaxf(floorf(pb_), lo), bmax);
         const float fc = fminf(fmaxf(floorf(pc_), lo), cmax);
         const float wa = pa_ - fa, wb = pb_ - fb, wc = pc_ - fc;
-        float2 *p00 = L + ((size_t)((int)fc + kPad) * pb + ((int)fb + kPad)) * pa + ((int)fa + kPad);
+        const size_t i00 = ((size_t)((int)fc + kPad) * pb + ((int)fb + kPad)) * pa + ((int)fa + kPad);
         const float c00 = c * (1.f - wb) * (1.f - wc), c10 = c * wb * (1.f - wc);
         const float c01 = c * (1.f - wb) * wc, c11 = c * wb * wc;
-        atomicAdd(p00, make_float2(c00 * (1.f - wa), c00 * wa));
-        atomicAdd(p00 + pa, make_float2(c10 * (1.f - wa), c10 * wa));
-        atomicAdd(p00 + (size_t)pa * pb, make_float2(c01 * (1.f - wa), c01 * wa));
-        atomicAdd(p00 + (size_t)pa * pb + pa, make_float2(c11 * (1.f - wa), c11 * wa));
+        if constexpr (QUAD) {
+            float4 *q = static_cast<float4 *>(L) + i00;
+            atomicAdd(q, make_float4(c00 * (1.f - wa), c00 * wa, c10 * (1.f - wa), c10 * wa));
+            atomicAdd(q + (size_t)pa * pb,
+                      make_float4(c01 * (1.f - wa), c01 * wa, c11 * (1.f - wa), c11 * wa));
+        } else {
+            float2 *p00 = static_cast<float2 *>(L) + i00;
+            atomicAdd(p00, make_float2(c00 * (1.f - wa), c00 * wa));
+            atomicAdd(p00 + pa, make_float2(c10 * (1.f - wa), c10 * wa));
+            atomicAdd(p00 + (size_t)pa * pb, make_float2(c01 * (1.f - wa), c01 * wa));
+            atomicAdd(p00 + (size_t)pa * pb + pa, make_float2(c11 * (1.f - wa), c11 * wa));
+        }
         t += h;
     }
 }
@@ -172,6 +185,23 @@ __global__ void k_fold3d(float *__restrict__ vol, const float2 *__restrict__ A,
     const float2 *ra = A + ((size_t)(z + kPad) * PY + (y + kPad)) * PX + (x + kPad);
     const float2 *rb = B + ((size_t)(x + kPad) * PY + (y + kPad)) * PZ + (z + kPad);
     vol[idx] += (ra[0].x + ra[-1].y) + (rb[0].x + rb[-1].y);
+}
+
+// The same fold for the quad accumulators: voxel (a, b) of slice c gathers
+// .x of (a, b), .y of (a - 1, b), .z of (a, b - 1) and .w of (a - 1, b - 1).
+__global__ void k_fold3d_quad(float *__restrict__ vol, const float4 *__restrict__ A,
+                              const float4 *__restrict__ B, int X, int Y, int Z) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)X * Y * Z) return;
+    const int x = (int)(idx % X);
+    const int y = (int)((idx / X) % Y);
+    const int z = (int)(idx / ((long long)X * Y));
+    const int PX = X + 2 * kPad, PY = Y + 2 * kPad, PZ = Z + 2 * kPad;
+    const float4 *ra = A + ((size_t)(z + kPad) * PY + (y + kPad)) * PX + (x + kPad);
+    const float4 *rb = B + ((size_t)(x + kPad) * PY + (y + kPad)) * PZ + (z + kPad);
+    const float sa = (ra[0].x + ra[-1].y) + (ra[-PX].z + ra[-PX - 1].w);
+    const float sb = (rb[0].x + rb[-1].y) + (rb[-PZ].z + rb[-PZ - 1].w);
+    vol[idx] += sa + sb;
 }
 
 }  // namespace
@@ -193,15 +223,33 @@ int launch_adjoint2d(const Plan2d &p, float *vol, const float *sino, cudaStream_
     return CG_OK;
 }
 
-int launch_adjoint3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s) {
-    CG_TRY_CUDA(cudaMemsetAsync(p.d_volA, 0, p.volA_elems * sizeof(float2), s));
-    CG_TRY_CUDA(cudaMemsetAsync(p.d_volB, 0, p.volB_elems * sizeof(float2), s));
+int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s) {
     if (p.nangles > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     dim3 grid(ceil_div(p.U, 32), ceil_div(p.V, 8), p.nangles);
-    k_adj3d<<<grid, dim3(32, 8), 0, s>>>(p.d_volA, p.d_volB, sino, p.d_forg, p.d_fdu, p.d_fdv,
-                                         p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V);
-    CG_TRY_CUDA(cudaGetLastError());
     const long long n = (long long)p.X * p.Y * p.Z;
+    const size_t elems = (size_t)(p.X + 2 * kPad) * (p.Y + 2 * kPad) * (p.Z + 2 * kPad);
+    // measured: quads are 31 % faster at 128^3 (74 MB of accumulators) and
+    // 2.5 % slower at 256^3 (281 MB), where the atomics spill out of L2
+    const bool quad = p.adj_quad > 0 || (p.adj_quad < 0 && 2 * elems * sizeof(float4) <= (96u << 20));
+    if (quad) {
+        if (!p.d_quadA) {
+            CG_TRY_CUDA(cudaMalloc(&p.d_quadA, elems * sizeof(float4)));
+            CG_TRY_CUDA(cudaMalloc(&p.d_quadB, elems * sizeof(float4)));
+        }
+        CG_TRY_CUDA(cudaMemsetAsync(p.d_quadA, 0, elems * sizeof(float4), s));
+        CG_TRY_CUDA(cudaMemsetAsync(p.d_quadB, 0, elems * sizeof(float4), s));
+        k_adj3d<true><<<grid, dim3(32, 8), 0, s>>>(p.d_quadA, p.d_quadB, sino, p.d_forg, p.d_fdu,
+                                                   p.d_fdv, p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V);
+        CG_TRY_CUDA(cudaGetLastError());
+        k_fold3d_quad<<<ceil_div(n, 256), 256, 0, s>>>(vol, p.d_quadA, p.d_quadB, p.X, p.Y, p.Z);
+        CG_TRY_CUDA(cudaGetLastError());
+        return CG_OK;
+    }
+    CG_TRY_CUDA(cudaMemsetAsync(p.d_volA, 0, p.volA_elems * sizeof(float2), s));
+    CG_TRY_CUDA(cudaMemsetAsync(p.d_volB, 0, p.volB_elems * sizeof(float2), s));
+    k_adj3d<false><<<grid, dim3(32, 8), 0, s>>>(p.d_volA, p.d_volB, sino, p.d_forg, p.d_fdu,
+                                                p.d_fdv, p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V);
+    CG_TRY_CUDA(cudaGetLastError());
     k_fold3d<<<ceil_div(n, 256), 256, 0, s>>>(vol, p.d_volA, p.d_volB, p.X, p.Y, p.Z);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;

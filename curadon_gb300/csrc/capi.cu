@@ -50,7 +50,8 @@ void free_plan3d(Plan3d *p) {
         if (a) cudaFreeArray(a);
     if (p->d_volT) cudaFree(p->d_volT);
     void *ptrs[] = {p->d_forg, p->d_fdu, p->d_fdv, p->d_fsrc, p->d_borg, p->d_bdx,
-                    p->d_bdy,  p->d_bdz, p->d_volA, p->d_volB, p->d_sinoP};
+                    p->d_bdy,  p->d_bdz, p->d_volA, p->d_volB, p->d_sinoP, p->d_quadA,
+                    p->d_quadB};
     for (void *q : ptrs)
         if (q) cudaFree(q);
 }
@@ -86,8 +87,11 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
         if (has("fwd3d=tex3")) p3->algo_fwd = 1;
         if (has("fwd3d=tex2l")) p3->algo_fwd = 2;
         if (has("fwd3d=slab")) p3->algo_fwd = 3;
-        if (has("bwd3d=pk")) p3->bwd_packed = true;
-        if (has("bwd3d=scalar")) p3->bwd_packed = false;
+        if (has("bwd3d=pk")) p3->bwd_packed = 1;
+        if (has("bwd3d=pkmagic")) p3->bwd_packed = 2;
+        if (has("bwd3d=scalar")) p3->bwd_packed = 0;
+        if (has("adj3d=pair")) p3->adj_quad = 0;
+        if (has("adj3d=quad")) p3->adj_quad = 1;
         const size_t at = e.find("fwd3d_block=");
         if (at != std::string::npos) {
             int bx = 0, by = 0, bz = 0;

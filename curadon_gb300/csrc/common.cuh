@@ -146,6 +146,11 @@ struct Plan3d {
     float2 *d_volB = nullptr;         // (X+2P)(Y+2P)(Z+2P) pairs along z
     float2 *d_sinoP = nullptr;        // nangles (V+2P)(U+2P) pairs along u
     size_t volA_elems = 0, volB_elems = 0, sinoP_elems = 0;
+    // matched adjoint: quad accumulators (float4 per padded voxel), on first
+    // use; adj_quad -1 = when both fit in 96 MB (the L2 holds the atomics),
+    // 1 = always, 0 = never (pair accumulators)
+    float4 *d_quadA = nullptr, *d_quadB = nullptr;
+    int adj_quad = -1;
 
     // texture-unit variants (allocated on first use)
     cudaArray_t arr3 = nullptr, arrA = nullptr, arrB = nullptr;
@@ -156,7 +161,10 @@ struct Plan3d {
     // 3 = shared-memory slabs;
     // defaults: the fastest measured on GB300 (256^3 and 512^3 workloads)
     int algo_fwd = 1, algo_bwd = 0;
-    bool bwd_packed = true;  // backprojection: two voxels per packed FP32 instruction
+    // backprojection: 2 = two voxels per packed FP32 instruction with the
+    // floor by FP32 adds (default, measured fastest), 1 = packed with the
+    // conversion unit's floor, 0 = one voxel at a time
+    int bwd_packed = 2;
     // texture forwards: detector cells (u, v) x views per thread block
     int fwd_bx = 8, fwd_by = 4, fwd_bz = 8;
 };
@@ -194,7 +202,7 @@ int launch_forward3d_slab(Plan3d &p, const float *vol, float *sino, cudaStream_t
 int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s);
 
 int launch_adjoint2d(const Plan2d &p, float *vol, const float *sino, cudaStream_t s);
-int launch_adjoint3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s);
+int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s);
 
 int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s);
 bool slab_supported(const Plan2d &p);

@@ -455,7 +455,8 @@ struct BwdTab {
 
 // Block = 32 (x) x 8 (y) threads, each with a run of kBZ voxels along z
 // (PK: taken two at a time with packed FP32 instructions, 11 % faster at
-// 512^3 than one at a time).
+// 512^3 than one at a time; MAGIC: the detector floor by FP32 adds,
+// floor_split two at a time, another 4 %).
 // Blocks are visited brick by brick (2 x 8 x 8 tiles) so that the blocks
 // resident at one time cover a compact region of the volume and share the
 // detector footprint they read from L2.  Per voxel and view: the reference's
@@ -463,7 +464,7 @@ struct BwdTab {
 // stepped along z from the run's first voxel -- then a bilinear sample of the
 // difference-encoded pair-packed projection in two 8-byte loads and three
 // FMAs, accumulated in registers; the volume is read and written once.
-template <bool PK>
+template <bool PK, bool MAGIC = false>
 __global__ void __launch_bounds__(256)
     k_bwd3d(float *__restrict__ vol, const float2 *__restrict__ S,
             const float4 *__restrict__ torg, const float4 *__restrict__ tdx,
@@ -526,14 +527,33 @@ __global__ void __launch_bounds__(256)
                     const float2 t = __fmul2_rn(
                         N2, make_float2(__fdividef(1.0f, DZ.x), __fdividef(1.0f, DZ.y)));
                     const float2 ub = __ffma2_rn(DX, t, SU), vb = __ffma2_rn(DY, t, SV);
-                    const int iu0 = __float2int_rd(ub.x), iu1 = __float2int_rd(ub.y);
-                    const int iv0 = __float2int_rd(vb.x), iv1 = __float2int_rd(vb.y);
-                    const float2 wu = __fadd2_rn(ub, make_float2(-(float)iu0, -(float)iu1));
-                    const float2 wv = __fadd2_rn(vb, make_float2(-(float)iv0, -(float)iv1));
-                    const float2 *q0 = plane + min((unsigned)(iv0 + kP3), vcap) * PU +
-                                       min((unsigned)(iu0 + kP3), ucap);
-                    const float2 *q1 = plane + min((unsigned)(iv1 + kP3), vcap) * PU +
-                                       min((unsigned)(iu1 + kP3), ucap);
+                    float2 wu, wv;
+                    unsigned cu0, cu1, cv0, cv1;
+                    if constexpr (MAGIC) {
+                        // floor by packed FP32 adds (floor_split, two at a time)
+                        const float2 m = make_float2(12582912.0f, 12582912.0f);
+                        const float2 h = make_float2(-0.5f, -0.5f), nm = make_float2(-12582912.0f,
+                                                                                     -12582912.0f);
+                        const float2 tu = __fadd2_rn(__fadd2_rn(ub, h), m);
+                        const float2 tv = __fadd2_rn(__fadd2_rn(vb, h), m);
+                        const float2 ku = __fadd2_rn(tu, nm), kv = __fadd2_rn(tv, nm);
+                        wu = __fadd2_rn(ub, make_float2(-ku.x, -ku.y));
+                        wv = __fadd2_rn(vb, make_float2(-kv.x, -kv.y));
+                        const unsigned base = 0x4B400000u - (unsigned)kP3;
+                        cu0 = min(__float_as_uint(tu.x) - base, ucap);
+                        cu1 = min(__float_as_uint(tu.y) - base, ucap);
+                        cv0 = min(__float_as_uint(tv.x) - base, vcap);
+                        cv1 = min(__float_as_uint(tv.y) - base, vcap);
+                    } else {
+                        const int iu0 = __float2int_rd(ub.x), iu1 = __float2int_rd(ub.y);
+                        const int iv0 = __float2int_rd(vb.x), iv1 = __float2int_rd(vb.y);
+                        wu = __fadd2_rn(ub, make_float2(-(float)iu0, -(float)iu1));
+                        wv = __fadd2_rn(vb, make_float2(-(float)iv0, -(float)iv1));
+                        cu0 = min((unsigned)(iu0 + kP3), ucap), cu1 = min((unsigned)(iu1 + kP3), ucap);
+                        cv0 = min((unsigned)(iv0 + kP3), vcap), cv1 = min((unsigned)(iv1 + kP3), vcap);
+                    }
+                    const float2 *q0 = plane + cv0 * PU + cu0;
+                    const float2 *q1 = plane + cv1 * PU + cu1;
                     const float2 a0 = __ldg(q0), b0 = __ldg(q0 + PU);
                     const float2 a1 = __ldg(q1), b1 = __ldg(q1 + PU);
                     const float2 l0 = make_float2(fmaf(wu.x, a0.y, a0.x), fmaf(wu.y, a1.y, a1.x));
@@ -644,7 +664,9 @@ int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream
     const int bricks = ceil_div(tiles_x, 2) * ceil_div(tiles_y, 8) * ceil_div(tiles_z, 8);
     const float zplane = p.DSO - p.DSD;
     const float hu = (float)(p.U / 2), hv = (float)(p.V / 2);
-    auto kernel = p.bwd_packed ? k_bwd3d<true> : k_bwd3d<false>;
+    auto kernel = p.bwd_packed == 2 ? k_bwd3d<true, true>
+                  : p.bwd_packed      ? k_bwd3d<true, false>
+                                      : k_bwd3d<false, false>;
     kernel<<<bricks * 128, dim3(32, 8), 0, s>>>(
         vol, p.d_sinoP, p.d_borg, p.d_bdx, p.d_bdy, p.d_bdz, p.bsrc[0], p.bsrc[1], p.bsrc[2],
         zplane, hu, hv, p.X, p.Y, p.Z, p.U, p.V, p.nangles, tiles_x, tiles_y, tiles_z);
