@@ -5,6 +5,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -56,47 +57,72 @@ void free_plan3d(Plan3d *p) {
         if (q) cudaFree(q);
 }
 
+// Overrides of a new plan's algorithms for measurement and testing, read
+// from CURADON_GB300_ALGO: comma-separated key=value tokens, e.g.
+// "fwd2d=tex,bwd2d_minb=4".  Keys: fwd2d = alu | tex | slab | cslab |
+// cslab<shape> | hyb<1..7>; bwd2d = alu | tex | smem; bwd2d_minb = 3 | 4 | 5
+// | 14 | 24; fwd3d = alu | tex3 | tex2l | slab; fwd3d_block = BXxBYxBZ;
+// bwd3d = scalar | pk | pkmagic; adj3d = pair | quad.  Unknown tokens are
+// ignored; without the variable every plan starts at the measured defaults.
 void apply_algo_env(Plan2d *p2, Plan3d *p3) {
     const char *env = std::getenv("CURADON_GB300_ALGO");
     if (!env) return;
-    std::string e(env);
-    auto has = [&](const char *kv) { return e.find(kv) != std::string::npos; };
-    if (p2) {
-        if (has("fwd2d=alu")) p2->algo_fwd = 0;
-        if (has("fwd2d=tex")) p2->algo_fwd = 1;
-        if (has("fwd2d=slab")) p2->algo_fwd = 3;
-        if (has("fwd2d=cslab")) p2->algo_fwd = 4;
-        // chunk shapes: 4 (rows) x 512 (pairs) or 8 x 384 for 256-cell
-        // bundles, 104 / 108: 4 or 8 x 256 for 128-cell bundles
-        for (int k : {4, 104, 108, 204, 304, 308, 404, 408}) {
-            const std::string key = "fwd2d=cslab" + std::to_string(k);
-            if (has(key.c_str())) p2->algo_fwd = 4, p2->fwd_chunk_rows = k;
+    std::vector<std::pair<std::string, std::string>> kv;
+    {
+        std::string e(env), tok;
+        for (size_t i = 0; i <= e.size(); ++i) {
+            if (i == e.size() || e[i] == ',') {
+                const size_t eq = tok.find('=');
+                if (eq != std::string::npos) kv.emplace_back(tok.substr(0, eq), tok.substr(eq + 1));
+                tok.clear();
+            } else {
+                tok += e[i];
+            }
         }
-        for (int k = 1; k < 8; ++k) {
-            const std::string key = "fwd2d=hyb" + std::to_string(k);
-            if (has(key.c_str())) p2->algo_fwd = 2, p2->tex_eighths = k;
-        }
-        if (has("bwd2d=alu")) p2->algo_bwd = 0;
-        if (has("bwd2d=tex")) p2->algo_bwd = 1;
-        if (has("bwd2d=smem")) p2->algo_bwd = 2;
-        for (int k : {3, 4, 5, 14, 24})
-            if (has(("bwd2d_minb=" + std::to_string(k)).c_str())) p2->bwd_min_blocks = k;
     }
-    if (p3) {
-        if (has("fwd3d=alu")) p3->algo_fwd = 0;
-        if (has("fwd3d=tex3")) p3->algo_fwd = 1;
-        if (has("fwd3d=tex2l")) p3->algo_fwd = 2;
-        if (has("fwd3d=slab")) p3->algo_fwd = 3;
-        if (has("bwd3d=pk")) p3->bwd_packed = 1;
-        if (has("bwd3d=pkmagic")) p3->bwd_packed = 2;
-        if (has("bwd3d=scalar")) p3->bwd_packed = 0;
-        if (has("adj3d=pair")) p3->adj_quad = 0;
-        if (has("adj3d=quad")) p3->adj_quad = 1;
-        const size_t at = e.find("fwd3d_block=");
-        if (at != std::string::npos) {
+    for (const auto &[key, val] : kv) {
+        if (p2 && key == "fwd2d") {
+            if (val == "alu") p2->algo_fwd = 0;
+            if (val == "tex") p2->algo_fwd = 1;
+            if (val == "slab") p2->algo_fwd = 3;
+            if (val.rfind("cslab", 0) == 0) {
+                p2->algo_fwd = 4;
+                // chunk shapes: 4 (rows x 512-pair rows, 256-cell bundles), 104 / 108
+                // (4 / 8 rows, 128-cell bundles), 204 / 304 / 308 (packed sums),
+                // 404 / 408 (packed sums and pair reuse)
+                for (int k : {4, 104, 108, 204, 304, 308, 404, 408})
+                    if (val == "cslab" + std::to_string(k)) p2->fwd_chunk_rows = k;
+            }
+            for (int k = 1; k < 8; ++k)
+                if (val == "hyb" + std::to_string(k)) p2->algo_fwd = 2, p2->tex_eighths = k;
+        }
+        if (p2 && key == "bwd2d") {
+            if (val == "alu") p2->algo_bwd = 0;
+            if (val == "tex") p2->algo_bwd = 1;
+            if (val == "smem") p2->algo_bwd = 2;
+        }
+        if (p2 && key == "bwd2d_minb")
+            for (int k : {3, 4, 5, 14, 24})
+                if (val == std::to_string(k)) p2->bwd_min_blocks = k;
+        if (p3 && key == "fwd3d") {
+            if (val == "alu") p3->algo_fwd = 0;
+            if (val == "tex3") p3->algo_fwd = 1;
+            if (val == "tex2l") p3->algo_fwd = 2;
+            if (val == "slab") p3->algo_fwd = 3;
+        }
+        if (p3 && key == "bwd3d") {
+            if (val == "scalar") p3->bwd_packed = 0;
+            if (val == "pk") p3->bwd_packed = 1;
+            if (val == "pkmagic") p3->bwd_packed = 2;
+        }
+        if (p3 && key == "adj3d") {
+            if (val == "pair") p3->adj_quad = 0;
+            if (val == "quad") p3->adj_quad = 1;
+        }
+        if (p3 && key == "fwd3d_block") {
             int bx = 0, by = 0, bz = 0;
-            if (std::sscanf(e.c_str() + at + 12, "%dx%dx%d", &bx, &by, &bz) == 3 && bx > 0 &&
-                by > 0 && bz > 0 && bx * by * bz <= 1024 && bx % 8 == 0)
+            if (std::sscanf(val.c_str(), "%dx%dx%d", &bx, &by, &bz) == 3 && bx > 0 && by > 0 &&
+                bz > 0 && bx * by * bz <= 1024 && bx % 8 == 0)
                 p3->fwd_bx = bx, p3->fwd_by = by, p3->fwd_bz = bz;
         }
     }
