@@ -4,7 +4,8 @@
 // Each kernel repeats its forward's ray set-up and sample points exactly and
 // scatters y_ray * (filter weights) into the same pair-packed, zero-padded
 // layouts the forward gathers from, with one 8-byte vector atomic per pair
-// (red.global.add.v2.f32).  A fold pass then adds the pair entries back onto
+// (red.global.add.v2.f32), or -- when the accumulators fit in L2 -- one
+// 16-byte atomic per sample into quad accumulators.  A fold pass then adds the pair entries back onto
 // the texels they cover; entries that land in the padding correspond to the
 // zero border the forward reads and are dropped, so the result is the exact
 // transpose of the forward as implemented.  The curadon reference has no
@@ -19,8 +20,12 @@ namespace {
 
 // ------------------------------------------------------------ 2D
 
+// QUAD: one float4 per (row, column) of the layout holding the contributions
+// to (row, col), (row, col + 1), (row + 1, col), (row + 1, col + 1), so a
+// sample is one 16-byte atomic instead of two 8-byte ones.
+template <bool QUAD>
 __global__ void __launch_bounds__(256)
-    k_adj2d(float2 *__restrict__ accA, float2 *__restrict__ accB, const float *__restrict__ sino,
+    k_adj2d(void *__restrict__ accA, void *__restrict__ accB, const float *__restrict__ sino,
             const float2 *__restrict__ tsrc, const float2 *__restrict__ tu0,
             const float2 *__restrict__ tdu, int W, int H, int det, int nangles, float sx,
             float sy, int pa, int pb) {
@@ -57,7 +62,7 @@ __global__ void __launch_bounds__(256)
     const float vp = ymajor ? vx : vy;
     const float q = (ymajor ? roy : rox) - 0.5f;
     const int sq = ((ymajor ? vy : vx) > 0.f) ? 1 : -1;
-    float2 *acc = ymajor ? accA : accB;
+    void *acc = ymajor ? accA : accB;
     const int pitch = ymajor ? pa : pb;
     const float pmax = (float)(ymajor ? W : H);
     const int qmax = ymajor ? H : W;
@@ -65,7 +70,7 @@ __global__ void __launch_bounds__(256)
     const float fq = q - qf;
     const int iq = (int)fminf(fmaxf(qf, -(float)kPad), (float)qmax);
     n = min(n, sq > 0 ? qmax - iq + 1 : iq + kPad + 1);
-    float2 *row = acc + (size_t)(iq + kPad) * pitch + kPad;
+    long long ri = (long long)(iq + kPad) * pitch + kPad;  // element of the row start
     const long long rstep = (long long)sq * pitch;
     const float clo = c * (1.f - fq), chi = c * fq;
     for (int j = 0; j < n; ++j) {
@@ -73,11 +78,30 @@ __global__ void __launch_bounds__(256)
         const float fp = p - pf;
         const int ip = (int)pf;
         // forward: lo = x + fp (y - x) -> weights (1 - fp, fp) on the pair
-        atomicAdd(row + ip, make_float2(clo * (1.f - fp), clo * fp));
-        atomicAdd(row + pitch + ip, make_float2(chi * (1.f - fp), chi * fp));
+        if constexpr (QUAD) {
+            atomicAdd(static_cast<float4 *>(acc) + ri + ip,
+                      make_float4(clo * (1.f - fp), clo * fp, chi * (1.f - fp), chi * fp));
+        } else {
+            float2 *row = static_cast<float2 *>(acc) + ri;
+            atomicAdd(row + ip, make_float2(clo * (1.f - fp), clo * fp));
+            atomicAdd(row + pitch + ip, make_float2(chi * (1.f - fp), chi * fp));
+        }
         p += vp;
-        row += rstep;
+        ri += rstep;
     }
+}
+
+// vol[y][x] += the four quad entries covering (x, y) in each layout.
+__global__ void k_fold2d_quad(float *__restrict__ vol, const float4 *__restrict__ A,
+                              const float4 *__restrict__ B, int W, int H, int pa, int pb) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const float4 *ra = A + (size_t)(y + kPad) * pa + (x + kPad);
+    const float4 *rb = B + (size_t)(x + kPad) * pb + (y + kPad);
+    const float sa = (ra[0].x + ra[-1].y) + (ra[-pa].z + ra[-pa - 1].w);
+    const float sb = (rb[0].x + rb[-1].y) + (rb[-pb].z + rb[-pb - 1].w);
+    vol[(size_t)y * W + x] += sa + sb;
 }
 
 // vol[y][x] += A[y][x].x + A[y][x-1].y + B[x][y].x + B[x][y-1].y (padded).
@@ -206,19 +230,38 @@ __global__ void k_fold3d_quad(float *__restrict__ vol, const float4 *__restrict_
 
 }  // namespace
 
-int launch_adjoint2d(const Plan2d &p, float *vol, const float *sino, cudaStream_t s) {
+int launch_adjoint2d(Plan2d &p, float *vol, const float *sino, cudaStream_t s) {
     const size_t na = (size_t)p.pitchA() * (p.H + 2 * kPad);
     const size_t nb = (size_t)p.pitchB() * (p.W + 2 * kPad);
-    CG_TRY_CUDA(cudaMemsetAsync(p.d_layA, 0, na * sizeof(float2), s));
-    CG_TRY_CUDA(cudaMemsetAsync(p.d_layB, 0, nb * sizeof(float2), s));
     dim3 block(p.fwd_bx, p.fwd_by);
     dim3 grid(ceil_div(p.det, p.fwd_bx), ceil_div(p.nangles, p.fwd_by));
     if (grid.y > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
-    k_adj2d<<<grid, block, 0, s>>>(p.d_layA, p.d_layB, sino, p.d_src, p.d_u0, p.d_du, p.W, p.H,
-                                   p.det, p.nangles, p.sx, p.sy, p.pitchA(), p.pitchB());
+    const dim3 fgrid(ceil_div(p.W, 32), ceil_div(p.H, 8));
+    // quad accumulators when both fit in 96 MB, where the L2 holds the atomics
+    if (p.adj_quad > 0 || (p.adj_quad < 0 && (na + nb) * sizeof(float4) <= (96u << 20))) {
+        if (!p.d_quadA) {
+            CG_TRY_CUDA(cudaMalloc(&p.d_quadA, na * sizeof(float4)));
+            CG_TRY_CUDA(cudaMalloc(&p.d_quadB, nb * sizeof(float4)));
+        }
+        CG_TRY_CUDA(cudaMemsetAsync(p.d_quadA, 0, na * sizeof(float4), s));
+        CG_TRY_CUDA(cudaMemsetAsync(p.d_quadB, 0, nb * sizeof(float4), s));
+        k_adj2d<true><<<grid, block, 0, s>>>(p.d_quadA, p.d_quadB, sino, p.d_src, p.d_u0, p.d_du,
+                                             p.W, p.H, p.det, p.nangles, p.sx, p.sy, p.pitchA(),
+                                             p.pitchB());
+        CG_TRY_CUDA(cudaGetLastError());
+        k_fold2d_quad<<<fgrid, dim3(32, 8), 0, s>>>(vol, p.d_quadA, p.d_quadB, p.W, p.H,
+                                                    p.pitchA(), p.pitchB());
+        CG_TRY_CUDA(cudaGetLastError());
+        return CG_OK;
+    }
+    CG_TRY_CUDA(cudaMemsetAsync(p.d_layA, 0, na * sizeof(float2), s));
+    CG_TRY_CUDA(cudaMemsetAsync(p.d_layB, 0, nb * sizeof(float2), s));
+    k_adj2d<false><<<grid, block, 0, s>>>(p.d_layA, p.d_layB, sino, p.d_src, p.d_u0, p.d_du, p.W,
+                                          p.H, p.det, p.nangles, p.sx, p.sy, p.pitchA(),
+                                          p.pitchB());
     CG_TRY_CUDA(cudaGetLastError());
-    k_fold2d<<<dim3(ceil_div(p.W, 32), ceil_div(p.H, 8)), dim3(32, 8), 0, s>>>(
-        vol, p.d_layA, p.d_layB, p.W, p.H, p.pitchA(), p.pitchB());
+    k_fold2d<<<fgrid, dim3(32, 8), 0, s>>>(vol, p.d_layA, p.d_layB, p.W, p.H, p.pitchA(),
+                                           p.pitchB());
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }

@@ -38,7 +38,7 @@ void free_plan2d(Plan2d *p) {
     if (p->arr_sino) cudaFreeArray(p->arr_sino);
     void *ptrs[] = {p->d_angles, p->d_DSO,   p->d_DSD,   p->d_src,   p->d_u0,    p->d_du,
                     p->d_bmeta,  p->d_bproj, p->d_layA,  p->d_layB,  p->d_sinoP, p->d_vol32,
-                    p->d_sino32};
+                    p->d_sino32, p->d_quadA, p->d_quadB};
     for (void *q : ptrs)
         if (q) cudaFree(q);
 }
@@ -61,7 +61,8 @@ void free_plan3d(Plan3d *p) {
 // from CURADON_GB300_ALGO: comma-separated key=value tokens, e.g.
 // "fwd2d=tex,bwd2d_minb=4".  Keys: fwd2d = alu | tex | slab | cslab |
 // cslab<shape> | hyb<1..7>; bwd2d = alu | tex | smem; bwd2d_minb = 3 | 4 | 5
-// | 14 | 24; fwd3d = alu | tex3 | tex2l | slab; fwd3d_block = BXxBYxBZ;
+// | 14 | 24; adj2d = pair | quad; fwd3d = alu | tex3 | tex2l | slab;
+// fwd3d_block = BXxBYxBZ;
 // bwd3d = scalar | pk | pkmagic; adj3d = pair | quad.  Unknown tokens are
 // ignored; without the variable every plan starts at the measured defaults.
 void apply_algo_env(Plan2d *p2, Plan3d *p3) {
@@ -100,6 +101,10 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
             if (val == "alu") p2->algo_bwd = 0;
             if (val == "tex") p2->algo_bwd = 1;
             if (val == "smem") p2->algo_bwd = 2;
+        }
+        if (p2 && key == "adj2d") {
+            if (val == "pair") p2->adj_quad = 0;
+            if (val == "quad") p2->adj_quad = 1;
         }
         if (p2 && key == "bwd2d_minb")
             for (int k : {3, 4, 5, 14, 24})

@@ -92,6 +92,12 @@ struct Plan2d {
     int vol_bits = 32, det_bits = 32;
     float *d_vol32 = nullptr, *d_sino32 = nullptr;
 
+    // matched adjoint: quad accumulators (float4 per padded texel of layA /
+    // layB), allocated on first use; adj_quad -1 = when both fit in 96 MB,
+    // 1 = always, 0 = never (pair accumulators in layA / layB)
+    float4 *d_quadA = nullptr, *d_quadB = nullptr;
+    int adj_quad = -1;
+
     // texture-unit variants (allocated on first use)
     cudaArray_t arr_vol = nullptr, arr_sino = nullptr;
     cudaTextureObject_t tex_vol = 0, tex_sino = 0;
@@ -201,7 +207,7 @@ int launch_forward3d(const Plan3d &p, const float *vol, float *sino, cudaStream_
 int launch_forward3d_slab(Plan3d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s);
 
-int launch_adjoint2d(const Plan2d &p, float *vol, const float *sino, cudaStream_t s);
+int launch_adjoint2d(Plan2d &p, float *vol, const float *sino, cudaStream_t s);
 int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s);
 
 int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s);

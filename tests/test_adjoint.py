@@ -38,6 +38,18 @@ def test_dot_product_2d(cuda_device, n, nangles):
     assert dot_test(geom, x, y, cuda_device) < 1e-5
 
 
+def test_dot_product_2d_pair_accumulators(cuda_device):
+    """Above ~1700^2 pixels the adjoint's accumulators no longer fit the L2
+    as quads and it scatters into pairs instead: the same transpose."""
+    n = 1800
+    g = fan_config(n, 48)
+    geom = FanGeometry(**g)
+    rng = np.random.default_rng(3)
+    x = rng.uniform(0, 1, (n, n)).astype(np.float32)
+    y = rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32)
+    assert dot_test(geom, x, y, cuda_device) < 1e-5
+
+
 def test_dot_product_2d_offsets(cuda_device):
     g = fan_config(48, 37, 70, 1.3, 90.0, 150.0)
     g.update(vol_shape=(48, 60), vol_spacing=(0.9, 1.2), vol_offset=(2.0, -3.0), det_offset=1.5)

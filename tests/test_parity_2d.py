@@ -227,3 +227,21 @@ def test_runs_on_the_current_stream(cuda_device):
         r = s.sum()
     st.synchronize()
     assert torch.equal(s, expect) and float(r) == pytest.approx(float(expect.sum()), rel=1e-6)
+
+
+def test_algorithm_override_variable(cuda_device):
+    """CURADON_GB300_ALGO (comma-separated key=value tokens) sets the
+    algorithms of plans made in that process; unknown tokens are ignored."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    code = ("import curadon_gb300 as cg\n"
+            "from curadon_gb300.phantom import fan_config\n"
+            "print(cg.FanGeometry(**fan_config(64, 30)).plan.algorithm)\n")
+    env = dict(os.environ, CURADON_GB300_ALGO="fwd2d=alu,bwd2d=tex,nonsense=1")
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                         cwd=Path(__file__).resolve().parents[1], timeout=300)
+    assert out.returncode == 0, out.stderr
+    assert "('registers', 'texture')" in out.stdout, out.stdout
