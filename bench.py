@@ -55,7 +55,8 @@ KERNELS = {
     ("fan", "backward", "registers"): "k_bwd2d", ("fan", "backward", "texture"): "k_bwd2d_tex",
     ("cone", "forward", "texture"): "k_fwd3d_tex3", ("cone", "forward", "layered"): "k_fwd3d_tex2l",
     ("cone", "forward", "registers"): "k_fwd3d", ("cone", "forward", "slab"): "k_fwd3d_slab",
-    ("cone", "backward", "registers"): "k_bwd3d",
+    ("cone", "forward", "quad"): "k_fwd3d_quad", ("cone", "forward", "mixed"): "k_fwd3d_quad",
+    ("cone", "backward", "registers"): "k_bwd3d", ("cone", "backward", "axial"): "k_bwd3d_ax",
 }
 
 

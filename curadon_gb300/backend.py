@@ -44,8 +44,8 @@ def _stream(t: torch.Tensor) -> C.c_void_p:
 
 FORWARD_2D = ("registers", "texture", "hybrid", "slab", "chunked")
 BACKWARD_2D = ("registers", "texture", "shared")
-FORWARD_3D = ("registers", "texture", "layered", "slab")
-BACKWARD_3D = ("registers",)
+FORWARD_3D = ("registers", "texture", "layered", "slab", "quad", "mixed")
+BACKWARD_3D = ("registers", "axial")
 
 
 def _algo_index(name, names, what):

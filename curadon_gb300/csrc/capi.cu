@@ -52,7 +52,7 @@ void free_plan3d(Plan3d *p) {
     if (p->d_volT) cudaFree(p->d_volT);
     void *ptrs[] = {p->d_forg, p->d_fdu, p->d_fdv, p->d_fsrc, p->d_borg, p->d_bdx,
                     p->d_bdy,  p->d_bdz, p->d_volA, p->d_volB, p->d_sinoP, p->d_quadA,
-                    p->d_quadB};
+                    p->d_quadB, p->d_sinoQ, p->d_volQA, p->d_volQB};
     for (void *q : ptrs)
         if (q) cudaFree(q);
 }
@@ -61,9 +61,11 @@ void free_plan3d(Plan3d *p) {
 // from CURADON_GB300_ALGO: comma-separated key=value tokens, e.g.
 // "fwd2d=tex,bwd2d_minb=4".  Keys: fwd2d = alu | tex | slab | cslab |
 // cslab<shape> | hyb<1..7>; bwd2d = alu | tex | smem; bwd2d_minb = 3 | 4 | 5
-// | 14 | 24; adj2d = pair | quad; fwd3d = alu | tex3 | tex2l | slab;
+// | 14 | 24; adj2d = pair | quad; fwd3d = alu | tex3 | tex2l | slab | quad |
+// mixed; fwd3d_tex = 0..8 (texture warps of 8 in forward 5);
 // fwd3d_block = BXxBYxBZ;
-// bwd3d = scalar | pk | pkmagic; adj3d = pair | quad.  Unknown tokens are
+// bwd3d = scalar | pk | pkmagic | quad (backward 0) | ax8m5 | ax8 | ax16 |
+// ax16m4 (backward 1); adj3d = pair | quad.  Unknown tokens are
 // ignored; without the variable every plan starts at the measured defaults.
 void apply_algo_env(Plan2d *p2, Plan3d *p3) {
     const char *env = std::getenv("CURADON_GB300_ALGO");
@@ -114,11 +116,19 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
             if (val == "tex3") p3->algo_fwd = 1;
             if (val == "tex2l") p3->algo_fwd = 2;
             if (val == "slab") p3->algo_fwd = 3;
+            if (val == "quad") p3->algo_fwd = 4;
+            if (val == "mixed") p3->algo_fwd = 5;
         }
+        if (p3 && key == "fwd3d_tex")
+            for (int k = 0; k <= 8; ++k)
+                if (val == std::to_string(k)) p3->fwd_tex_warps = k;
         if (p3 && key == "bwd3d") {
-            if (val == "scalar") p3->bwd_packed = 0;
-            if (val == "pk") p3->bwd_packed = 1;
-            if (val == "pkmagic") p3->bwd_packed = 2;
+            static const char *general[] = {"scalar", "pk", "pkmagic", "quad"};
+            static const char *runs[] = {"ax8m5", "ax8", "ax16", "ax16m4"};
+            for (int i = 0; i < 4; ++i) {
+                if (val == general[i]) p3->algo_bwd = 0, p3->bwd_packed = i;
+                if (val == runs[i]) p3->algo_bwd = 1, p3->bwd_axial = i;
+            }
         }
         if (p3 && key == "adj3d") {
             if (val == "pair") p3->adj_quad = 0;
@@ -341,6 +351,16 @@ int make_plan3d(cg_plan3d **out, int device, const uint64_t vol_shape[3], const 
     if ((rc = alloc_copy(&p->d_bdx, bx.data(), nangles))) return fail(rc);
     if ((rc = alloc_copy(&p->d_bdy, by.data(), nangles))) return fail(rc);
     if ((rc = alloc_copy(&p->d_bdz, bz.data(), nangles))) return fail(rc);
+    p->axial = true;
+    for (const float4 &d : by) p->axial = p->axial && d.x == 0.f && d.z == 0.f;
+    if (p->axial) {
+        p->ax_views.reserve(nangles * 10);
+        for (uint64_t i = 0; i < nangles; ++i) {
+            const float v[10] = {bo[i].x - p->bsrc[0], bo[i].y - p->bsrc[1], bo[i].z - p->bsrc[2],
+                                 bx[i].x, bx[i].y, bx[i].z, bz[i].x, bz[i].y, bz[i].z, by[i].y};
+            p->ax_views.insert(p->ax_views.end(), v, v + 10);
+        }
+    }
     *out = p.release();
     return CG_OK;
 }
@@ -709,8 +729,8 @@ int cg_plan3d_create(cg_plan3d **plan, int device, const uint64_t vol_shape[3],
 int cg_plan3d_set_algorithm(cg_plan3d *plan, int forward, int backward) {
     clear_error();
     CG_REQUIRE(plan, "plan is NULL");
-    CG_REQUIRE(forward >= -1 && forward <= 3, "3D forward algorithm must be -1..3");
-    CG_REQUIRE(backward >= -1 && backward <= 0, "3D backward algorithm must be -1..0");
+    CG_REQUIRE(forward >= -1 && forward <= 5, "3D forward algorithm must be -1..5");
+    CG_REQUIRE(backward >= -1 && backward <= 1, "3D backward algorithm must be -1..1");
     if (forward >= 0) plan->algo_fwd = forward;
     if (backward >= 0) plan->algo_bwd = backward;
     return CG_OK;
@@ -719,7 +739,7 @@ int cg_plan3d_set_algorithm(cg_plan3d *plan, int forward, int backward) {
 int cg_plan3d_get_algorithm(const cg_plan3d *plan, int *forward, int *backward) {
     clear_error();
     CG_REQUIRE(plan && forward && backward, "NULL argument");
-    *forward = plan->algo_fwd, *backward = plan->algo_bwd;
+    *forward = plan->algo_fwd, *backward = plan->runs_axial() ? 1 : 0;
     return CG_OK;
 }
 
@@ -741,6 +761,7 @@ int cg_forward_3d_plan(cg_plan3d *plan, const float *volume, float *sinogram, vo
     DeviceGuard guard(plan->device);
     CG_REQUIRE(guard.ok(), "cannot select the plan's device");
     if (plan->algo_fwd == 3) return launch_forward3d_slab(*plan, volume, sinogram, (cudaStream_t)stream);
+    if (plan->algo_fwd >= 4) return launch_forward3d_quad(*plan, volume, sinogram, (cudaStream_t)stream);
     if (plan->algo_fwd != 0) return launch_forward3d_tex(*plan, volume, sinogram, (cudaStream_t)stream);
     int rc = ensure_plan3d_scratch(*plan, true, false);
     if (rc) return rc;
@@ -789,6 +810,8 @@ int cg_forward_3d(const float *x, const uint64_t vol_shape[3], const float vol_s
     if (rc) return rc;
     if (p->algo_fwd == 3) {
         rc = launch_forward3d_slab(*p, x, sinogram, (cudaStream_t)stream);
+    } else if (p->algo_fwd >= 4) {
+        rc = launch_forward3d_quad(*p, x, sinogram, (cudaStream_t)stream);
     } else if (p->algo_fwd != 0) {
         rc = launch_forward3d_tex(*p, x, sinogram, (cudaStream_t)stream);
     } else {

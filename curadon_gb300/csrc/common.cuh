@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include "curadon_gb300.h"
 
@@ -151,6 +152,9 @@ struct Plan3d {
     float2 *d_volA = nullptr;         // (Z+2P)(Y+2P)(X+2P) pairs along x
     float2 *d_volB = nullptr;         // (X+2P)(Y+2P)(Z+2P) pairs along z
     float2 *d_sinoP = nullptr;        // nangles (V+2P)(U+2P) pairs along u
+    float4 *d_sinoQ = nullptr;        // quads of rows v, v+1 (backward 1; 0 variant 3)
+    float4 *d_volQA = nullptr;        // forward 4: quads, slices z (Z+kQP)(Y+kQP)(X+kQP)
+    float4 *d_volQB = nullptr;        // forward 4: quads, slices x (X+kQP)(Y+kQP)(Z+kQP)
     size_t volA_elems = 0, volB_elems = 0, sinoP_elems = 0;
     // matched adjoint: quad accumulators (float4 per padded voxel), on first
     // use; adj_quad -1 = when both fit in 96 MB (the L2 holds the atomics),
@@ -164,13 +168,30 @@ struct Plan3d {
     float *d_volT = nullptr;          // x<->z transposed volume for arrB
 
     // forward 0 = registers, 1 = tex3D, 2 = layered bilinear + lerp,
-    // 3 = shared-memory slabs;
+    // 3 = shared-memory slabs, 4 = quads (FP32 trilinear, two 16-byte loads
+    // per sample), 5 = quads with some warps on the texture unit; backward 0 = general voxel runs along z,
+    // 1 = runs along y when every view maps y onto the detector's v axis
+    // (`axial`; otherwise 0 runs);
     // defaults: the fastest measured on GB300 (256^3 and 512^3 workloads)
-    int algo_fwd = 1, algo_bwd = 0;
-    // backprojection: 2 = two voxels per packed FP32 instruction with the
-    // floor by FP32 adds (default, measured fastest), 1 = packed with the
-    // conversion unit's floor, 0 = one voxel at a time
-    int bwd_packed = 2;
+    int algo_fwd = 5, algo_bwd = 1;
+    // backward 0: 3 = two voxels per packed FP32 instruction with the floor
+    // by FP32 adds, each bilinear sample one 16-byte load of a row-pair quad
+    // (default; -9 % at 256^3 and 512^3 against 2), 2 = the same reading two
+    // 8-byte pairs, 1 = packed with the conversion unit's floor, 0 = one
+    // voxel at a time
+    int bwd_packed = 3;
+    // backward 1: 0 = runs of 8 voxels at <= 48 registers (default; -27 % at
+    // 256^3 and -29 % at 512^3 against backward 0), 1 = runs of 8 at <= 64,
+    // 2 / 3 = runs of 16 at <= 80 / 64
+    int bwd_axial = 0;
+    // forward 5: warps of each 8 that sample through the texture unit
+    int fwd_tex_warps = 3;
+    bool axial = false;  // every backward table's y step is (0, dy, 0)
+    // axial backprojection, per view: source -> voxel (0, 0, 0) (3), x step
+    // (3), z step (3), y step's v component (1)
+    std::vector<float> ax_views;
+    bool runs_axial() const { return algo_bwd == 1 && axial; }
+    bool reads_quads() const { return runs_axial() || bwd_packed == 3; }
     // texture forwards: detector cells (u, v) x views per thread block
     int fwd_bx = 8, fwd_by = 4, fwd_bz = 8;
 };
@@ -205,6 +226,7 @@ int launch_backward2d(const Plan2d &p, float *vol, cudaStream_t s);
 int ensure_plan3d_scratch(Plan3d &p, bool fwd, bool bwd);
 int launch_forward3d(const Plan3d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_forward3d_slab(Plan3d &p, const float *vol, float *sino, cudaStream_t s);
+int launch_forward3d_quad(Plan3d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s);
 
 int launch_adjoint2d(Plan2d &p, float *vol, const float *sino, cudaStream_t s);
@@ -222,6 +244,7 @@ int launch_forward2d_tex(Plan2d &p, const float *vol, float *sino, cudaStream_t 
 int launch_forward2d_hyb(Plan2d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t s);
 int launch_forward3d_tex(Plan3d &p, const float *vol, float *sino, cudaStream_t s);
+int upload_volume_texture3(Plan3d &p, const float *vol, cudaStream_t s);
 
 // Reads CURADON_GB300_ALGO ("fwd2d=tex,bwd2d=smem,fwd3d=tex2l,...") over the
 // defaults of a new plan.

@@ -12,12 +12,15 @@
 #include <cfloat>
 #include <climits>
 
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace cg {
 namespace {
 
 constexpr int kP3 = kPad;
+constexpr int kQP = 2 * kP3 + 1;  // quad copies: kP3 zero planes below, kP3 + 1 above
 
 // ------------------------------------------------------------ re-layouts
 
@@ -65,6 +68,62 @@ __global__ void __launch_bounds__(256)
     (void)PX;
 }
 
+// Quads of the volume for k_fwd3d_quad.  Element (c, b, a) holds, in slice
+// c, the values at rows b, b + 1 and columns a, a + 1 as A = v00,
+// B = v01 - v00, C = v10 - v00, D = (v11 - v10) - (v01 - v00) (first index
+// the row), so the bilinear value at fractions (wa, wb) is
+// A + wa B + wb (C + wa D).  Every axis is padded with kP3 zero planes below
+// and kP3 + 1 above (kQP in all), so the samples of a ray inside the box
+// [-1, N + 1]^3 and their slice c + 1 stay inside the array.
+// QA: slices z, rows y, columns x.
+__global__ void k_relayout3d_qa(const float *__restrict__ vol, int X, int Y, int Z,
+                                float4 *__restrict__ QA) {
+    const int PX = X + kQP, PY = Y + kQP, PZ = Z + kQP;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)PX * PY * PZ) return;
+    const int x = (int)(idx % PX) - kP3;
+    const long long r = idx / PX;
+    const int y = (int)(r % PY) - kP3;
+    const int z = (int)(r / PY) - kP3;
+    float v[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    if (z >= 0 && z < Z)
+        for (int i = 0; i < 2; ++i) {
+            if (y + i < 0 || y + i >= Y) continue;
+            const float *row = vol + ((size_t)z * Y + (y + i)) * X;
+            if (x >= 0 && x < X) v[i][0] = row[x];
+            if (x + 1 >= 0 && x + 1 < X) v[i][1] = row[x + 1];
+        }
+    const float b = v[0][1] - v[0][0];
+    QA[idx] = make_float4(v[0][0], b, v[1][0] - v[0][0], (v[1][1] - v[1][0]) - b);
+}
+
+// QB: slices x, rows y, columns z; an x <-> z transpose of the rows y, y + 1
+// through shared memory, 32 x 32 (x, z) tiles.
+__global__ void __launch_bounds__(256)
+    k_relayout3d_qb(const float *__restrict__ vol, int X, int Y, int Z, float4 *__restrict__ QB) {
+    __shared__ float tile[2][33][33];  // [row][z][x]
+    const int PX = X + kQP, PY = Y + kQP, PZ = Z + kQP;
+    const int a0 = blockIdx.x * 32, c0 = blockIdx.y * 32, b = blockIdx.z;
+    const int z0 = a0 - kP3, x0 = c0 - kP3, y = b - kP3;
+    for (int j = threadIdx.y; j < 33; j += blockDim.y)
+        for (int i = 0; i < 2; ++i) {
+            const int x = x0 + threadIdx.x, z = z0 + j, yy = y + i;
+            tile[i][j][threadIdx.x] = (x >= 0 && x < X && z >= 0 && z < Z && yy >= 0 && yy < Y)
+                                          ? vol[((size_t)z * Y + yy) * X + x]
+                                          : 0.f;
+        }
+    __syncthreads();
+    const int tz = threadIdx.x, a = a0 + tz;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int c = c0 + i;
+        if (c >= PX || a >= PZ) continue;
+        const float v00 = tile[0][tz][i], v01 = tile[0][tz + 1][i];
+        const float v10 = tile[1][tz][i], v11 = tile[1][tz + 1][i];
+        const float bb = v01 - v00;
+        QB[((size_t)c * PY + b) * PZ + a] = make_float4(v00, bb, v10 - v00, (v11 - v10) - bb);
+    }
+}
+
 __global__ void k_relayout_sino3d(const float *__restrict__ sino, int U, int V, int nangles,
                                   float2 *__restrict__ S) {
     const int PU = U + 2 * kP3, PV = V + 2 * kP3;
@@ -81,6 +140,52 @@ __global__ void k_relayout_sino3d(const float *__restrict__ sino, int U, int V, 
         if (a + 1 >= 0 && a + 1 < U) t1 = row[a + 1];
     }
     S[idx] = make_float2(t0, t1 - t0);
+}
+
+// The same layout with rows b and b + 1 in one float4 (pair of row b, pair
+// of row b + 1), so a bilinear sample is one 16-byte load.
+__global__ void k_relayout_sino3d_quad(const float *__restrict__ sino, int U, int V, int nangles,
+                                       float4 *__restrict__ S) {
+    const int PU = U + 2 * kP3, PV = V + 2 * kP3;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)PU * PV * nangles) return;
+    const int a = (int)(idx % PU) - kP3;
+    const long long r = idx / PU;
+    const int b = (int)(r % PV) - kP3;
+    const int view = (int)(r / PV);
+    float t[4] = {0.f, 0.f, 0.f, 0.f};  // (row b: a, a + 1), (row b + 1: a, a + 1)
+    for (int k = 0; k < 2; ++k) {
+        const int bb = b + k;
+        if (bb < 0 || bb >= V) continue;
+        const float *row = sino + ((size_t)view * V + bb) * U;
+        if (a >= 0 && a < U) t[2 * k] = row[a];
+        if (a + 1 >= 0 && a + 1 < U) t[2 * k + 1] = row[a + 1];
+    }
+    S[idx] = make_float4(t[0], t[1] - t[0], t[2], t[3] - t[2]);
+}
+
+// Double-difference quads for the axial backprojector: element (b, a) holds
+// s00, s01 - s00, s10 - s00 and (s11 - s10) - (s01 - s00) of the cells
+// (row b, b + 1) x (column a, a + 1), zero outside the detector, so the
+// bilinear value at fractions (wu, wv) is s00 + wu B + wv (C + wu D).
+__global__ void k_relayout_sino3d_qd(const float *__restrict__ sino, int U, int V, int nangles,
+                                     float4 *__restrict__ S) {
+    const int PU = U + 2 * kP3, PV = V + 2 * kP3;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)PU * PV * nangles) return;
+    const int a = (int)(idx % PU) - kP3;
+    const long long r = idx / PU;
+    const int b = (int)(r % PV) - kP3;
+    const int view = (int)(r / PV);
+    float t[4] = {0.f, 0.f, 0.f, 0.f};  // s00, s01, s10, s11
+    for (int k = 0; k < 2; ++k) {
+        const int bb = b + k;
+        if (bb < 0 || bb >= V) continue;
+        const float *row = sino + ((size_t)view * V + bb) * U;
+        if (a >= 0 && a < U) t[2 * k] = row[a];
+        if (a + 1 >= 0 && a + 1 < U) t[2 * k + 1] = row[a + 1];
+    }
+    S[idx] = make_float4(t[0], t[1] - t[0], t[2] - t[0], (t[3] - t[2]) - (t[1] - t[0]));
 }
 
 // ------------------------------------------------------------ forward
@@ -217,6 +322,84 @@ __device__ __forceinline__ Ray3 setup_ray3(const float4 o, const float4 du, cons
     r.h = r.hit ? (tmax - tmin) / (float)r.nsteps : 0.f;
     if (!(r.h > 0.f) || !isfinite(tmax) || r.nsteps > (1 << 22)) r.hit = false;
     return r;
+}
+
+// FP32 forward from the quad copies.  The reference's ray set-up and float
+// t-loop (forward_3d.hpp:56-93), each sample trilinear in FP32: the floors
+// by FP32 adds rounded toward -inf (bits of p + 1.5 * 2^23 = floor(p) +
+// const), one offset for the three axes, two 16-byte loads (slices c and
+// c + 1) and eight FMAs.  Rays that travel mostly along x read QB (columns
+// z, slices x), the others QA, so that the warp's rays -- an 8 x 4 patch of
+// detector cells -- spread along the contiguous axis.  Blocks are 32 x 8
+// cells of one view, ordered cells fastest, then views, then bands of 8
+// detector rows: the blocks resident at one time cover one band of rows of
+// many views, whose rays cross a slab of the volume's y range that stays in
+// L2.  The offset is clamped into the array (a guard; samples inside the box
+// need no clamp).  With tex_warps > 0 (algorithm 5) the first tex_warps
+// warps of each block take their rays through the texture unit instead
+// (the reference's tex3D sampling): the texture path and the L1 load path
+// then work side by side (3 of 8 warps: -8 % at 256^3, -21 % at 512^3
+// against quads alone).
+__global__ void __launch_bounds__(256)
+    k_fwd3d_quad(const float4 *__restrict__ QA, const float4 *__restrict__ QB,
+                 float *__restrict__ sino, const float4 *__restrict__ torg,
+                 const float4 *__restrict__ tdu, const float4 *__restrict__ tdv,
+                 const float4 *__restrict__ tsrc, int X, int Y, int Z, int U, int V, int P,
+                 int utiles, cudaTextureObject_t tex, int tex_warps) {
+    const int lin = blockIdx.x;
+    const int ut = lin % utiles, rest = lin / utiles;
+    const int view = rest % P, band = rest / P;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int iu = ut * 32 + (warp & 3) * 8 + (lane & 7);
+    const int iv = band * 8 + (warp >> 2) * 4 + (lane >> 3);
+    if (iu >= U || iv >= V) return;
+    const Ray3 r = setup_ray3(torg[view], tdu[view], tdv[view], tsrc[view], iu, iv, X, Y, Z);
+    if (!r.hit) return;
+    if (warp < tex_warps) {
+        // this warp's rays through the texture unit (trilinear, 8-bit weights)
+        float acc = 0.f, t = r.tmin;
+        for (int k = 0; k <= r.nsteps + 1; ++k) {
+            if (!(t <= r.tmax)) break;
+            acc += tex3D<float>(tex, fmaf(r.dx, t, r.sx) + 0.5f, fmaf(r.dy, t, r.sy) + 0.5f,
+                                fmaf(r.dz, t, r.sz) + 0.5f);
+            t += r.h;
+        }
+        sino[((size_t)view * V + iv) * U + iu] = acc;
+        return;
+    }
+    const bool xmajor = fabsf(r.dx) > fabsf(r.dz);
+    const float4 *Q = xmajor ? QB : QA;
+    const float sa = xmajor ? r.sz : r.sx, da = xmajor ? r.dz : r.dx;
+    const float sc = xmajor ? r.sx : r.sz, dc = xmajor ? r.dx : r.dz;
+    const unsigned PA = (unsigned)((xmajor ? Z : X) + kQP), PB = (unsigned)(Y + kQP);
+    const unsigned PC = (unsigned)((xmajor ? X : Z) + kQP);
+    const unsigned slice = PA * PB;
+    const unsigned maxoff = (PC - 1) * slice - 1;  // off + slice stays inside
+    constexpr float kMagic = 12582912.0f;          // 1.5 * 2^23
+    const unsigned base = 0x4B400000u - (unsigned)kP3;
+    // off = (bits_c - base) slice + (bits_b - base) PA + (bits_a - base), mod 2^32
+    const unsigned K = base * slice + base * PA + base;
+    const float4 *Q1 = Q + slice;
+    float acc = 0.f, t = r.tmin;
+    for (int k = 0; k <= r.nsteps + 1; ++k) {
+        if (!(t <= r.tmax)) break;
+        const float pa = fmaf(da, t, sa), pb = fmaf(r.dy, t, r.sy), pc = fmaf(dc, t, sc);
+        const float ta = __fadd_rd(pa, kMagic), tb = __fadd_rd(pb, kMagic),
+                    tc = __fadd_rd(pc, kMagic);
+        const float wa = __fadd_rn(pa, -__fadd_rn(ta, -kMagic));
+        const float wb = __fadd_rn(pb, -__fadd_rn(tb, -kMagic));
+        const float wc = __fadd_rn(pc, -__fadd_rn(tc, -kMagic));
+        unsigned off = __float_as_uint(tc) * slice + __float_as_uint(tb) * PA +
+                       (__float_as_uint(ta) - K);
+        off = min(off, maxoff);
+        const float4 q0 = __ldg(Q + off), q1 = __ldg(Q1 + off);
+        const float l0 = fmaf(wa, q0.y, q0.x), g0 = fmaf(wa, q0.w, q0.z);
+        const float l1 = fmaf(wa, q1.y, q1.x), g1 = fmaf(wa, q1.w, q1.z);
+        const float m0 = fmaf(wb, g0, l0), m1 = fmaf(wb, g1, l1);
+        acc += fmaf(wc, m1 - m0, m0);
+        t += r.h;
+    }
+    sino[((size_t)view * V + iv) * U + iu] = acc;
 }
 
 // Chunked slab forward.  Block = kS3G views x (32 x 8 detector cells) x ray
@@ -464,14 +647,16 @@ struct BwdTab {
 // stepped along z from the run's first voxel -- then a bilinear sample of the
 // difference-encoded pair-packed projection in two 8-byte loads and three
 // FMAs, accumulated in registers; the volume is read and written once.
-template <bool PK, bool MAGIC = false>
+template <bool PK, bool MAGIC = false, bool QS = false>
 __global__ void __launch_bounds__(256)
-    k_bwd3d(float *__restrict__ vol, const float2 *__restrict__ S,
+    k_bwd3d(float *__restrict__ vol, const void *__restrict__ Sv,
             const float4 *__restrict__ torg, const float4 *__restrict__ tdx,
             const float4 *__restrict__ tdy, const float4 *__restrict__ tdz, float srcx,
             float srcy, float srcz, float zplane, float hu, float hv, int X, int Y, int Z, int U,
             int V, int nangles, int tiles_x, int tiles_y, int tiles_z) {
     __shared__ BwdTab stab[kBViews];
+    const float2 *S = static_cast<const float2 *>(Sv);
+    const float4 *SQ = static_cast<const float4 *>(Sv);  // QS: row-pair quads
     // brick-ordered tile index
     constexpr int BX = 2, BY = 8, BZ = 8;
     const int bricks_x = (tiles_x + BX - 1) / BX, bricks_y = (tiles_y + BY - 1) / BY;
@@ -512,6 +697,7 @@ __global__ void __launch_bounds__(256)
             float diry = fmaf(fz0, tb.dz.y, fmaf(fy, tb.dy.y, fmaf(fx, tb.dx.y, tb.o.y))) - srcy;
             float dirz = fmaf(fz0, tb.dz.z, fmaf(fy, tb.dy.z, fmaf(fx, tb.dx.z, tb.o.z))) - srcz;
             const float2 *plane = S + (size_t)(v0 + j) * PU * PV;
+            const float4 *planeQ = SQ + (size_t)(v0 + j) * PU * PV;
             if constexpr (PK) {
                 // two voxels (k, k + 1) per packed FP32 instruction
                 const float2 step_x = make_float2(2.f * tb.dz.x, 2.f * tb.dz.x);
@@ -552,10 +738,18 @@ __global__ void __launch_bounds__(256)
                         cu0 = min((unsigned)(iu0 + kP3), ucap), cu1 = min((unsigned)(iu1 + kP3), ucap);
                         cv0 = min((unsigned)(iv0 + kP3), vcap), cv1 = min((unsigned)(iv1 + kP3), vcap);
                     }
-                    const float2 *q0 = plane + cv0 * PU + cu0;
-                    const float2 *q1 = plane + cv1 * PU + cu1;
-                    const float2 a0 = __ldg(q0), b0 = __ldg(q0 + PU);
-                    const float2 a1 = __ldg(q1), b1 = __ldg(q1 + PU);
+                    float2 a0, b0, a1, b1;
+                    if constexpr (QS) {
+                        const float4 w0 = __ldg(planeQ + cv0 * PU + cu0);
+                        const float4 w1 = __ldg(planeQ + cv1 * PU + cu1);
+                        a0 = make_float2(w0.x, w0.y), b0 = make_float2(w0.z, w0.w);
+                        a1 = make_float2(w1.x, w1.y), b1 = make_float2(w1.z, w1.w);
+                    } else {
+                        const float2 *q0 = plane + cv0 * PU + cu0;
+                        const float2 *q1 = plane + cv1 * PU + cu1;
+                        a0 = __ldg(q0), b0 = __ldg(q0 + PU);
+                        a1 = __ldg(q1), b1 = __ldg(q1 + PU);
+                    }
                     const float2 l0 = make_float2(fmaf(wu.x, a0.y, a0.x), fmaf(wu.y, a1.y, a1.x));
                     const float2 l1 = make_float2(fmaf(wu.x, b0.y, b0.x), fmaf(wu.y, b1.y, b1.x));
                     const float2 m =
@@ -566,24 +760,24 @@ __global__ void __launch_bounds__(256)
                     DY = __fadd2_rn(DY, step_y);
                     DZ = __fadd2_rn(DZ, step_z);
                 }
-                continue;
-            }
+            } else {
 #pragma unroll
-            for (int k = 0; k < kBZ; ++k) {
-                const float t = __fdividef(num, dirz);
-                const float ub = fmaf(dirx, t, su), vb = fmaf(diry, t, sv);
-                const int iu = __float2int_rd(ub), iv = __float2int_rd(vb);
-                const float wu = ub - (float)iu, wv = vb - (float)iv;
-                const unsigned cu = min((unsigned)(iu + kP3), ucap);
-                const unsigned cv = min((unsigned)(iv + kP3), vcap);
-                const float2 *q = plane + cv * PU + cu;
-                const float2 a = __ldg(q), b = __ldg(q + PU);
-                const float l0 = fmaf(wu, a.y, a.x);
-                const float l1 = fmaf(wu, b.y, b.x);
-                acc[k] += fmaf(wv, l1 - l0, l0);
-                dirx += tb.dz.x;
-                diry += tb.dz.y;
-                dirz += tb.dz.z;
+                for (int k = 0; k < kBZ; ++k) {
+                    const float t = __fdividef(num, dirz);
+                    const float ub = fmaf(dirx, t, su), vb = fmaf(diry, t, sv);
+                    const int iu = __float2int_rd(ub), iv = __float2int_rd(vb);
+                    const float wu = ub - (float)iu, wv = vb - (float)iv;
+                    const unsigned cu = min((unsigned)(iu + kP3), ucap);
+                    const unsigned cv = min((unsigned)(iv + kP3), vcap);
+                    const float2 *q = plane + cv * PU + cu;
+                    const float2 a = __ldg(q), b = __ldg(q + PU);
+                    const float l0 = fmaf(wu, a.y, a.x);
+                    const float l1 = fmaf(wu, b.y, b.x);
+                    acc[k] += fmaf(wv, l1 - l0, l0);
+                    dirx += tb.dz.x;
+                    diry += tb.dz.y;
+                    dirz += tb.dz.z;
+                }
             }
         }
     }
@@ -592,6 +786,105 @@ __global__ void __launch_bounds__(256)
     for (int k = 0; k < kBZ; ++k) {
         const int z = z0 + k;
         if (z < Z) vol[((size_t)z * Y + y) * X + x] += acc[k];
+    }
+}
+
+// Views per launch of k_bwd3d_ax: their tables travel as a 30 KB kernel
+// parameter (the limit is 32 KB).
+constexpr int kAxViews = 768;
+struct AxViewParams {
+    float4 p0[kAxViews];  // source -> voxel (0, 0, 0): x, y, z; v component of the y step
+    float4 p1[kAxViews];  // x step; z step's x
+    float2 p2[kAxViews];  // z step's y, z
+};
+
+// Backprojection for geometries whose every view maps the volume's y axis
+// onto the detector's v axis (the y step of the view table is (0, dy, 0)):
+// circular orbits about y without detector tilt.  Along a run of voxels in
+// y the ray's detector-normal and u components are then constant, so a
+// thread takes RUN voxels along y with one reciprocal, one u floor and one
+// detector column per view, and per voxel only the v coordinate: the floor
+// by an FP32 add rounded toward -inf (the magic 1.5 * 2^23 has unit
+// spacing, so the sum's bits are floor(v) + const exactly), one 16-byte
+// load of a double-difference quad and three FMAs.  Block = 256 threads
+// over 32 (x) x 8 (z) voxels, each warp on an 8 x 4 patch so its lanes read
+// a compact piece of the projection; blocks are visited in bricks of 2 x 8
+// x 8 tiles like k_bwd3d.  The per-view tables are a kernel parameter, read
+// through the constant cache uniformly across the warp: no shared-memory
+// staging or barriers, and the table reads stay off the L1's register
+// write-back path, which the projection loads saturate (-9 % against
+// staging them in shared memory).  Same ray/plane intersection as the
+// reference (backward_3d.hpp:78-94).
+template <int RUN, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+    k_bwd3d_ax(float *__restrict__ vol, const float4 *__restrict__ SQ,
+                const __grid_constant__ AxViewParams tab, int nv, float num, float su, float sv,
+                int X, int Y, int Z, int U, int V, int tiles_x, int tiles_y, int tiles_z) {
+    constexpr int BX = 2, BY = 8, BZ = 8;
+    const int bricks_x = (tiles_x + BX - 1) / BX, bricks_y = (tiles_y + BY - 1) / BY;
+    const int lin = blockIdx.x;
+    const int brick = lin / (BX * BY * BZ), in = lin % (BX * BY * BZ);
+    const int bx = brick % bricks_x, by = (brick / bricks_x) % bricks_y,
+              bz = brick / (bricks_x * bricks_y);
+    const int tx_ = bx * BX + in % BX, ty_ = by * BY + (in / BX) % BY, tz_ = bz * BZ + in / (BX * BY);
+    if (tx_ >= tiles_x || ty_ >= tiles_y || tz_ >= tiles_z) return;
+
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int x = tx_ * 32 + (warp & 3) * 8 + (lane & 7);
+    const int z = tz_ * 8 + (warp >> 2) * 4 + (lane >> 3);
+    const int y0 = ty_ * RUN;
+    const float fx = (float)x, fz = (float)z, fy0 = (float)y0;
+    const int PU = U + 2 * kP3, PV = V + 2 * kP3;
+    const size_t plane_elems = (size_t)PU * PV;
+    const unsigned rowb = (unsigned)PU * (unsigned)sizeof(float4);
+    const unsigned ucap = (unsigned)(U + kP3), vcap = (unsigned)(V + kP3);
+    const unsigned base = 0x4B400000u - (unsigned)kP3;  // bits of 1.5 * 2^23 - kP3
+    constexpr float kMagic = 12582912.0f;              // 1.5 * 2^23
+    const float2 M2 = make_float2(kMagic, kMagic), NEG1 = make_float2(-1.f, -1.f);
+
+    float acc[RUN];
+#pragma unroll
+    for (int k = 0; k < RUN; ++k) acc[k] = 0.f;
+
+    const float4 *plane = SQ;
+    for (int j = 0; j < nv; ++j, plane += plane_elems) {
+        const float4 p0 = tab.p0[j], p1 = tab.p1[j];
+        const float2 p2 = tab.p2[j];
+        const float dirx = fmaf(fz, p1.w, fmaf(fx, p1.x, p0.x));
+        const float diry = fmaf(fy0, p0.w, fmaf(fz, p2.x, fmaf(fx, p1.y, p0.y)));
+        const float dirz = fmaf(fz, p2.y, fmaf(fx, p1.z, p0.z));
+        const float t = __fdividef(num, dirz);
+        const float ub = fmaf(dirx, t, su);
+        const float vb0 = fmaf(diry, t, sv), dvb = p0.w * t;
+        const float tu = __fadd_rd(ub, kMagic);
+        const float wu = __fadd_rn(ub, -__fadd_rn(tu, -kMagic));
+        const unsigned cu = min(__float_as_uint(tu) - base, ucap);
+        const float4 *col = plane + cu;
+        float2 vb = make_float2(vb0, vb0 + dvb);
+        const float2 step = make_float2(2.f * dvb, 2.f * dvb);
+#pragma unroll
+        for (int k = 0; k < RUN; k += 2) {
+            const float2 tv = __fadd2_rd(vb, M2);
+            const float2 wv = __fadd2_rn(vb, __ffma2_rn(tv, NEG1, M2));  // vb - floor(vb)
+            const unsigned c0 = min(__float_as_uint(tv.x) - base, vcap);
+            const unsigned c1 = min(__float_as_uint(tv.y) - base, vcap);
+            const float4 q0 = __ldg(reinterpret_cast<const float4 *>(
+                reinterpret_cast<const char *>(col) + (size_t)c0 * rowb));
+            const float4 q1 = __ldg(reinterpret_cast<const float4 *>(
+                reinterpret_cast<const char *>(col) + (size_t)c1 * rowb));
+            const float2 l0 = make_float2(fmaf(wu, q0.y, q0.x), fmaf(wu, q1.y, q1.x));
+            const float2 g = make_float2(fmaf(wu, q0.w, q0.z), fmaf(wu, q1.w, q1.z));
+            const float2 a = __ffma2_rn(wv, g, __fadd2_rn(make_float2(acc[k], acc[k + 1]), l0));
+            acc[k] = a.x, acc[k + 1] = a.y;
+            vb = __fadd2_rn(vb, step);
+        }
+    }
+    if (x >= X || z >= Z) return;
+#pragma unroll
+    for (int k = 0; k < RUN; ++k) {
+        const int y = y0 + k;
+        if (y < Y) vol[((size_t)z * Y + y) * X + x] += acc[k];
     }
 }
 
@@ -606,10 +899,14 @@ int ensure_plan3d_scratch(Plan3d &p, bool fwd, bool bwd) {
         CG_TRY_CUDA(cudaMalloc(&p.d_volB, n * sizeof(float2)));
         p.volA_elems = p.volB_elems = n;
     }
-    if (bwd && !p.d_sinoP) {
+    if (bwd) {
+        // one of the two re-laid projections, as the plan's variant reads it
         const size_t n = (size_t)(p.U + 2 * kP3) * (p.V + 2 * kP3) * p.nangles;
-        CG_TRY_CUDA(cudaMalloc(&p.d_sinoP, n * sizeof(float2)));
         p.sinoP_elems = n;
+        const bool quads = p.reads_quads();
+        if (quads && !p.d_sinoQ) CG_TRY_CUDA(cudaMalloc(&p.d_sinoQ, n * sizeof(float4)));
+        if (!quads && !p.d_sinoP)
+            CG_TRY_CUDA(cudaMalloc(&p.d_sinoP, n * sizeof(float2)));
     }
     return CG_OK;
 }
@@ -627,6 +924,36 @@ int launch_forward3d(const Plan3d &p, const float *vol, float *sino, cudaStream_
     dim3 grid(ceil_div(p.U, 32), ceil_div(p.V, 8), p.nangles);
     k_fwd3d<<<grid, dim3(32, 8), 0, s>>>(p.d_volA, p.d_volB, sino, p.d_forg, p.d_fdu, p.d_fdv,
                                          p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
+int launch_forward3d_quad(Plan3d &p, const float *vol, float *sino, cudaStream_t s) {
+    const size_t n = (size_t)(p.X + kQP) * (p.Y + kQP) * (p.Z + kQP);
+    if (n >= (1ull << 32)) return set_error(CG_ERR_INVALID, "volume too large for forward 4");
+    if (!p.d_volQA) {
+        CG_TRY_CUDA(cudaMalloc(&p.d_volQA, n * sizeof(float4)));
+        CG_TRY_CUDA(cudaMalloc(&p.d_volQB, n * sizeof(float4)));
+    }
+    k_relayout3d_qa<<<ceil_div((long long)n, 256), 256, 0, s>>>(vol, p.X, p.Y, p.Z, p.d_volQA);
+    CG_TRY_CUDA(cudaGetLastError());
+    dim3 g(ceil_div(p.Z + kQP, 32), ceil_div(p.X + kQP, 32), p.Y + kQP);
+    k_relayout3d_qb<<<g, dim3(32, 8), 0, s>>>(vol, p.X, p.Y, p.Z, p.d_volQB);
+    CG_TRY_CUDA(cudaGetLastError());
+    const int utiles = ceil_div(p.U, 32);
+    const long long blocks = (long long)utiles * p.nangles * ceil_div(p.V, 8);
+    if (blocks >= (1ll << 31)) return set_error(CG_ERR_INVALID, "too many rays for one launch");
+    // algorithm 5: some warps of each block sample through the texture unit
+    const int tex_warps = p.algo_fwd == 5 ? p.fwd_tex_warps : 0;
+    cudaTextureObject_t tex = 0;
+    if (tex_warps > 0) {
+        int rc = upload_volume_texture3(p, vol, s);
+        if (rc) return rc;
+        tex = p.tex3;
+    }
+    k_fwd3d_quad<<<(unsigned)blocks, 256, 0, s>>>(p.d_volQA, p.d_volQB, sino, p.d_forg, p.d_fdu,
+                                                  p.d_fdv, p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V,
+                                                  p.nangles, utiles, tex, tex_warps);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }
@@ -655,21 +982,61 @@ int launch_forward3d_slab(Plan3d &p, const float *vol, float *sino, cudaStream_t
 }
 
 int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s) {
+    const float zplane = p.DSO - p.DSD;
+    const float hu = (float)(p.U / 2), hv = (float)(p.V / 2);
+    if (p.runs_axial()) {
+        const long long n = (long long)p.sinoP_elems;
+        k_relayout_sino3d_qd<<<ceil_div(n, 256), 256, 0, s>>>(sino, p.U, p.V, p.nangles,
+                                                              p.d_sinoQ);
+        CG_TRY_CUDA(cudaGetLastError());
+        const int run = p.bwd_axial == 2 || p.bwd_axial == 3 ? 16 : 8;
+        const int tiles_x = ceil_div(p.X, 32), tiles_y = ceil_div(p.Y, run),
+                  tiles_z = ceil_div(p.Z, 8);
+        const int bricks = ceil_div(tiles_x, 2) * ceil_div(tiles_y, 8) * ceil_div(tiles_z, 8);
+        const size_t plane = (size_t)(p.U + 2 * kP3) * (p.V + 2 * kP3);
+        auto kernel = p.bwd_axial == 0   ? k_bwd3d_ax<8, 5>
+                      : p.bwd_axial == 1 ? k_bwd3d_ax<8, 4>
+                      : p.bwd_axial == 2 ? k_bwd3d_ax<16, 3>
+                                         : k_bwd3d_ax<16, 4>;
+        // the view tables travel as a kernel parameter, kAxViews per launch
+        AxViewParams tab{};
+        for (int c0 = 0; c0 < p.nangles; c0 += kAxViews) {
+            const int nv = std::min(kAxViews, p.nangles - c0);
+            for (int j = 0; j < nv; ++j) {
+                const float *a = p.ax_views.data() + (size_t)(c0 + j) * 10;
+                tab.p0[j] = make_float4(a[0], a[1], a[2], a[9]);
+                tab.p1[j] = make_float4(a[3], a[4], a[5], a[6]);
+                tab.p2[j] = make_float2(a[7], a[8]);
+            }
+            kernel<<<bricks * 128, 256, 0, s>>>(vol, p.d_sinoQ + plane * c0, tab, nv,
+                                                zplane - p.bsrc[2], p.bsrc[0] + hu - 0.5f,
+                                                p.bsrc[1] + hv - 0.5f, p.X, p.Y, p.Z, p.U, p.V,
+                                                tiles_x, tiles_y, tiles_z);
+            CG_TRY_CUDA(cudaGetLastError());
+        }
+        return CG_OK;
+    }
+    const bool quad = p.bwd_packed == 3;
     {
         const long long n = (long long)p.sinoP_elems;
-        k_relayout_sino3d<<<ceil_div(n, 256), 256, 0, s>>>(sino, p.U, p.V, p.nangles, p.d_sinoP);
+        if (quad) {
+            k_relayout_sino3d_quad<<<ceil_div(n, 256), 256, 0, s>>>(sino, p.U, p.V, p.nangles,
+                                                                    p.d_sinoQ);
+        } else {
+            k_relayout_sino3d<<<ceil_div(n, 256), 256, 0, s>>>(sino, p.U, p.V, p.nangles,
+                                                               p.d_sinoP);
+        }
         CG_TRY_CUDA(cudaGetLastError());
     }
     const int tiles_x = ceil_div(p.X, 32), tiles_y = ceil_div(p.Y, 8), tiles_z = ceil_div(p.Z, kBZ);
     const int bricks = ceil_div(tiles_x, 2) * ceil_div(tiles_y, 8) * ceil_div(tiles_z, 8);
-    const float zplane = p.DSO - p.DSD;
-    const float hu = (float)(p.U / 2), hv = (float)(p.V / 2);
-    auto kernel = p.bwd_packed == 2 ? k_bwd3d<true, true>
+    auto kernel = quad                ? k_bwd3d<true, true, true>
+                  : p.bwd_packed == 2 ? k_bwd3d<true, true>
                   : p.bwd_packed      ? k_bwd3d<true, false>
                                       : k_bwd3d<false, false>;
     kernel<<<bricks * 128, dim3(32, 8), 0, s>>>(
-        vol, p.d_sinoP, p.d_borg, p.d_bdx, p.d_bdy, p.d_bdz, p.bsrc[0], p.bsrc[1], p.bsrc[2],
-        zplane, hu, hv, p.X, p.Y, p.Z, p.U, p.V, p.nangles, tiles_x, tiles_y, tiles_z);
+        vol, quad ? (const void *)p.d_sinoQ : (const void *)p.d_sinoP, p.d_borg, p.d_bdx,
+        p.d_bdy, p.d_bdz, p.bsrc[0], p.bsrc[1], p.bsrc[2], zplane, hu, hv, p.X, p.Y, p.Z, p.U, p.V, p.nangles, tiles_x, tiles_y, tiles_z);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }

@@ -424,6 +424,15 @@ int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t
     return CG_OK;
 }
 
+int upload_volume_texture3(Plan3d &p, const float *vol, cudaStream_t s) {
+    if (!p.arr3) {
+        int rc = alloc_array(&p.arr3, p.X, p.Y, p.Z, cudaArrayDefault);
+        if (rc) return rc;
+        if ((rc = make_texture(p.arr3, &p.tex3))) return rc;
+    }
+    return copy_to_array(p.arr3, vol, p.X, p.Y, p.Z, s);
+}
+
 int launch_forward3d_tex(Plan3d &p, const float *vol, float *sino, cudaStream_t s) {
     const dim3 block(p.fwd_bx, p.fwd_by, p.fwd_bz);
     const dim3 grid(ceil_div(p.U, p.fwd_bx), ceil_div(p.V, p.fwd_by), ceil_div(p.nangles, p.fwd_bz));

@@ -85,7 +85,7 @@ def request_bytes(req: Request) -> int:
     scratch and iterates), an upper estimate."""
     g = req.geom
     nv, ns = _numel(g.vol_shape), _numel(g.sinogram_shape())
-    plan = 2 * 8 * _numel([int(v) + 4 for v in g.vol_shape]) + 8 * ns + 4 * nv
+    plan = 2 * 8 * _numel([int(v) + 4 for v in g.vol_shape]) + 16 * ns + 4 * nv
     work = {"fbp": 2 * ns + nv, "sirt": 3 * nv + 3 * ns, "cgls": 3 * nv + 2 * ns}[req.kind]
     return 4 * (ns + nv + work) + plan
 

@@ -167,9 +167,14 @@ int cg_plan3d_destroy(cg_plan3d *plan);
 /* Algorithm of each 3D operator; -1 leaves one unchanged.
  *   forward:  0 registers (FP32 trilinear from pair-packed copies),
  *             1 texture unit (tex3D), 2 texture unit bilinear per layer +
- *             FP32 lerp across layers, 3 shared-memory slabs (FP32)
- *   backward: 0 registers
- * cg_adjoint_3d_plan is the transpose of forward algorithms 0 and 3 (the
+ *             FP32 lerp across layers, 3 shared-memory slabs (FP32),
+ *             4 quads (FP32 trilinear, two 16-byte loads per sample),
+ *             5 quads with 3 of every 8 warps on the texture unit (default)
+ *   backward: 0 registers (voxel runs along z), 1 runs along y when every
+ *             view maps the volume's y axis onto the detector's v axis
+ *             (circular orbits without detector tilt; default), else 0.
+ * cg_plan3d_get_algorithm reports the backward algorithm that runs.
+ * cg_adjoint_3d_plan is the transpose of forward algorithms 0, 3 and 4 (the
  * same samples and trilinear weights, up to FP32 rounding). */
 int cg_plan3d_set_algorithm(cg_plan3d *plan, int forward, int backward);
 int cg_plan3d_get_algorithm(const cg_plan3d *plan, int *forward, int *backward);

@@ -105,9 +105,9 @@ def test_dot_product_2d_per_forward_algorithm(cuda_device, algo):
     assert dot_test(geom, x, y, cuda_device) < 1e-5
 
 
-@pytest.mark.parametrize("algo", ["registers", "slab"])
+@pytest.mark.parametrize("algo", ["registers", "slab", "quad"])
 def test_dot_product_3d_per_forward_algorithm(cuda_device, algo):
-    """The FP32-weight 3D forwards (registers, slab) share the adjoint."""
+    """The FP32-weight 3D forwards (registers, slab, quad) share the adjoint."""
     g = cone_config(40, 36, 64)
     geom = ConeGeometry(**g)
     geom.exact_plan.set_algorithm(forward=algo)
