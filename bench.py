@@ -43,8 +43,10 @@ NCU_TRAFFIC = {
     ("fan2048", "k_fwd2d_cslab"): 80_521_088,  # profiles/dram_fan2048.md
     ("fan2048", "k_bwd2d_smem"): 62_423_552,
     ("fan2048", "k_fwd2d_tex"): 17_007_744,    # the texture-unit forward (algorithm 1)
-    ("cone256", "k_fwd3d_tex3"): 172_266_542,  # profiles/k_bwd3d_cone256.md
-    ("cone256", "k_bwd3d"): 51_088_249,
+    ("cone256", "k_fwd3d_quad"): 2_015_147_008,  # profiles/k_fwd3d_quad_cone256.md (algorithm 5)
+    ("cone256", "k_bwd3d_ax"): 500_470_784,      # profiles/k_bwd3d_ax_cone256.md
+    ("cone256", "k_fwd3d_tex3"): 1_281_753_856,  # profiles/k_bwd3d_cone256.md
+    ("cone256", "k_bwd3d"): 504_137_984,
 }
 
 # Main kernel of each operator by the plan's algorithm name.
