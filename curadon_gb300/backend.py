@@ -42,8 +42,8 @@ def _stream(t: torch.Tensor) -> C.c_void_p:
     return C.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
 
 
-FORWARD_2D = ("registers", "texture", "hybrid", "slab", "chunked")
-BACKWARD_2D = ("registers", "texture", "shared")
+FORWARD_2D = ("registers", "texture", "hybrid", "slab", "chunked", "split")
+BACKWARD_2D = ("registers", "texture", "shared", "split")
 FORWARD_3D = ("registers", "texture", "layered", "slab", "quad", "mixed")
 BACKWARD_3D = ("registers", "axial")
 

@@ -36,6 +36,9 @@ void free_plan2d(Plan2d *p) {
     if (p->tex_sino) cudaDestroyTextureObject(p->tex_sino);
     if (p->arr_vol) cudaFreeArray(p->arr_vol);
     if (p->arr_sino) cudaFreeArray(p->arr_sino);
+    if (p->aux) cudaStreamDestroy(p->aux);
+    if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+    if (p->ev_join) cudaEventDestroy(p->ev_join);
     void *ptrs[] = {p->d_angles, p->d_DSO,   p->d_DSD,   p->d_src,   p->d_u0,    p->d_du,
                     p->d_bmeta,  p->d_bproj, p->d_layA,  p->d_layB,  p->d_sinoP, p->d_vol32,
                     p->d_sino32, p->d_quadA, p->d_quadB};
@@ -60,7 +63,8 @@ void free_plan3d(Plan3d *p) {
 // Overrides of a new plan's algorithms for measurement and testing, read
 // from CURADON_GB300_ALGO: comma-separated key=value tokens, e.g.
 // "fwd2d=tex,bwd2d_minb=4".  Keys: fwd2d = alu | tex | slab | cslab |
-// cslab<shape> | hyb<1..7>; bwd2d = alu | tex | smem; bwd2d_minb = 3 | 4 | 5
+// cslab<shape> | hyb<1..7> | split<0..16>; bwd2d = alu | tex | smem |
+// split<0..16>; bwd2d_minb = 3 | 4 | 5
 // | 14 | 24; adj2d = pair | quad; fwd3d = alu | tex3 | tex2l | slab | quad |
 // mixed; fwd3d_tex = 0..8 (texture warps of 8 in forward 5);
 // fwd3d_block = BXxBYxBZ;
@@ -86,6 +90,8 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
     for (const auto &[key, val] : kv) {
         if (p2 && key == "fwd2d") {
             if (val == "alu") p2->algo_fwd = 0;
+            for (int k = 0; k <= 16; ++k)
+                if (val == "split" + std::to_string(k)) p2->algo_fwd = 5, p2->split_sixteenths = k;
             if (val == "tex") p2->algo_fwd = 1;
             if (val == "slab") p2->algo_fwd = 3;
             if (val.rfind("cslab", 0) == 0) {
@@ -103,6 +109,9 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
             if (val == "alu") p2->algo_bwd = 0;
             if (val == "tex") p2->algo_bwd = 1;
             if (val == "smem") p2->algo_bwd = 2;
+            for (int k = 0; k <= 16; ++k)
+                if (val == "split" + std::to_string(k) && !p2->vec && p2->nangles <= 2048)
+                    p2->algo_bwd = 3, p2->bwd_split_sixteenths = k;
         }
         if (p2 && key == "adj2d") {
             if (val == "pair") p2->adj_quad = 0;
@@ -597,10 +606,12 @@ int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by) {
 int cg_plan2d_set_algorithm(cg_plan2d *plan, int forward, int backward) {
     clear_error();
     CG_REQUIRE(plan, "plan is NULL");
-    CG_REQUIRE(forward >= -1 && forward <= 4, "2D forward algorithm must be -1..4");
-    CG_REQUIRE(backward >= -1 && backward <= 2, "2D backward algorithm must be -1..2");
+    CG_REQUIRE(forward >= -1 && forward <= 5, "2D forward algorithm must be -1..5");
+    CG_REQUIRE(backward >= -1 && backward <= 3, "2D backward algorithm must be -1..3");
     CG_REQUIRE(!plan->vec || backward == -1 || backward == 2,
                "vector-geometry plans backproject with the staged algorithm (2)");
+    CG_REQUIRE(backward != 3 || plan->nangles <= 2048,
+               "the split backprojection takes at most 2048 views");
     if (forward >= 0) plan->algo_fwd = forward;
     if (backward >= 0) plan->algo_bwd = backward;
     return CG_OK;
@@ -626,6 +637,32 @@ int cg_plan2d_tables(const cg_plan2d *plan, float *sources, float *u_origins, fl
 
 namespace {
 
+int ensure_aux_stream(cg_plan2d *plan);
+
+// Forward algorithm 5: the first share of the views through the texture unit
+// on the plan's internal stream, the rest by the chunked forward on the
+// caller's stream, the two kernels resident side by side (the chunked
+// forward's blocks are bounded by shared memory, the texture forward's use
+// none).  The internal stream forks from and joins back into the caller's
+// stream through events, so the call stays stream-ordered and capturable.
+int forward2d_split(cg_plan2d *plan, const float *volume, float *sinogram, cudaStream_t s) {
+    int rc = load_vol_texture(*plan, volume, s);
+    if (rc) return rc;
+    if ((rc = ensure_aux_stream(plan))) return rc;
+    const int vt = (int)((long long)plan->nangles * plan->split_sixteenths / 16);
+    CG_TRY_CUDA(cudaEventRecord(plan->ev_fork, s));
+    CG_TRY_CUDA(cudaStreamWaitEvent(plan->aux, plan->ev_fork, 0));
+    rc = launch_forward2d_tex_views(*plan, sinogram, 0, vt, plan->aux);
+    if (!rc) rc = launch_forward2d_cslab(*plan, sinogram, s, plan->fwd_chunk_rows, vt);
+    // join even after an error so the caller's stream (or capture) is whole
+    const cudaError_t e1 = cudaEventRecord(plan->ev_join, plan->aux);
+    const cudaError_t e2 = cudaStreamWaitEvent(s, plan->ev_join, 0);
+    if (rc) return rc;
+    CG_TRY_CUDA(e1);
+    CG_TRY_CUDA(e2);
+    return CG_OK;
+}
+
 int forward2d_f32(cg_plan2d *plan, const float *volume, float *sinogram, cudaStream_t s) {
     if (plan->algo_fwd == 1) return launch_forward2d_tex(*plan, volume, sinogram, s);
     if (plan->algo_fwd == 2) return launch_forward2d_hyb(*plan, volume, sinogram, s);
@@ -634,13 +671,49 @@ int forward2d_f32(cg_plan2d *plan, const float *volume, float *sinogram, cudaStr
     if (plan->algo_fwd == 3 && slab_supported(*plan))
         return launch_forward2d_slab(*plan, sinogram, s);
     if (plan->algo_fwd == 4) return launch_forward2d_cslab(*plan, sinogram, s, plan->fwd_chunk_rows);
+    if (plan->algo_fwd == 5) return forward2d_split(plan, volume, sinogram, s);
     return launch_forward2d(*plan, sinogram, s);
+}
+
+// Backward algorithm 3: the last share of the pixel rows through the
+// texture unit on the plan's internal stream, the first rows by the staged
+// backprojector on the caller's stream, side by side (the staged kernel is
+// bound by instruction issue, the texture one by the texture unit); the rows
+// are disjoint, so the two add into the volume independently.
+int ensure_aux_stream(cg_plan2d *plan) {
+    if (!plan->aux) {
+        CG_TRY_CUDA(cudaStreamCreateWithFlags(&plan->aux, cudaStreamNonBlocking));
+        CG_TRY_CUDA(cudaEventCreateWithFlags(&plan->ev_fork, cudaEventDisableTiming));
+        CG_TRY_CUDA(cudaEventCreateWithFlags(&plan->ev_join, cudaEventDisableTiming));
+    }
+    return CG_OK;
+}
+
+int backward2d_split(cg_plan2d *plan, float *volume, cudaStream_t s) {
+    constexpr int kTile = 64;  // pixel rows of one staged tile
+    const int ys = (int)((long long)plan->H * (16 - plan->bwd_split_sixteenths) / 16) / kTile * kTile;
+    int rc = ensure_aux_stream(plan);
+    if (rc) return rc;
+    CG_TRY_CUDA(cudaEventRecord(plan->ev_fork, s));
+    CG_TRY_CUDA(cudaStreamWaitEvent(plan->aux, plan->ev_fork, 0));
+    rc = launch_backward2d_tex_rows(*plan, volume, ys, plan->aux);
+    if (!rc) rc = launch_backward2d_smem(*plan, volume, s, ys);
+    const cudaError_t e1 = cudaEventRecord(plan->ev_join, plan->aux);
+    const cudaError_t e2 = cudaStreamWaitEvent(s, plan->ev_join, 0);
+    if (rc) return rc;
+    CG_TRY_CUDA(e1);
+    CG_TRY_CUDA(e2);
+    return CG_OK;
 }
 
 int backward2d_f32(cg_plan2d *plan, float *volume, const float *sinogram, cudaStream_t s) {
     if (plan->algo_bwd == 1) return launch_backward2d_tex(*plan, volume, sinogram, s);
     int rc = launch_relayout_sino2d(*plan, sinogram, s);
     if (rc) return rc;
+    if (plan->algo_bwd == 3) {
+        if ((rc = load_sino_texture(*plan, sinogram, s))) return rc;
+        return backward2d_split(plan, volume, s);
+    }
     if (plan->algo_bwd == 2) return launch_backward2d_smem(*plan, volume, s);
     return launch_backward2d(*plan, volume, s);
 }

@@ -105,12 +105,21 @@ struct Plan2d {
 
     // algorithm per operator: forward 0 = registers, 1 = texture unit,
     // 2 = texture + registers, 3 = shared-memory row slabs, 4 = chunked
-    // shared-memory slabs;
+    // shared-memory slabs, 5 = chunked slabs beside the texture unit on a
+    // share of the views;
     // backprojection 0 = registers, 1 = texture unit, 2 = shared-memory rows.
     // Defaults: the fastest measured on GB300 (2D n-sweep); the forward
     // becomes chunked for volumes of 1536^2 pixels and more (cg_plan2d_create).
     int algo_fwd = 1, algo_bwd = 2;
     int tex_eighths = 4;              // hybrid forward: share of warps on the texture unit
+    // split forward (algorithm 5): sixteenths of the views projected by the
+    // texture unit on an internal stream beside the chunked forward's rest
+    int split_sixteenths = 4;
+    // split backprojection (algorithm 3): sixteenths of the pixel rows
+    // backprojected by the texture unit beside the staged kernel's rest
+    int bwd_split_sixteenths = 3;
+    cudaStream_t aux = nullptr;       // internal stream, created on first use
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int fwd_chunk_rows = 408;         // chunked forward: chunk shape (8 rows, 128-cell
                                       // bundles, packed sums, pair reuse)
     // staged backprojector variant: 24 = 4 blocks/SM, packed FP32 pairs of
@@ -232,12 +241,16 @@ int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream
 int launch_adjoint2d(Plan2d &p, float *vol, const float *sino, cudaStream_t s);
 int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s);
 
-int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s);
+int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s, int rows = -1);
+int load_sino_texture(Plan2d &p, const float *sino, cudaStream_t s);
+int launch_backward2d_tex_rows(const Plan2d &p, float *vol, int y0, cudaStream_t s);
 bool slab_supported(const Plan2d &p);
 int launch_forward2d_slab(const Plan2d &p, float *sino, cudaStream_t s);
 // rows: chunk shape (4, 8: rows of 256-cell bundles; 104, 108: 4 or 8 rows
 // of 128-cell bundles)
-int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int rows);
+int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int rows, int v0 = 0,
+                           int nv = -1);
+int launch_forward2d_tex_views(const Plan2d &p, float *sino, int v0, int nv, cudaStream_t s);
 // Copies the volume into the plan's 2D texture array.
 int load_vol_texture(Plan2d &p, const float *vol, cudaStream_t s);
 int launch_forward2d_tex(Plan2d &p, const float *vol, float *sino, cudaStream_t s);

@@ -659,8 +659,12 @@ __global__ void __launch_bounds__(T)
 
 }  // namespace
 
-int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int rows) {
-    const int groups = ceil_div(p.nangles, kCs2G);
+int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int rows, int v0,
+                           int nv) {
+    // views [v0, v0 + nv): the kernel sees offset tables and sinogram rows
+    if (nv < 0) nv = p.nangles - v0;
+    if (nv <= 0) return CG_OK;
+    const int groups = ceil_div(nv, kCs2G);
     if (groups > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     if (std::max(p.pitchA(), p.pitchB()) >= 32768)
         return set_error(CG_ERR_INVALID, "volume too wide for the chunked forward");
@@ -668,9 +672,9 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
         const size_t smem = 2 * sizeof(float2) * (k + 1) * stride;
         if (int rc = ensure_smem_attr((const void *)kernel, (int)smem)) return rc;
         dim3 grid(ceil_div(p.det, threads), groups, 2);
-        kernel<<<grid, threads, smem, s>>>(p.d_layA, p.d_layB, sino, p.d_src, p.d_u0, p.d_du,
-                                           p.W, p.H, p.det, p.nangles, p.sx, p.sy, p.pitchA(),
-                                           p.pitchB());
+        kernel<<<grid, threads, smem, s>>>(p.d_layA, p.d_layB, sino + (size_t)v0 * p.det,
+                                           p.d_src + v0, p.d_u0 + v0, p.d_du + v0, p.W, p.H,
+                                           p.det, nv, p.sx, p.sy, p.pitchA(), p.pitchB());
         CG_TRY_CUDA(cudaGetLastError());
         return CG_OK;
     };
@@ -853,14 +857,13 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                         float2 f;
                         unsigned l0, l1;
                         if constexpr (MAGIC) {
-                            // floor without the conversion unit: ub - 1/2 + 1.5 * 2^23
-                            // rounds to the nearest integer, i.e. floor(ub) (at an exact
-                            // integer possibly one less, with fraction 1: the same lerp);
-                            // |ub| >= 2^22 lands outside the window and is clamped
-                            const float2 t = __fadd2_rn(__fadd2_rn(ub, make_float2(-0.5f, -0.5f)),
-                                                        make_float2(12582912.0f, 12582912.0f));
-                            const float2 kf = __fadd2_rn(t, make_float2(-12582912.0f, -12582912.0f));
-                            f = __fadd2_rn(ub, make_float2(-kf.x, -kf.y));
+                            // floor without the conversion unit: ub + 1.5 * 2^23
+                            // rounded toward -inf is floor(ub) + 1.5 * 2^23 exactly
+                            // (unit spacing there); |ub| >= 2^22 lands outside the
+                            // window and is clamped.  f = ub + (1.5 * 2^23 - t).
+                            const float2 M2 = make_float2(12582912.0f, 12582912.0f);
+                            const float2 t = __fadd2_rd(ub, M2);
+                            f = __fadd2_rn(ub, __ffma2_rn(t, make_float2(-1.f, -1.f), M2));
                             const unsigned base = 0x4B400000u + (unsigned)k0;
                             l0 = min(__float_as_uint(t.x) - base, (unsigned)(kSmWin - 1));
                             l1 = min(__float_as_uint(t.y) - base, (unsigned)(kSmWin - 1));
@@ -1047,8 +1050,11 @@ int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s) {
     return CG_OK;
 }
 
-int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s) {
-    dim3 grid(ceil_div(p.W, 32), ceil_div(p.H, 8 * kSmRows));
+int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s, int rows) {
+    // pixel rows [0, rows): whole tiles of 8 * kSmRows rows, or all of H
+    if (rows < 0) rows = p.H;
+    if (rows <= 0) return CG_OK;
+    dim3 grid(ceil_div(p.W, 32), ceil_div(rows, 8 * kSmRows));
     auto go = [&](auto kernel) {
         kernel<<<grid, dim3(32, 8), 0, s>>>(vol, p.d_sinoP, p.d_bproj, p.W, p.H, p.det,
                                             p.nangles, p.sx, p.sy, p.ox, p.oy, p.ds);

@@ -198,11 +198,11 @@ constexpr int kTexBwdViews = 256;
 __global__ void __launch_bounds__(256)
     k_bwd2d_tex(float *__restrict__ vol, cudaTextureObject_t tex, const float4 *__restrict__ meta,
                 int W, int H, int det, int v0, int nv, float sx, float sy, float ox, float oy,
-                float ds) {
+                float ds, int ybase) {
     __shared__ float4 smeta[kTexBwdViews];
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const int x = blockIdx.x * 32 + threadIdx.x;
-    const int y0 = blockIdx.y * 32 + threadIdx.y;
+    const int y0 = ybase + blockIdx.y * 32 + threadIdx.y;
     const float ex = (float)W / 2.0f, ey = (float)H / 2.0f, ed = (float)det / 2.0f;
     const float inv = __fdividef(1.0f, ds);
     const float X = ((float)x - ex) * sx + ox + 0.5f;
@@ -378,6 +378,19 @@ int launch_forward2d_tex(Plan2d &p, const float *vol, float *sino, cudaStream_t 
     return CG_OK;
 }
 
+// Views [v0, v0 + nv) from the volume texture already loaded.
+int launch_forward2d_tex_views(const Plan2d &p, float *sino, int v0, int nv, cudaStream_t s) {
+    if (nv <= 0) return CG_OK;
+    dim3 block(p.fwd_bx, p.fwd_by);
+    dim3 grid(ceil_div(p.det, p.fwd_bx), ceil_div(nv, p.fwd_by));
+    if (grid.y > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
+    k_fwd2d_tex<<<grid, block, 0, s>>>(p.tex_vol, sino + (size_t)v0 * p.det, p.d_src + v0,
+                                       p.d_u0 + v0, p.d_du + v0, p.W, p.H, p.det, nv, p.sx,
+                                       p.sy);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
 int load_vol_texture(Plan2d &p, const float *vol, cudaStream_t s) {
     if (!p.arr_vol) {
         int rc = alloc_array(&p.arr_vol, p.W, p.H, 0, cudaArrayDefault);
@@ -418,9 +431,29 @@ int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t
         int rc = copy_to_array(p.arr_sino, sino + (size_t)v0 * p.det, p.det, 1, nv, s);
         if (rc) return rc;
         k_bwd2d_tex<<<grid, dim3(32, 8), 0, s>>>(vol, p.tex_sino, p.d_bmeta, p.W, p.H, p.det, v0,
-                                                 nv, p.sx, p.sy, p.ox, p.oy, p.ds);
+                                                 nv, p.sx, p.sy, p.ox, p.oy, p.ds, 0);
         CG_TRY_CUDA(cudaGetLastError());
     }
+    return CG_OK;
+}
+
+int load_sino_texture(Plan2d &p, const float *sino, cudaStream_t s) {
+    if (p.nangles > 2048) return set_error(CG_ERR_INVALID, "more views than one layered texture");
+    if (!p.arr_sino) {
+        int rc = alloc_array(&p.arr_sino, p.det, 0, p.nangles, cudaArrayLayered);
+        if (rc) return rc;
+        if ((rc = make_texture(p.arr_sino, &p.tex_sino))) return rc;
+    }
+    return copy_to_array(p.arr_sino, sino, p.det, 1, p.nangles, s);
+}
+
+// Pixel rows [y0, H) through the texture unit (the sinogram texture loaded).
+int launch_backward2d_tex_rows(const Plan2d &p, float *vol, int y0, cudaStream_t s) {
+    if (y0 >= p.H) return CG_OK;
+    dim3 grid(ceil_div(p.W, 32), ceil_div(p.H - y0, 32));
+    k_bwd2d_tex<<<grid, dim3(32, 8), 0, s>>>(vol, p.tex_sino, p.d_bmeta, p.W, p.H, p.det, 0,
+                                             p.nangles, p.sx, p.sy, p.ox, p.oy, p.ds, y0);
+    CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }
 

@@ -96,8 +96,12 @@ int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by);
  *   forward:  0 registers (FP32 filtering of pair-packed copies, gathered
  *               through L1), 1 texture unit, 2 texture unit + registers on
  *               alternate warps, 3 shared-memory row slabs, 4 chunked
- *               shared-memory slabs
- *   backward: 0 registers, 1 texture unit, 2 shared-memory detector windows
+ *               shared-memory slabs, 5 chunked slabs beside the texture unit
+ *               on a share of the views (an internal stream forked from and
+ *               joined back into the caller's)
+ *   backward: 0 registers, 1 texture unit, 2 shared-memory detector windows,
+ *             3 windows beside the texture unit on a share of the pixel rows
+ *             (circular geometry, at most 2048 views)
  * The texture unit filters with 8-bit weight fractions, exactly as the
  * reference does; the other algorithms filter in FP32, and cg_adjoint_2d is
  * the transpose of forward algorithms 0, 3 and 4 (exact for 0 and 3; 4 takes

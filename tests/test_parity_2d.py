@@ -95,6 +95,10 @@ def test_backward_algorithms(cuda_device, algo, n, nangles):
     the layered texture's 2048 views."""
     g = fan_config(n, nangles)
     geom = make(g, cuda_device)
+    if algo == "split" and nangles > 2048:
+        with pytest.raises(ValueError, match="2048"):
+            geom.plan.set_algorithm(backward=algo)
+        return
     geom.plan.set_algorithm(backward=algo)
     rng = np.random.default_rng(n + nangles)
     sino = rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32)
@@ -245,3 +249,66 @@ def test_algorithm_override_variable(cuda_device):
                          cwd=Path(__file__).resolve().parents[1], timeout=300)
     assert out.returncode == 0, out.stderr
     assert "('registers', 'texture')" in out.stdout, out.stdout
+
+
+@pytest.mark.parametrize("k", [0, 3, 16])
+def test_split_forward_shares_and_graph(cuda_device, monkeypatch, k):
+    """The split forward (k sixteenths of the views on the texture unit, on an
+    internal stream forked from the caller's) equals the oracle for every
+    share and is capturable in a CUDA graph: a replay equals a direct call."""
+    n, nangles = 160, 90
+    g = fan_config(n, nangles)
+    monkeypatch.setenv("CURADON_GB300_ALGO", f"fwd2d=split{k}")
+    geom = FanGeometry(**g, device=cuda_device.index or 0)
+    assert geom.plan.algorithm[0] == "split"
+    monkeypatch.delenv("CURADON_GB300_ALGO")
+    v = ellipses_2d(n, 3, device=cuda_device).contiguous()
+    s = torch.zeros(geom.sinogram_shape(), device=cuda_device)
+    forward(v, s, geom)
+    torch.cuda.synchronize()
+    so = oracle.fwd2d(g, v.cpu().numpy())
+    assert rel_l2(s.cpu().numpy(), so) < TOL
+    out = torch.zeros_like(s)
+    graph = torch.cuda.CUDAGraph()
+    st = torch.cuda.Stream()
+    st.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(st), torch.cuda.graph(graph, stream=st):
+        forward(v, out, geom)
+    torch.cuda.current_stream().wait_stream(st)
+    out.zero_()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out, s)
+
+
+@pytest.mark.parametrize("k", [0, 5, 16])
+def test_split_backward_shares_and_graph(cuda_device, monkeypatch, k):
+    """The split backprojection (k sixteenths of the pixel rows on the texture
+    unit, on an internal stream) equals the oracle for every share, adds into
+    the volume, and replays from a CUDA graph like a direct call."""
+    n, nangles = 200, 120
+    g = fan_config(n, nangles)
+    monkeypatch.setenv("CURADON_GB300_ALGO", f"bwd2d=split{k}")
+    geom = FanGeometry(**g, device=cuda_device.index or 0)
+    assert geom.plan.algorithm[1] == "split"
+    monkeypatch.delenv("CURADON_GB300_ALGO")
+    rng = np.random.default_rng(k)
+    sino = torch.as_tensor(rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32),
+                           device=cuda_device)
+    v0 = torch.as_tensor(rng.uniform(0, 1, (n, n)).astype(np.float32), device=cuda_device)
+    b = v0.clone()
+    backward(sino, b, geom)
+    torch.cuda.synchronize()
+    e = rel_l2((b - v0).cpu().numpy(), oracle.bwd2d(g, sino.cpu().numpy()))
+    assert e < TOL, e
+    out = v0.clone()
+    graph = torch.cuda.CUDAGraph()
+    st = torch.cuda.Stream()
+    st.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(st), torch.cuda.graph(graph, stream=st):
+        backward(sino, out, geom)
+    torch.cuda.current_stream().wait_stream(st)
+    out.copy_(v0)
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out, b)
