@@ -64,8 +64,8 @@ void free_plan3d(Plan3d *p) {
 // from CURADON_GB300_ALGO: comma-separated key=value tokens, e.g.
 // "fwd2d=tex,bwd2d_minb=4".  Keys: fwd2d = alu | tex | slab | cslab |
 // cslab<shape> | hyb<1..7> | split<0..16>; bwd2d = alu | tex | smem |
-// split<0..16>; bwd2d_minb = 3 | 4 | 5
-// | 14 | 24; adj2d = pair | quad; fwd3d = alu | tex3 | tex2l | slab | quad |
+// split<0..16>; bwd2d_minb = 3 | 4 | 5 | 14 | 24 | 25 | 26 | 27 | 28 (staged
+// backprojector shapes); adj2d = pair | quad; fwd3d = alu | tex3 | tex2l | slab | quad |
 // mixed; fwd3d_tex = 0..8 (texture warps of 8 in forward 5);
 // fwd3d_block = BXxBYxBZ;
 // bwd3d = scalar | pk | pkmagic | quad (backward 0) | ax8m5 | ax8 | ax16 |
@@ -118,7 +118,7 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
             if (val == "quad") p2->adj_quad = 1;
         }
         if (p2 && key == "bwd2d_minb")
-            for (int k : {3, 4, 5, 14, 24})
+            for (int k : {3, 4, 5, 14, 24, 25, 26, 27, 28})
                 if (val == std::to_string(k)) p2->bwd_min_blocks = k;
         if (p3 && key == "fwd3d") {
             if (val == "alu") p3->algo_fwd = 0;

@@ -122,10 +122,12 @@ struct Plan2d {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int fwd_chunk_rows = 408;         // chunked forward: chunk shape (8 rows, 128-cell
                                       // bundles, packed sums, pair reuse)
-    // staged backprojector variant: 24 = 4 blocks/SM, packed FP32 pairs of
-    // rows, floor taken by FP32 adds (default, measured fastest); 14 = the
-    // same with the conversion unit's floor; 3, 4, 5 = scalar at 3..5 blocks/SM
-    int bwd_min_blocks = 24;
+    // staged backprojector variant: 27 = 4 blocks/SM, packed FP32 pairs of
+    // rows, floor taken by FP32 adds, windows copied with cp.async (default,
+    // measured fastest); 24 = the same with register copies; 25 / 26 = 24
+    // with the view loop unrolled 4 / 1 times; 28 = 27 unrolled 4 times; 14 =
+    // 24 with the conversion unit's floor; 3, 4, 5 = scalar at 3..5 blocks/SM
+    int bwd_min_blocks = 27;
 
     // row pitches of layA / layB in pairs, even so every row starts on 16 bytes
     int pitchA() const { return (W + 2 * kPad + 1) & ~1; }

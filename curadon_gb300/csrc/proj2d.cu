@@ -774,7 +774,7 @@ constexpr int kSmWin = 128;   // pairs of one view's row staged for a tile
 // with the per-view terms of each thread's column hoisted, then one
 // reciprocal, one 8-byte shared load and two FMAs.  The same table describes
 // an arbitrary per-view source / detector placement (vector geometry).
-template <bool PK, bool MAGIC = false>
+template <bool PK, bool MAGIC = false, int VU = 2, bool CPA = false>
 __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                                                 const float2 *__restrict__ S,
                                                 const float4 *__restrict__ proj, int W, int H,
@@ -791,12 +791,23 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
     const float edm = (float)det / 2.0f - 0.5f;
     const float inv = __fdividef(1.0f, ds);
     const float X = ((float)x - ex) * sx + ox + 0.5f;
-    float Y[kSmRows], acc[kSmRows];
+    // rows r and r + 1 of the thread's column as one pair (the packed loop's
+    // operands and accumulators)
+    float2 Y2[kSmRows / 2], acc2[kSmRows / 2];
 #pragma unroll
-    for (int r = 0; r < kSmRows; ++r) {
-        Y[r] = ((float)(y0 + 8 * r) - ey) * sy + oy + 0.5f;
-        acc[r] = 0.f;
+    for (int i = 0; i < kSmRows / 2; ++i) {
+        Y2[i] = make_float2(((float)(y0 + 16 * i) - ey) * sy + oy + 0.5f,
+                            ((float)(y0 + 16 * i + 8) - ey) * sy + oy + 0.5f);
+        acc2[i] = make_float2(0.f, 0.f);
     }
+    auto Yv = [&](int r) -> float { return (r & 1) ? Y2[r >> 1].y : Y2[r >> 1].x; };
+    auto add = [&](int r, float v) {
+        if (r & 1) acc2[r >> 1].y += v; else acc2[r >> 1].x += v;
+    };
+    auto fma_acc = [&](int r, float a, float b) {
+        if (r & 1) acc2[r >> 1].y = fmaf(a, b, acc2[r >> 1].y);
+        else acc2[r >> 1].x = fmaf(a, b, acc2[r >> 1].x);
+    };
     const int pitch = det + 2 * kPad;
     for (int v0 = 0; v0 < nangles; v0 += kSmViews) {
         const int nv = min(kSmViews, nangles - v0);
@@ -831,10 +842,18 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
             const int k0 = skmin[j];
             if (k0 == INT_MIN) continue;
             const int k = min(max(k0 + i, -kPad), det);
-            srow[j][i] = S[(size_t)(v0 + j) * pitch + kPad + k];
+            if constexpr (CPA) {
+                // 8-byte asynchronous copy, no register round trip
+                const unsigned d = (unsigned)__cvta_generic_to_shared(&srow[j][i]);
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d),
+                             "l"(S + (size_t)(v0 + j) * pitch + kPad + k));
+            } else {
+                srow[j][i] = S[(size_t)(v0 + j) * pitch + kPad + k];
+            }
         }
+        if constexpr (CPA) asm volatile("cp.async.wait_all;\n" ::);
         __syncthreads();
-#pragma unroll 2
+#pragma unroll VU
         for (int j = 0; j < nv; ++j) {
             const float4 a = sA[j], b = sB[j];
             const int k0 = skmin[j];
@@ -849,7 +868,7 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                     const float2 e2 = make_float2(edm, edm);
 #pragma unroll
                     for (int r = 0; r < kSmRows; r += 2) {
-                        const float2 Yr = make_float2(Y[r], Y[r + 1]);
+                        const float2 Yr = Y2[r >> 1];
                         const float2 den = __ffma2_rn(ay, Yr, A2);
                         const float2 yi = __ffma2_rn(by, Yr, B2);
                         const float2 w = make_float2(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y));
@@ -875,36 +894,35 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                         }
                         const float2 t0 = sr[l0], t1 = sr[l1];
                         const float2 v = make_float2(fmaf(f.x, t0.y, t0.x), fmaf(f.y, t1.y, t1.x));
-                        const float2 acc2 = __ffma2_rn(v, w, make_float2(acc[r], acc[r + 1]));
-                        acc[r] = acc2.x, acc[r + 1] = acc2.y;
+                        acc2[r >> 1] = __ffma2_rn(v, w, acc2[r >> 1]);
                     }
                 } else {
 #pragma unroll
                     for (int r = 0; r < kSmRows; ++r) {
-                        const float den = fmaf(a.y, Y[r], A);
-                        const float yi = fmaf(b.y, Y[r], B);
+                        const float den = fmaf(a.y, Yv(r), A);
+                        const float yi = fmaf(b.y, Yv(r), B);
                         const float w = __fdividef(1.0f, den);
                         const float ub = fmaf(w, yi, edm);
                         const float kf = floorf(ub);
                         const float f = ub - kf;
                         const unsigned li = min((unsigned)((int)kf - k0), (unsigned)(kSmWin - 1));
                         const float2 t = sr[li];
-                        acc[r] = fmaf(fmaf(f, t.y, t.x), w, acc[r]);
+                        fma_acc(r, fmaf(f, t.y, t.x), w);
                     }
                 }
             } else {
                 const float2 *row = S + (size_t)(v0 + j) * pitch;
 #pragma unroll
                 for (int r = 0; r < kSmRows; ++r) {
-                    const float den = fmaf(a.y, Y[r], A);
-                    const float yi = fmaf(b.y, Y[r], B);
+                    const float den = fmaf(a.y, Yv(r), A);
+                    const float yi = fmaf(b.y, Yv(r), B);
                     const float w = __fdividef(1.0f, den);
                     const float ub = fmaf(w, yi, edm);
                     const float kf = floorf(ub);
                     const float f = ub - kf;
                     const unsigned col = min((unsigned)((int)kf + kPad), (unsigned)(det + kPad));
                     const float2 t = __ldg(row + col);
-                    acc[r] = fmaf(fmaf(f, t.y, t.x), w, acc[r]);
+                    fma_acc(r, fmaf(f, t.y, t.x), w);
                 }
             }
         }
@@ -913,19 +931,20 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
 #pragma unroll
         for (int r = 0; r < kSmRows; ++r) {
             const int y = y0 + 8 * r;
-            if (y < H) vol[(size_t)y * W + x] += acc[r] * inv;
+            const float a = (r & 1) ? acc2[r >> 1].y : acc2[r >> 1].x;
+            if (y < H) vol[(size_t)y * W + x] += a * inv;
         }
     }
 }
 
 // MINB: resident blocks per SM the register allocation must allow
-template <int MINB, bool PK, bool MAGIC = false>
+template <int MINB, bool PK, bool MAGIC = false, int VU = 2, bool CPA = false>
 __global__ void __launch_bounds__(256, MINB)
     k_bwd2d_smem(float *__restrict__ vol, const float2 *__restrict__ S,
                  const float4 *__restrict__ proj, int W, int H, int det, int nangles, float sx,
                  float sy, float ox, float oy, float ds) {
-    bwd2d_smem_tile<PK, MAGIC>(vol, S, proj, W, H, det, nangles, sx, sy, ox, oy, ds, blockIdx.x,
-                               blockIdx.y);
+    bwd2d_smem_tile<PK, MAGIC, VU, CPA>(vol, S, proj, W, H, det, nangles, sx, sy, ox, oy, ds,
+                                        blockIdx.x, blockIdx.y);
 }
 
 }  // namespace
@@ -1064,7 +1083,12 @@ int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s, int rows
         case 4: go(k_bwd2d_smem<4, false>); break;
         case 5: go(k_bwd2d_smem<5, false>); break;
         case 14: go(k_bwd2d_smem<4, true>); break;
-        default: go(k_bwd2d_smem<4, true, true>); break;
+        case 25: go(k_bwd2d_smem<4, true, true, 4>); break;
+        case 26: go(k_bwd2d_smem<4, true, true, 1>); break;
+        case 27: go(k_bwd2d_smem<4, true, true, 2, true>); break;
+        case 28: go(k_bwd2d_smem<4, true, true, 4, true>); break;
+        case 24: go(k_bwd2d_smem<4, true, true>); break;
+        default: go(k_bwd2d_smem<4, true, true, 2, true>); break;
     }
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;

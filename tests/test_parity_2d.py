@@ -312,3 +312,22 @@ def test_split_backward_shares_and_graph(cuda_device, monkeypatch, k):
     graph.replay()
     torch.cuda.synchronize()
     assert torch.equal(out, b)
+
+
+@pytest.mark.parametrize("shape", [3, 4, 5, 14, 24, 25, 26, 27, 28])
+def test_staged_backprojector_shapes(cuda_device, monkeypatch, shape):
+    """Every compiled shape of the staged backprojector (CURADON_GB300_ALGO
+    bwd2d_minb=...: blocks per SM, packed rows, floor by FP32 adds, view-loop
+    unrolling, asynchronous window copies) against the oracle."""
+    n, nangles = 256, 150
+    g = fan_config(n, nangles)
+    monkeypatch.setenv("CURADON_GB300_ALGO", f"bwd2d=smem,bwd2d_minb={shape}")
+    geom = FanGeometry(**g, device=cuda_device.index or 0)
+    geom.plan
+    monkeypatch.delenv("CURADON_GB300_ALGO")
+    rng = np.random.default_rng(shape)
+    sino = rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32)
+    b = run_bwd(geom, sino, cuda_device)
+    e = rel_l2(b, oracle.bwd2d(g, sino))
+    print(f"shape {shape} bwd rel-L2 {e:.2e}")
+    assert e < TOL
