@@ -219,13 +219,22 @@ def kernels_per_step(wl, geom) -> int:
     with the plan's algorithms (texture-unit paths copy the input into a
     CUDA array with a memcpy, which is not a kernel)."""
     fwd, bwd = geom.plan.algorithm
+    nv = len(wl["geom"]["angles"])
     if wl["kind"] == "fan":
-        nv = len(wl["geom"]["angles"])
-        f = 1 if fwd == "texture" else 2
-        b = -(-nv // 2048) if bwd == "texture" else 2
+        # forward: texture 1; split: re-layout + texture share + chunked rest;
+        # others: re-layout + kernel
+        f = {"texture": 1, "split": 3}.get(fwd, 2)
+        # backprojection: texture one per 2048 views; split: re-layout +
+        # texture rows + staged rows; others: re-layout + kernel
+        b = {"texture": -(-nv // 2048), "split": 3}.get(bwd, 2)
         return f + b
-    f = 1 if fwd == "texture" else 3 if fwd in ("registers", "slab") else 2
-    return f + 2
+    # forward: texture 1; layered: transpose + kernel; registers, slab, quad,
+    # mixed: two re-layouts + kernel
+    f = {"texture": 1, "layered": 2}.get(fwd, 3)
+    # backprojection: re-layout + one kernel (axial: one per 768 views)
+    b = 1 + (-(-nv // 768) if bwd == "axial" else 1)
+    return f + b
+
 
 def run_ours(args, rank, world, local_rank):
     import torch
