@@ -3,14 +3,15 @@
 ``Batch2d(geoms, volumes, sinograms)`` binds any number of fan-beam problems
 -- any sizes, circular or vector geometries -- to their float32 CUDA
 tensors.  ``forward()`` then projects every volume into its sinogram and
-``backward()`` adds every backprojection into its volume, each as two
-kernel launches over a (problem, tile) work list instead of two per problem.
+``backward()`` adds every backprojection into its volume, each over a
+(problem, tile) work list in one or two launches instead of two per problem.
 The buffers stay bound, so both calls can be captured in a CUDA graph
 (``torch.cuda.graph``) and an iteration loop replayed without launch
-overhead.  The forward is the FP32 register ray march and the backprojection
-the staged one; their results equal the single-problem operators with those
-algorithms bit for bit.  No counterpart in the reference, which runs one
-problem per call.
+overhead.  The forward is the texture-unit ray march (``forward="texture"``,
+default: one array copy per problem, then one launch) or the FP32 register
+march (``forward="registers"``); the backprojection is the staged one; their
+results equal the single-problem operators with those algorithms bit for
+bit.  No counterpart in the reference, which runs one problem per call.
 """
 from __future__ import annotations
 
@@ -27,8 +28,12 @@ __all__ = ["Batch2d"]
 
 
 class Batch2d:
+    FORWARD = ("registers", "texture")
+
     def __init__(self, geoms: Sequence[FanGeometry], volumes: Sequence[torch.Tensor],
-                 sinograms: Sequence[torch.Tensor]):
+                 sinograms: Sequence[torch.Tensor], forward: str = "texture"):
+        if forward not in self.FORWARD:
+            raise ValueError(f"batched forward must be one of {self.FORWARD}")
         if not (len(geoms) == len(volumes) == len(sinograms)) or not geoms:
             raise ValueError("geoms, volumes and sinograms must be non-empty and of one length")
         dev = volumes[0].device
@@ -57,6 +62,7 @@ class Batch2d:
         h = C.c_void_p()
         check(self._L.cg_batch2d_create(C.byref(h), hp, vp, sp, n))
         self._h = h
+        check(self._L.cg_batch2d_set_forward(h, self.FORWARD.index(forward)))
         self._keep = (list(geoms), list(volumes), list(sinograms), plans)
         self.device = dev
         self.count = n
@@ -66,6 +72,12 @@ class Batch2d:
         if h is not None and h.value:
             self._L.cg_batch2d_destroy(h)
             self._h = None
+
+    @property
+    def forward_algorithm(self) -> str:
+        a = C.c_int()
+        check(self._L.cg_batch2d_get_forward(self._h, C.byref(a)))
+        return self.FORWARD[a.value]
 
     def forward(self):
         """sinogram_i = A_i volume_i for every problem (on the current stream)."""

@@ -9,11 +9,13 @@
 // calls stream-ordered and capturable in a CUDA graph (an iteration loop is
 // captured once and replayed).
 //
-// The batched forward is the register ray march (algorithm 0) and the
-// batched backprojection the staged one (algorithm 2), the FP32 algorithms
-// that need no per-problem texture; each problem uses its own plan's scratch,
-// so a plan may appear in one batch only once, and a batch must not overlap
-// on the GPU with other calls on its plans.
+// The batched forward is the texture-unit ray march (algorithm 1; each
+// problem's volume is copied into its plan's array, then one launch samples
+// all problems through their bindless texture handles) or, selected with
+// cg_batch2d_set_forward, the FP32 register march (algorithm 0); the batched
+// backprojection is the staged one (algorithm 2).  Each problem uses its own
+// plan's scratch, so a plan may appear in one batch only once, and a batch
+// must not overlap on the GPU with other calls on its plans.
 #include <memory>
 #include <set>
 #include <string>
@@ -24,7 +26,9 @@
 struct cg_batch2d {
     int device = 0;
     int count = 0;
+    int fwd_algo = 1;  // 1 texture unit, 0 registers
     std::vector<cg::Plan2d *> plans;
+    std::vector<cg::Prob2d> probs;  // host copy (the texture forward's copies)
     cg::Prob2d *d_probs = nullptr;
     int *d_starts = nullptr;  // 4 stages x (count + 1)
     int totals[4] = {0, 0, 0, 0};
@@ -72,6 +76,8 @@ int cg_batch2d_create(cg_batch2d **batch, cg_plan2d *const *plans, float *const 
         q.W = p.W, q.H = p.H, q.det = p.det, q.nangles = p.nangles;
         q.pa = p.pitchA(), q.pb = p.pitchB();
         q.sx = p.sx, q.sy = p.sy, q.ox = p.ox, q.oy = p.oy, q.ds = p.ds;
+        if (int rc = ensure_vol_texture(*plans[i])) return rc;
+        q.tex = p.tex_vol, q.arr = p.arr_vol;
         int blocks[4];
         batch_blocks(p, blocks);
         for (int st = 0; st < 4; ++st) {
@@ -87,6 +93,7 @@ int cg_batch2d_create(cg_batch2d **batch, cg_plan2d *const *plans, float *const 
     b->device = plans[0]->device;
     b->count = count;
     b->plans.assign(plans, plans + count);
+    b->probs = probs;
     for (int st = 0; st < 4; ++st) b->totals[st] = (int)totals[st];
     auto fail = [&](cudaError_t e) {
         free_batch(b.get());
@@ -122,8 +129,27 @@ int cg_batch2d_forward(cg_batch2d *batch, void *stream) {
     CG_REQUIRE(batch, "batch is NULL");
     DeviceGuard guard(batch->device);
     CG_REQUIRE(guard.ok(), "cannot select the batch's device");
+    if (batch->fwd_algo == 1)
+        return launch_batch2d_fwd_tex(batch->d_probs, batch->probs,
+                                      batch->d_starts + (batch->count + 1), batch->totals[1],
+                                      (cudaStream_t)stream);
     return launch_batch2d(batch->d_probs, batch->d_starts, batch->totals, batch->count, true,
                           (cudaStream_t)stream);
+}
+
+int cg_batch2d_set_forward(cg_batch2d *batch, int algorithm) {
+    clear_error();
+    CG_REQUIRE(batch, "batch is NULL");
+    CG_REQUIRE(algorithm == 0 || algorithm == 1, "batched forward algorithm must be 0 or 1");
+    batch->fwd_algo = algorithm;
+    return CG_OK;
+}
+
+int cg_batch2d_get_forward(const cg_batch2d *batch, int *algorithm) {
+    clear_error();
+    CG_REQUIRE(batch && algorithm, "NULL argument");
+    *algorithm = batch->fwd_algo;
+    return CG_OK;
 }
 
 int cg_batch2d_backward(cg_batch2d *batch, void *stream) {

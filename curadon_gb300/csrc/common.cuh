@@ -144,6 +144,8 @@ struct Prob2d {
     float2 *layA, *layB, *sinoP;
     int W, H, det, nangles, pa, pb;
     float sx, sy, ox, oy, ds;
+    cudaTextureObject_t tex;  // the plan's volume texture (texture forward)
+    cudaArray_t arr;          // and its array
 };
 
 struct Plan3d {
@@ -255,6 +257,9 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
 int launch_forward2d_tex_views(const Plan2d &p, float *sino, int v0, int nv, cudaStream_t s);
 // Copies the volume into the plan's 2D texture array.
 int load_vol_texture(Plan2d &p, const float *vol, cudaStream_t s);
+int ensure_vol_texture(Plan2d &p);
+int launch_batch2d_fwd_tex(const Prob2d *d_probs, const std::vector<Prob2d> &probs,
+                           const int *starts, int total, cudaStream_t s);
 int launch_forward2d_tex(Plan2d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_forward2d_hyb(Plan2d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t s);

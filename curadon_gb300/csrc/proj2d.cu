@@ -995,14 +995,16 @@ __global__ void __launch_bounds__(256)
     relayout_sino2d_elem(q.sino, q.det, q.nangles, q.sinoP, idx);
 }
 
-__global__ void __launch_bounds__(256)
+// The staged tile of the single-problem default (packed rows, round-down
+// floor, cp.async windows), so results equal it bit for bit.
+__global__ void __launch_bounds__(256, 4)
     k_batch_bwd2d(const Prob2d *__restrict__ probs, const int *__restrict__ start, int count) {
     const int i = batch_problem(start, count, blockIdx.x);
     const Prob2d &q = probs[i];
     const int local = blockIdx.x - start[i];
     const int gx = (q.W + 31) / 32;
-    bwd2d_smem_tile<false>(q.vol, q.sinoP, q.bproj, q.W, q.H, q.det, q.nangles, q.sx, q.sy, q.ox,
-                           q.oy, q.ds, local % gx, local / gx);
+    bwd2d_smem_tile<true, true, 2, true>(q.vol, q.sinoP, q.bproj, q.W, q.H, q.det, q.nangles,
+                                         q.sx, q.sy, q.ox, q.oy, q.ds, local % gx, local / gx);
 }
 
 }  // namespace

@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cstring>
+#include <vector>
 
 #include "common.cuh"
 
@@ -61,14 +62,13 @@ namespace {
 
 // ------------------------------------------------------------ 2D forward
 
-__global__ void __launch_bounds__(256)
-    k_fwd2d_tex(cudaTextureObject_t tex, float *__restrict__ sino,
-                const float2 *__restrict__ tsrc, const float2 *__restrict__ tu0,
-                const float2 *__restrict__ tdu, int W, int H, int det, int nangles, float sx,
-                float sy) {
-    const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    const int view = blockIdx.y * blockDim.y + threadIdx.y;
-    if (u >= det || view >= nangles) return;
+// Ray (u, view) of the reference's 2D forward (forward_2d.hpp:21-79) through
+// the texture unit.
+__device__ __forceinline__ void fwd2d_tex_ray(cudaTextureObject_t tex, float *__restrict__ sino,
+                                              const float2 *__restrict__ tsrc,
+                                              const float2 *__restrict__ tu0,
+                                              const float2 *__restrict__ tdu, int W, int H,
+                                              int det, float sx, float sy, int u, int view) {
     const float2 s = tsrc[view], o = tu0[view], du = tdu[view];
     const float fu = (float)u;
     const float dx = fmaf(du.x, fu, o.x);
@@ -103,6 +103,36 @@ __global__ void __launch_bounds__(256)
         y += vy;
     }
     *out = acc * hypotf(vx * sx, vy * sy);
+}
+
+__global__ void __launch_bounds__(256)
+    k_fwd2d_tex(cudaTextureObject_t tex, float *__restrict__ sino,
+                const float2 *__restrict__ tsrc, const float2 *__restrict__ tu0,
+                const float2 *__restrict__ tdu, int W, int H, int det, int nangles, float sx,
+                float sy) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    const int view = blockIdx.y * blockDim.y + threadIdx.y;
+    if (u >= det || view >= nangles) return;
+    fwd2d_tex_ray(tex, sino, tsrc, tu0, tdu, W, H, det, sx, sy, u, view);
+}
+
+// Many problems' texture forwards in one launch: blocks of 32 cells x 8
+// views over a (problem, tile) work list, each problem with its own texture
+// (bindless handles in the work list).
+__global__ void __launch_bounds__(256)
+    k_batch_fwd2d_tex(const Prob2d *__restrict__ probs, const int *__restrict__ start,
+                      int count) {
+    int lo = 0, hi = count - 1;
+    const int b = blockIdx.x;
+    while (lo < hi) {  // last problem whose first block is <= b
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= b) lo = mid; else hi = mid - 1;
+    }
+    const Prob2d &q = probs[lo];
+    const int t = b - start[lo], tiles_u = (q.det + 31) / 32;
+    const int u = (t % tiles_u) * 32 + threadIdx.x, view = (t / tiles_u) * 8 + threadIdx.y;
+    if (u >= q.det || view >= q.nangles) return;
+    fwd2d_tex_ray(q.tex, q.sino, q.src, q.u0, q.du, q.W, q.H, q.det, q.sx, q.sy, u, view);
 }
 
 // Warps whose (block, warp) index falls in the first `tex_eighths` of every
@@ -387,6 +417,28 @@ int launch_forward2d_tex_views(const Plan2d &p, float *sino, int v0, int nv, cud
     k_fwd2d_tex<<<grid, block, 0, s>>>(p.tex_vol, sino + (size_t)v0 * p.det, p.d_src + v0,
                                        p.d_u0 + v0, p.d_du + v0, p.W, p.H, p.det, nv, p.sx,
                                        p.sy);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
+int ensure_vol_texture(Plan2d &p) {
+    if (!p.arr_vol) {
+        int rc = alloc_array(&p.arr_vol, p.W, p.H, 0, cudaArrayDefault);
+        if (rc) return rc;
+        if ((rc = make_texture(p.arr_vol, &p.tex_vol))) return rc;
+    }
+    return CG_OK;
+}
+
+// Batched texture forward: each problem's volume into its plan's array, then
+// one launch over the work list (stage-1 starts: 32 x 8 cell-view tiles).
+int launch_batch2d_fwd_tex(const Prob2d *d_probs, const std::vector<Prob2d> &probs,
+                           const int *starts, int total, cudaStream_t s) {
+    for (const Prob2d &q : probs)
+        CG_TRY_CUDA(cudaMemcpy2DToArrayAsync(q.arr, 0, 0, q.vol, sizeof(float) * q.W,
+                                             sizeof(float) * q.W, q.H, cudaMemcpyDeviceToDevice,
+                                             s));
+    k_batch_fwd2d_tex<<<total, dim3(32, 8), 0, s>>>(d_probs, starts, (int)probs.size());
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }

@@ -252,7 +252,9 @@ int cg_filter_rows(const float *in, float *out, const float *h, const float *pre
  * of the whole batch then runs as two launches over a (problem, tile) work
  * list instead of two launches per problem: the serving / many-problem entry
  * point, capturable in a CUDA graph because the buffers are bound.  The
- * batched forward is the register ray march (algorithm 0), the batched
+ * batched forward is the texture-unit ray march (algorithm 1, default: one
+ * array copy per problem, then one launch) or the register ray march
+ * (algorithm 0: a re-layout launch and one launch), the batched
  * backprojection the staged one (algorithm 2); results equal cg_forward_2d /
  * cg_backward_2d with those algorithms bit for bit.  A batch must not run
  * concurrently with other calls on its plans.  No counterpart call in the
@@ -265,6 +267,9 @@ int cg_batch2d_destroy(cg_batch2d *batch);
 int cg_batch2d_forward(cg_batch2d *batch, void *stream);
 /* volume_i += A_i^T sinogram_i for every problem */
 int cg_batch2d_backward(cg_batch2d *batch, void *stream);
+/* the batched forward's algorithm: 1 texture unit (default), 0 registers */
+int cg_batch2d_set_forward(cg_batch2d *batch, int algorithm);
+int cg_batch2d_get_forward(const cg_batch2d *batch, int *algorithm);
 
 #ifdef __cplusplus
 }

@@ -2,8 +2,8 @@
 direction for many problems of mixed sizes and geometries.
 
 The batched kernels run the same per-ray / per-tile code as the single-problem
-register forward and staged backprojection, so results must be equal bit for
-bit; CUDA-graph replay of a batch must equal direct calls."""
+texture or register forward and staged backprojection, so results must be
+equal bit for bit; CUDA-graph replay of a batch must equal direct calls."""
 import numpy as np
 import pytest
 import torch
@@ -34,12 +34,12 @@ def mixed_problems(dev, seed=0):
     return geoms, vols, sinos
 
 
-def reference_results(geoms, vols, dev):
+def reference_results(geoms, vols, dev, forward_algo="texture"):
     """Single-problem operators with the batch's algorithms."""
     fw, bw = [], []
     for g, v in zip(geoms, vols):
         p = g._make_plan()
-        p.set_algorithm(forward="registers", backward="shared")
+        p.set_algorithm(forward=forward_algo, backward="shared")
         from curadon_gb300.backend import backward_2d, forward_2d
 
         s = torch.zeros(g.sinogram_shape(), device=dev)
@@ -52,10 +52,12 @@ def reference_results(geoms, vols, dev):
     return fw, bw
 
 
-def test_batch_equals_single_problem_operators(cuda_device):
+@pytest.mark.parametrize("algo", ["texture", "registers"])
+def test_batch_equals_single_problem_operators(cuda_device, algo):
     geoms, vols, sinos = mixed_problems(cuda_device)
-    fw, bw = reference_results(geoms, vols, cuda_device)
-    b = Batch2d(geoms, vols, sinos)
+    fw, bw = reference_results(geoms, vols, cuda_device, algo)
+    b = Batch2d(geoms, vols, sinos, forward=algo)
+    assert b.forward_algorithm == algo
     b.forward()
     torch.cuda.synchronize()
     for s, r in zip(sinos, fw):
@@ -68,11 +70,13 @@ def test_batch_equals_single_problem_operators(cuda_device):
         assert torch.equal(o, r)
 
 
-def test_batch_graph_replay(cuda_device):
-    """A forward + backprojection iteration captured once and replayed."""
+@pytest.mark.parametrize("algo", ["texture", "registers"])
+def test_batch_graph_replay(cuda_device, algo):
+    """A forward + backprojection iteration captured once and replayed (the
+    texture forward's per-problem array copies are captured too)."""
     geoms, vols, sinos = mixed_problems(cuda_device, seed=1)
     outs = [torch.zeros_like(v) for v in vols]
-    bf = Batch2d(geoms, vols, sinos)
+    bf = Batch2d(geoms, vols, sinos, forward=algo)
     bb = Batch2d(geoms, outs, sinos)
     # first calls outside capture (plans and scratch exist by now)
     bf.forward(), bb.backward()
@@ -105,6 +109,8 @@ def test_batch_rejects_bad_input(cuda_device):
         Batch2d([g], [torch.zeros((32, 32), device=cuda_device)], [s])
     with pytest.raises(ValueError):
         Batch2d([], [], [])
+    with pytest.raises(ValueError):
+        Batch2d([g], [v], [s], forward="chunked")
     # the same geometry twice gets a private plan for its second use
     b = Batch2d([g, g], [v, v.clone()], [s, s.clone()])
     b.forward()
