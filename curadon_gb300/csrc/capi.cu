@@ -333,6 +333,9 @@ int make_plan3d(cg_plan3d **out, int device, const uint64_t vol_shape[3], const 
     p->U = (int)det_shape[1], p->V = (int)det_shape[0];
     p->nangles = (int)nangles;
     p->DSO = DSO, p->DSD = DSD;
+    // forward 5: 4 of 8 warps on the texture unit from 300^3 voxels (512^3:
+    // -2 % against 3), 3 below (256^3 and 128^3: -2 % against 4)
+    if ((long long)p->X * p->Y * p->Z >= 27000000LL) p->fwd_tex_warps = 4;
     apply_algo_env(nullptr, p.get());
     Cone c;
     c.shape_f = {{(float)vol_shape[2], (float)vol_shape[1], (float)vol_shape[0]}};

@@ -197,7 +197,8 @@ struct Plan3d {
     // 256^3 and -29 % at 512^3 against backward 0), 1 = runs of 8 at <= 64,
     // 2 / 3 = runs of 16 at <= 80 / 64
     int bwd_axial = 0;
-    // forward 5: warps of each 8 that sample through the texture unit
+    // forward 5: warps of each 8 that sample through the texture unit (4 for
+    // volumes of 300^3 voxels and more, set at plan creation)
     int fwd_tex_warps = 3;
     bool axial = false;  // every backward table's y step is (0, dy, 0)
     // axial backprojection, per view: source -> voxel (0, 0, 0) (3), x step

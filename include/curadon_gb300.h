@@ -173,7 +173,8 @@ int cg_plan3d_destroy(cg_plan3d *plan);
  *             1 texture unit (tex3D), 2 texture unit bilinear per layer +
  *             FP32 lerp across layers, 3 shared-memory slabs (FP32),
  *             4 quads (FP32 trilinear, two 16-byte loads per sample),
- *             5 quads with 3 of every 8 warps on the texture unit (default)
+ *             5 quads with 3 of every 8 warps (4 from 300^3 voxels) on the
+ *             texture unit (default)
  *   backward: 0 registers (voxel runs along z), 1 runs along y when every
  *             view maps the volume's y axis onto the detector's v axis
  *             (circular orbits without detector tilt; default), else 0.
