@@ -265,6 +265,9 @@ int launch_forward2d_tex(Plan2d &p, const float *vol, float *sino, cudaStream_t 
 int launch_forward2d_hyb(Plan2d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t s);
 int launch_forward3d_tex(Plan3d &p, const float *vol, float *sino, cudaStream_t s);
+// texture forward, trilinear (tex3D) or layered bilinear + FP32 lerp
+int launch_forward3d_texture(Plan3d &p, const float *vol, float *sino, cudaStream_t s,
+                             bool trilinear);
 int upload_volume_texture3(Plan3d &p, const float *vol, cudaStream_t s);
 
 // Reads CURADON_GB300_ALGO ("fwd2d=tex,bwd2d=smem,fwd3d=tex2l,...") over the

@@ -930,7 +930,8 @@ int launch_forward3d(const Plan3d &p, const float *vol, float *sino, cudaStream_
 
 int launch_forward3d_quad(Plan3d &p, const float *vol, float *sino, cudaStream_t s) {
     const size_t n = (size_t)(p.X + kQP) * (p.Y + kQP) * (p.Z + kQP);
-    if (n >= (1ull << 32)) return set_error(CG_ERR_INVALID, "volume too large for forward 4");
+    // the kernel's offsets are 32-bit: larger volumes take the texture unit
+    if (n >= (1ull << 32)) return launch_forward3d_texture(p, vol, sino, s, true);
     if (!p.d_volQA) {
         CG_TRY_CUDA(cudaMalloc(&p.d_volQA, n * sizeof(float4)));
         CG_TRY_CUDA(cudaMalloc(&p.d_volQB, n * sizeof(float4)));

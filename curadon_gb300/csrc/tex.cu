@@ -519,10 +519,15 @@ int upload_volume_texture3(Plan3d &p, const float *vol, cudaStream_t s) {
 }
 
 int launch_forward3d_tex(Plan3d &p, const float *vol, float *sino, cudaStream_t s) {
+    return launch_forward3d_texture(p, vol, sino, s, p.algo_fwd == 1);
+}
+
+int launch_forward3d_texture(Plan3d &p, const float *vol, float *sino, cudaStream_t s,
+                             bool trilinear) {
     const dim3 block(p.fwd_bx, p.fwd_by, p.fwd_bz);
     const dim3 grid(ceil_div(p.U, p.fwd_bx), ceil_div(p.V, p.fwd_by), ceil_div(p.nangles, p.fwd_bz));
     if (grid.z > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
-    if (p.algo_fwd == 1) {
+    if (trilinear) {
         if (!p.arr3) {
             int rc = alloc_array(&p.arr3, p.X, p.Y, p.Z, cudaArrayDefault);
             if (rc) return rc;
