@@ -121,15 +121,36 @@ __global__ void k_fold2d(float *__restrict__ vol, const float2 *__restrict__ A,
 // voxels (a, b), (a + 1, b), (a, b + 1), (a + 1, b + 1) of slice c as one
 // float4, so a sample is two 16-byte atomics instead of four 8-byte ones
 // (the scatter is bound by the L2's atomic operations).
-template <bool QUAD>
+// BAND: blocks of 32 x 8 cells of one view in a linear grid ordered cells,
+// then views, then bands of 8 detector rows, each warp on an 8 x 4 patch of
+// cells (the quad forward's order): the blocks resident at one time scatter
+// into a slab of the volume's y range, so the atomics stay in L2; otherwise
+// a (U/32, V/8, views) grid of 32 x 8 blocks.
+// MERGE (quads): a sample's upper-slice contribution is held in registers
+// and, when the next sample's lower slice is the same element (the ray
+// advanced one slice within the same row and column), added to it, so the
+// two go out as one atomic.
+template <bool QUAD, bool BAND = false, bool MERGE = false>
 __global__ void __launch_bounds__(256)
     k_adj3d(void *__restrict__ A, void *__restrict__ B, const float *__restrict__ sino,
             const float4 *__restrict__ torg, const float4 *__restrict__ tdu,
             const float4 *__restrict__ tdv, const float4 *__restrict__ tsrc, int X, int Y, int Z,
-            int U, int V) {
-    const int iu = blockIdx.x * blockDim.x + threadIdx.x;
-    const int iv = blockIdx.y * blockDim.y + threadIdx.y;
-    const int view = blockIdx.z;
+            int U, int V, int P, int utiles) {
+    int iu, iv, view;
+    if constexpr (BAND) {
+        const int lin = blockIdx.x;
+        const int ut = lin % utiles, rest = lin / utiles;
+        view = rest % P;
+        const int band = rest / P;
+        const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+        const int lane = tid & 31, warp = tid >> 5;
+        iu = ut * 32 + (warp & 3) * 8 + (lane & 7);
+        iv = band * 8 + (warp >> 2) * 4 + (lane >> 3);
+    } else {
+        iu = blockIdx.x * blockDim.x + threadIdx.x;
+        iv = blockIdx.y * blockDim.y + threadIdx.y;
+        view = blockIdx.z;
+    }
     if (iu >= U || iv >= V) return;
     const float c = sino[((size_t)view * V + iv) * U + iu];
     if (c == 0.f) return;
@@ -171,6 +192,8 @@ __global__ void __launch_bounds__(256)
     const float amax = (float)Na, bmax = (float)Y, cmax = (float)Nc;
     const float lo = -(float)kPad;
     float t = tmin;
+    size_t held_at = ~(size_t)0;  // MERGE: element of the held contribution
+    float4 held = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int k = 0; k <= nsteps + 1; ++k) {
         if (!(t <= tmax)) break;
         const float pa_ = fmaf(da, t, sa), pb_ = fmaf(dy, t, s.y), pc_ = fmaf(dc, t, sc);
@@ -181,7 +204,19 @@ __global__ void __launch_bounds__(256)
         const size_t i00 = ((size_t)((int)fc + kPad) * pb + ((int)fb + kPad)) * pa + ((int)fa + kPad);
         const float c00 = c * (1.f - wb) * (1.f - wc), c10 = c * wb * (1.f - wc);
         const float c01 = c * (1.f - wb) * wc, c11 = c * wb * wc;
-        if constexpr (QUAD) {
+        if constexpr (QUAD && MERGE) {
+            float4 *q = static_cast<float4 *>(L);
+            float4 lower = make_float4(c00 * (1.f - wa), c00 * wa, c10 * (1.f - wa), c10 * wa);
+            const float4 upper =
+                make_float4(c01 * (1.f - wa), c01 * wa, c11 * (1.f - wa), c11 * wa);
+            if (i00 == held_at) {
+                lower.x += held.x, lower.y += held.y, lower.z += held.z, lower.w += held.w;
+            } else if (held_at != ~(size_t)0) {
+                atomicAdd(q + held_at, held);
+            }
+            atomicAdd(q + i00, lower);
+            held = upper, held_at = i00 + (size_t)pa * pb;
+        } else if constexpr (QUAD) {
             float4 *q = static_cast<float4 *>(L) + i00;
             atomicAdd(q, make_float4(c00 * (1.f - wa), c00 * wa, c10 * (1.f - wa), c10 * wa));
             atomicAdd(q + (size_t)pa * pb,
@@ -194,6 +229,9 @@ __global__ void __launch_bounds__(256)
             atomicAdd(p00 + (size_t)pa * pb + pa, make_float2(c11 * (1.f - wa), c11 * wa));
         }
         t += h;
+    }
+    if constexpr (QUAD && MERGE) {
+        if (held_at != ~(size_t)0) atomicAdd(static_cast<float4 *>(L) + held_at, held);
     }
 }
 
@@ -268,12 +306,19 @@ int launch_adjoint2d(Plan2d &p, float *vol, const float *sino, cudaStream_t s) {
 
 int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s) {
     if (p.nangles > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
-    dim3 grid(ceil_div(p.U, 32), ceil_div(p.V, 8), p.nangles);
+    const int utiles = ceil_div(p.U, 32);
+    const long long bblocks = (long long)utiles * p.nangles * ceil_div(p.V, 8);
     const long long n = (long long)p.X * p.Y * p.Z;
     const size_t elems = (size_t)(p.X + 2 * kPad) * (p.Y + 2 * kPad) * (p.Z + 2 * kPad);
-    // measured: quads are 31 % faster at 128^3 (74 MB of accumulators) and
-    // 2.5 % slower at 256^3 (281 MB), where the atomics spill out of L2
-    const bool quad = p.adj_quad > 0 || (p.adj_quad < 0 && 2 * elems * sizeof(float4) <= (96u << 20));
+    // measured at 128^3 (74 MB of quad accumulators, L2-resident) and 256^3
+    // (281 MB): quads beat pairs at both (3.29 against 4.78 ms; 32.8 against
+    // 47.2 ms); view-major order is best while the accumulators fit in L2,
+    // band-major order (a y-slab of the volume at a time) once they do not
+    // (256^3: 32.8 against 48.3 ms; 128^3: 3.64 against 3.29 ms)
+    const bool quad = p.adj_quad != 0;
+    const bool fits = 2 * elems * (quad ? sizeof(float4) : sizeof(float2)) <= (96u << 20);
+    const bool band = (p.adj_band > 0 || (p.adj_band < 0 && !fits)) && bblocks < (1ll << 31);
+    dim3 grid = band ? dim3((unsigned)bblocks) : dim3(utiles, ceil_div(p.V, 8), p.nangles);
     if (quad) {
         if (!p.d_quadA) {
             CG_TRY_CUDA(cudaMalloc(&p.d_quadA, elems * sizeof(float4)));
@@ -281,8 +326,10 @@ int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s) {
         }
         CG_TRY_CUDA(cudaMemsetAsync(p.d_quadA, 0, elems * sizeof(float4), s));
         CG_TRY_CUDA(cudaMemsetAsync(p.d_quadB, 0, elems * sizeof(float4), s));
-        k_adj3d<true><<<grid, dim3(32, 8), 0, s>>>(p.d_quadA, p.d_quadB, sino, p.d_forg, p.d_fdu,
-                                                   p.d_fdv, p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V);
+        auto kq = p.adj_merge ? (band ? k_adj3d<true, true, true> : k_adj3d<true, false, true>)
+                              : (band ? k_adj3d<true, true> : k_adj3d<true, false>);
+        kq<<<grid, dim3(32, 8), 0, s>>>(p.d_quadA, p.d_quadB, sino, p.d_forg, p.d_fdu, p.d_fdv,
+                                        p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V, p.nangles, utiles);
         CG_TRY_CUDA(cudaGetLastError());
         k_fold3d_quad<<<ceil_div(n, 256), 256, 0, s>>>(vol, p.d_quadA, p.d_quadB, p.X, p.Y, p.Z);
         CG_TRY_CUDA(cudaGetLastError());
@@ -290,8 +337,9 @@ int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s) {
     }
     CG_TRY_CUDA(cudaMemsetAsync(p.d_volA, 0, p.volA_elems * sizeof(float2), s));
     CG_TRY_CUDA(cudaMemsetAsync(p.d_volB, 0, p.volB_elems * sizeof(float2), s));
-    k_adj3d<false><<<grid, dim3(32, 8), 0, s>>>(p.d_volA, p.d_volB, sino, p.d_forg, p.d_fdu,
-                                                p.d_fdv, p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V);
+    auto kp = band ? k_adj3d<false, true> : k_adj3d<false, false>;
+    kp<<<grid, dim3(32, 8), 0, s>>>(p.d_volA, p.d_volB, sino, p.d_forg, p.d_fdu, p.d_fdv,
+                                    p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V, p.nangles, utiles);
     CG_TRY_CUDA(cudaGetLastError());
     k_fold3d<<<ceil_div(n, 256), 256, 0, s>>>(vol, p.d_volA, p.d_volB, p.X, p.Y, p.Z);
     CG_TRY_CUDA(cudaGetLastError());

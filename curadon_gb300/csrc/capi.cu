@@ -69,7 +69,9 @@ void free_plan3d(Plan3d *p) {
 // mixed; fwd3d_tex = 0..8 (texture warps of 8 in forward 5);
 // fwd3d_block = BXxBYxBZ;
 // bwd3d = scalar | pk | pkmagic | quad (backward 0) | ax8m5 | ax8 | ax16 |
-// ax16m4 (backward 1); adj3d = pair | quad.  Unknown tokens are
+// ax16m4 (backward 1); adj3d = pair | quad; adj3d_order = band | view;
+// adj3d_merge = 0 | 1.
+// Unknown tokens are
 // ignored; without the variable every plan starts at the measured defaults.
 void apply_algo_env(Plan2d *p2, Plan3d *p3) {
     const char *env = std::getenv("CURADON_GB300_ALGO");
@@ -138,6 +140,14 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
                 if (val == general[i]) p3->algo_bwd = 0, p3->bwd_packed = i;
                 if (val == runs[i]) p3->algo_bwd = 1, p3->bwd_axial = i;
             }
+        }
+        if (p3 && key == "adj3d_merge") {
+            if (val == "0") p3->adj_merge = false;
+            if (val == "1") p3->adj_merge = true;
+        }
+        if (p3 && key == "adj3d_order") {
+            if (val == "view") p3->adj_band = 0;
+            if (val == "band") p3->adj_band = 1;
         }
         if (p3 && key == "adj3d") {
             if (val == "pair") p3->adj_quad = 0;

@@ -127,3 +127,22 @@ def test_adjoint_accumulates(cuda_device):
     adjoint(y, b, geom)
     torch.cuda.synchronize()
     assert torch.allclose(b, a + 1.0, rtol=1e-6, atol=1e-5)
+
+
+@pytest.mark.parametrize("variant", ["adj3d_merge=1", "adj3d_order=band",
+                                     "adj3d_order=band,adj3d_merge=1",
+                                     "adj3d=pair,adj3d_order=band", "adj3d=pair"])
+def test_dot_product_3d_scatter_variants(cuda_device, monkeypatch, variant):
+    """Every shape of the 3D scatter (accumulators, block order, merged slice
+    atomics; CURADON_GB300_ALGO) is the transpose of the quad forward."""
+    g = cone_config(40, 36, 64)
+    monkeypatch.setenv("CURADON_GB300_ALGO", variant)
+    geom = ConeGeometry(**g)
+    geom.exact_plan
+    monkeypatch.delenv("CURADON_GB300_ALGO")
+    rng = np.random.default_rng(8)
+    x = rng.uniform(0, 1, (40, 40, 40)).astype(np.float32)
+    y = rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32)
+    e = dot_test(geom, x, y, cuda_device)
+    print(f"{variant}: dot-test relative error {e:.2e}")
+    assert e < 1e-5
