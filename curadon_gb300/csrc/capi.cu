@@ -100,8 +100,9 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
                 p2->algo_fwd = 4;
                 // chunk shapes: 4 (rows x 512-pair rows, 256-cell bundles), 104 / 108
                 // (4 / 8 rows, 128-cell bundles), 204 / 304 / 308 (packed sums),
-                // 404 / 408 (packed sums and pair reuse)
-                for (int k : {4, 104, 108, 204, 304, 308, 404, 408})
+                // 404 / 408 (packed sums and pair reuse), 414 / 418 / 428 (the
+                // same with 2 threads per cell, each on 2 of the 4 views)
+                for (int k : {4, 104, 108, 204, 304, 308, 404, 408, 414, 418, 428})
                     if (val == "cslab" + std::to_string(k)) p2->fwd_chunk_rows = k;
             }
             for (int k = 1; k < 8; ++k)

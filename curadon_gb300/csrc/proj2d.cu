@@ -464,8 +464,8 @@ struct RowAcc {
 // stepping towards smaller rows are summed in reverse), so the matched
 // adjoint is this forward's transpose up to the order of summation.  A chunk
 // whose window does not fit reads global memory.
-template <int K, int S, int T, bool PK, bool REUSE = false>
-__global__ void __launch_bounds__(T)
+template <int K, int S, int T, bool PK, bool REUSE = false, int VS = 1>
+__global__ void __launch_bounds__(T * VS)
     k_fwd2d_cslab(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
                   float *__restrict__ sino, const float2 *__restrict__ tsrc,
                   const float2 *__restrict__ tu0, const float2 *__restrict__ tdu, int W, int H,
@@ -481,8 +481,15 @@ __global__ void __launch_bounds__(T)
     const int pitch = cls_y ? pa : pb;
     const int qmax = cls_y ? H : W;
     const int pmaxi = cls_y ? W : H;
+    // VS = 2: 2T threads, each on 2 of the bundle's 4 views; a warp holds 16
+    // adjacent cells of two views, so one shared load spans half the columns
+    // of 32 adjacent cells (fewer bank conflicts)
+    constexpr int NT = T * VS, GV = kCs2G / VS;
+    static_assert(VS == 1 || (VS == 2 && kCs2G % 2 == 0), "view split of 1 or 2");
+    const int cell = VS == 1 ? (int)threadIdx.x : (int)((threadIdx.x >> 5) * 16 + (threadIdx.x & 15));
+    const int gb = VS == 1 ? 0 : (int)((threadIdx.x >> 4) & 1) * GV;
     const int u0 = blockIdx.x * T, v0 = blockIdx.y * kCs2G;
-    const int u = u0 + threadIdx.x;
+    const int u = u0 + cell;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
     if (threadIdx.x == 0) s_rmin = INT_MAX, s_rmax = INT_MIN;
@@ -502,13 +509,13 @@ __global__ void __launch_bounds__(T)
         s_cor[threadIdx.x][1] = b;
     }
     // per ray: column at its first row (p), step per row (V), row sums
-    float p[kCs2G], V[kCs2G];
-    RowAcc<PK> acc[kCs2G];
-    int rlo[kCs2G], len[kCs2G];
+    float p[GV], V[GV];
+    RowAcc<PK> acc[GV];
+    int rlo[GV], len[GV];
     int my_min = INT_MAX, my_max = INT_MIN;
 #pragma unroll
-    for (int g = 0; g < kCs2G; ++g) {
-        const int view = v0 + g;
+    for (int g = 0; g < GV; ++g) {
+        const int view = v0 + gb + g;
         acc[g].zero(), len[g] = 0, rlo[g] = 0, p[g] = V[g] = 0.f;
         if (view >= nangles || u >= det) continue;
         FanRay r;
@@ -531,7 +538,7 @@ __global__ void __launch_bounds__(T)
     const int rmin = s_rmin, rmax = s_rmax;
     const int nch = rmin <= rmax ? (rmax - rmin) / K + 1 : 0;
     {
-        for (int ci = threadIdx.x; ci < min(nch, kCs2MaxChunks); ci += T) {
+        for (int ci = threadIdx.x; ci < min(nch, kCs2MaxChunks); ci += NT) {
             const float ra = (float)(rmin + ci * K), rb = ra + (float)K;
             float lo = FLT_MAX, hi = -FLT_MAX;
 #pragma unroll
@@ -560,7 +567,7 @@ __global__ void __launch_bounds__(T)
         if (win < 0) return;
         const int c0 = win >> 16, wx = win & 0xffff, r0 = rmin + ci * K;
         float2 *base = cwin + buf * kBuf;
-        for (int row = warp; row <= K; row += T / 32) {
+        for (int row = warp; row <= K; row += NT / 32) {
             const int q = min(r0 + row, qmax + 1);
             const float2 *src = lay + (size_t)(q + kPad) * pitch + c0;
             float2 *dst = base + row * S;
@@ -585,7 +592,7 @@ __global__ void __launch_bounds__(T)
             const unsigned cmax = (unsigned)(wx - 1);
             const float2 *b0 = cwin + (ci & 1) * kBuf;
 #pragma unroll
-            for (int g = 0; g < kCs2G; ++g) {
+            for (int g = 0; g < GV; ++g) {
                 const int rel = r0 - rlo[g];
                 if (rel >= 0 && rel + K <= len[g]) {
                     // REUSE: row k's lower pair is row k-1's upper pair when the
@@ -623,7 +630,7 @@ __global__ void __launch_bounds__(T)
         } else {
             const unsigned gcap = (unsigned)(pmaxi + kPad);
 #pragma unroll
-            for (int g = 0; g < kCs2G; ++g) {
+            for (int g = 0; g < GV; ++g) {
                 const int ra = max(r0, rlo[g]), rb = min(r0 + K - 1, rlo[g] + len[g] - 1);
                 for (int r = ra; r <= rb; ++r) {
                     const float pf = floorf(p[g]);
@@ -640,8 +647,8 @@ __global__ void __launch_bounds__(T)
     asm volatile("cp.async.wait_group 0;\n" ::);
 
 #pragma unroll
-    for (int g = 0; g < kCs2G; ++g) {
-        const int view = v0 + g;
+    for (int g = 0; g < GV; ++g) {
+        const int view = v0 + gb + g;
         if (view >= nangles || u >= det) continue;
         FanRay r;
         float out;
@@ -668,11 +675,11 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
     if (groups > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     if (std::max(p.pitchA(), p.pitchB()) >= 32768)
         return set_error(CG_ERR_INVALID, "volume too wide for the chunked forward");
-    auto go = [&](auto kernel, int k, int stride, int threads) -> int {
+    auto go = [&](auto kernel, int k, int stride, int cells, int vs = 1) -> int {
         const size_t smem = 2 * sizeof(float2) * (k + 1) * stride;
         if (int rc = ensure_smem_attr((const void *)kernel, (int)smem)) return rc;
-        dim3 grid(ceil_div(p.det, threads), groups, 2);
-        kernel<<<grid, threads, smem, s>>>(p.d_layA, p.d_layB, sino + (size_t)v0 * p.det,
+        dim3 grid(ceil_div(p.det, cells), groups, 2);
+        kernel<<<grid, cells * vs, smem, s>>>(p.d_layA, p.d_layB, sino + (size_t)v0 * p.det,
                                            p.d_src + v0, p.d_u0 + v0, p.d_du + v0, p.W, p.H,
                                            p.det, nv, p.sx, p.sy, p.pitchA(), p.pitchB());
         CG_TRY_CUDA(cudaGetLastError());
@@ -686,6 +693,9 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
         case 304: return go(k_fwd2d_cslab<4, 256, 128, true>, 4, 256, 128);
         case 308: return go(k_fwd2d_cslab<8, 256, 128, true>, 8, 256, 128);
         case 408: return go(k_fwd2d_cslab<8, 256, 128, true, true>, 8, 256, 128);
+        case 418: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2>, 8, 256, 128, 2);
+        case 414: return go(k_fwd2d_cslab<4, 256, 128, true, true, 2>, 4, 256, 128, 2);
+        case 428: return go(k_fwd2d_cslab<8, 512, 256, true, true, 2>, 8, 512, 256, 2);
         case 404: return go(k_fwd2d_cslab<4, 256, 128, true, true>, 4, 256, 128);
         default: return set_error(CG_ERR_INVALID, "unknown chunk shape");
     }

@@ -331,3 +331,22 @@ def test_staged_backprojector_shapes(cuda_device, monkeypatch, shape):
     e = rel_l2(b, oracle.bwd2d(g, sino))
     print(f"shape {shape} bwd rel-L2 {e:.2e}")
     assert e < TOL
+
+
+@pytest.mark.parametrize("shape", [4, 104, 108, 204, 304, 308, 404, 408, 414, 418, 428])
+def test_chunked_forward_shapes(cuda_device, monkeypatch, shape):
+    """Every compiled shape of the chunked forward (CURADON_GB300_ALGO
+    fwd2d=cslab<shape>: rows per chunk, bundle width, packed sums, pair reuse,
+    one or two threads per cell) against the oracle, on a wide detector whose
+    bundles hold rays of both stepping classes."""
+    n, nangles, det = 190, 77, 600
+    g = fan_config(n, nangles, det)
+    monkeypatch.setenv("CURADON_GB300_ALGO", f"fwd2d=cslab{shape}")
+    geom = FanGeometry(**g, device=cuda_device.index or 0)
+    assert geom.plan.algorithm[0] == "chunked"
+    monkeypatch.delenv("CURADON_GB300_ALGO")
+    ph = ellipses_2d(n, 4).numpy()
+    s = run_fwd(geom, ph, cuda_device)
+    e = rel_l2(s, oracle.fwd2d(g, ph))
+    print(f"shape {shape} fwd rel-L2 {e:.2e}")
+    assert e < TOL
