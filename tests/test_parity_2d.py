@@ -350,3 +350,33 @@ def test_chunked_forward_shapes(cuda_device, monkeypatch, shape):
     e = rel_l2(s, oracle.fwd2d(g, ph))
     print(f"shape {shape} fwd rel-L2 {e:.2e}")
     assert e < TOL
+
+
+def test_full_size_backprojection_cross_check(cuda_device):
+    """n=2048 with 2048 views, where the reference's backprojection cannot be
+    run as a check (its chunks race above 1024 views): the default staged
+    backprojector against this library's texture-unit one, an independent
+    kernel with the reference's 8-bit texture weights; and linearity."""
+    n = 2048
+    g = fan_config(n)
+    geom = make(g, cuda_device)
+    rng = np.random.default_rng(2048)
+    s1 = torch.as_tensor(rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32),
+                         device=cuda_device)
+    s2 = torch.as_tensor(rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32),
+                         device=cuda_device)
+    b1 = torch.zeros((n, n), device=cuda_device)
+    backward(s1, b1, geom)
+    other = make(g, cuda_device)
+    other.plan.set_algorithm(backward="texture")
+    bt = torch.zeros_like(b1)
+    backward(s1, bt, other)
+    b12 = torch.zeros_like(b1)
+    backward(2 * s1 - s2, b12, geom)
+    b2 = torch.zeros_like(b1)
+    backward(s2, b2, geom)
+    torch.cuda.synchronize()
+    e = rel_l2(b1.cpu(), bt.cpu())
+    print(f"n=2048 staged vs texture bwd rel-L2 {e:.2e} max-abs {max_abs(b1.cpu(), bt.cpu()):.2e}")
+    assert e < TOL
+    assert rel_l2(b12.cpu(), (2 * b1 - b2).cpu()) < 1e-5

@@ -100,7 +100,8 @@ def test_forward_algorithms(cuda_device, algo, shape, nangles, det):
     check_fwd(s, oracle.fwd3d(g, ph, sino0=np.full(geom.sinogram_shape(), SENTINEL)))
 
 
-@pytest.mark.parametrize("n,nangles,det", [(64, 90, 96), (128, 180, 192), (256, 360, 384)])
+@pytest.mark.parametrize("n,nangles,det", [(64, 90, 96), (128, 180, 192), (256, 360, 384),
+                                           (512, 720, 768)])
 def test_against_reference(cuda_device, ref_ops, n, nangles, det):
     g = cone_config(n, nangles, det)
     geom = make(g, cuda_device)
