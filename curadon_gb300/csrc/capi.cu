@@ -101,8 +101,13 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
                 // chunk shapes: 4 (rows x 512-pair rows, 256-cell bundles), 104 / 108
                 // (4 / 8 rows, 128-cell bundles), 204 / 304 / 308 (packed sums),
                 // 404 / 408 (packed sums and pair reuse), 414 / 418 / 428 (the
-                // same with 2 threads per cell, each on 2 of the 4 views)
-                for (int k : {4, 104, 108, 204, 304, 308, 404, 408, 414, 418, 428})
+                // same with 2 threads per cell, each on 2 of the 4 views), 438
+                // (8 views per bundle, 2 threads per cell on 4 each), 448 (16
+                // views per 64-cell bundle, 4 threads per cell on 4 each), 439
+                // (438 at <= 64 registers), 447 (8 views per 64-cell bundle, 4
+                // threads per cell on 2 each)
+                for (int k : {4, 104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438, 439,
+                              440, 447, 448, 449, 450})
                     if (val == "cslab" + std::to_string(k)) p2->fwd_chunk_rows = k;
             }
             for (int k = 1; k < 8; ++k)
@@ -509,9 +514,10 @@ int cg_plan2d_create(cg_plan2d **plan, int device, uint32_t vol_prec, const uint
     p->det = (int)det_count, p->ds = det_spacing, p->doff = det_offset;
     p->nangles = (int)nangles, p->pitch = det_pitch, p->COR = COR;
     p->vol_bits = (int)vol_prec, p->det_bits = (int)det_prec;
-    // measured on GB300 (n-sweep): the chunked forward is 4 % faster than the
-    // texture unit at 2048^2 and 9 % at 4096^2, 6 % slower at 1024^2
-    if ((long long)p->W * p->H >= 1536LL * 1536) p->algo_fwd = 4;
+    // measured on GB300 (n-sweep): the chunked forward (shape 439) is 2.5 %
+    // faster than the texture unit at 1024^2, 9 % at 1280^2, 13 % at 1536^2,
+    // 17 % at 2048^2; 20-44 % slower at 768^2 and below
+    if ((long long)p->W * p->H >= 1024LL * 1024) p->algo_fwd = 4;
     apply_algo_env(p.get(), nullptr);
     int rc = CG_OK;
     auto fail = [&](int code) {
@@ -569,7 +575,7 @@ int cg_plan2d_create_vec(cg_plan2d **plan, int device, uint32_t vol_prec,
     CG_REQUIRE(guard.ok(), "cannot select device");
     p->device = device;
     p->vec = true;
-    if ((long long)p->W * p->H >= 1536LL * 1536) p->algo_fwd = 4;
+    if ((long long)p->W * p->H >= 1024LL * 1024) p->algo_fwd = 4;
     apply_algo_env(p.get(), nullptr);
     p->algo_bwd = 2;  // the staged backprojector is the one driven by the projective table
     int rc = CG_OK;

@@ -109,7 +109,7 @@ struct Plan2d {
     // share of the views;
     // backprojection 0 = registers, 1 = texture unit, 2 = shared-memory rows.
     // Defaults: the fastest measured on GB300 (2D n-sweep); the forward
-    // becomes chunked for volumes of 1536^2 pixels and more (cg_plan2d_create).
+    // becomes chunked for volumes of 1024^2 pixels and more (cg_plan2d_create).
     int algo_fwd = 1, algo_bwd = 2;
     int tex_eighths = 4;              // hybrid forward: share of warps on the texture unit
     // split forward (algorithm 5): sixteenths of the views projected by the
@@ -120,8 +120,11 @@ struct Plan2d {
     int bwd_split_sixteenths = 3;
     cudaStream_t aux = nullptr;       // internal stream, created on first use
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    int fwd_chunk_rows = 408;         // chunked forward: chunk shape (8 rows, 128-cell
-                                      // bundles, packed sums, pair reuse)
+    // chunked forward: chunk shape; 439 = 8-row chunks, bundles of 8 views x
+    // 128 cells, two threads per cell on 4 views each, packed sums, pair
+    // reuse, <= 64 registers (-11 % at n=2048 and 4096 against 408: the
+    // same with 4-view bundles, one thread per cell)
+    int fwd_chunk_rows = 439;
     // staged backprojector variant: 27 = 4 blocks/SM, packed FP32 pairs of
     // rows, floor taken by FP32 adds, windows copied with cp.async (default,
     // measured fastest); 24 = the same with register copies; 25 / 26 = 24

@@ -464,8 +464,9 @@ struct RowAcc {
 // stepping towards smaller rows are summed in reverse), so the matched
 // adjoint is this forward's transpose up to the order of summation.  A chunk
 // whose window does not fit reads global memory.
-template <int K, int S, int T, bool PK, bool REUSE = false, int VS = 1>
-__global__ void __launch_bounds__(T * VS)
+template <int K, int S, int T, bool PK, bool REUSE = false, int VS = 1, int NG = kCs2G,
+          int MB = 0>
+__global__ void __launch_bounds__(T * VS, MB)
     k_fwd2d_cslab(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
                   float *__restrict__ sino, const float2 *__restrict__ tsrc,
                   const float2 *__restrict__ tu0, const float2 *__restrict__ tdu, int W, int H,
@@ -473,7 +474,7 @@ __global__ void __launch_bounds__(T * VS)
     static_assert(S % 2 == 0, "rows of the window buffers must stay 16-byte aligned");
     constexpr int kBuf = (K + 1) * S;               // pairs per buffer
     extern __shared__ __align__(16) float2 cwin[];  // 2 buffers
-    __shared__ float s_cor[2 * kCs2G][2];            // column = a + b * row
+    __shared__ float s_cor[2 * NG][2];               // column = a + b * row
     __shared__ int s_win[kCs2MaxChunks];             // (first column << 16) | width, or -1
     __shared__ int s_rmin, s_rmax;
     const bool cls_y = blockIdx.z == 0;
@@ -484,17 +485,21 @@ __global__ void __launch_bounds__(T * VS)
     // VS = 2: 2T threads, each on 2 of the bundle's 4 views; a warp holds 16
     // adjacent cells of two views, so one shared load spans half the columns
     // of 32 adjacent cells (fewer bank conflicts)
-    constexpr int NT = T * VS, GV = kCs2G / VS;
-    static_assert(VS == 1 || (VS == 2 && kCs2G % 2 == 0), "view split of 1 or 2");
-    const int cell = VS == 1 ? (int)threadIdx.x : (int)((threadIdx.x >> 5) * 16 + (threadIdx.x & 15));
-    const int gb = VS == 1 ? 0 : (int)((threadIdx.x >> 4) & 1) * GV;
-    const int u0 = blockIdx.x * T, v0 = blockIdx.y * kCs2G;
+    constexpr int NT = T * VS, GV = NG / VS;
+    static_assert(VS == 1 || ((VS == 2 || VS == 4) && NG % VS == 0), "view split of 1, 2, 4");
+    static_assert(2 * NG <= 32, "corner lanes within one warp");
+    // VS > 1: a warp holds 16 adjacent cells x 2 view groups; cells advance
+    // every 16 * VS threads
+    const int cell = VS == 1 ? (int)threadIdx.x
+                             : (int)((threadIdx.x / (16 * VS)) * 16 + (threadIdx.x & 15));
+    const int gb = VS == 1 ? 0 : (int)((threadIdx.x >> 4) % VS) * GV;
+    const int u0 = blockIdx.x * T, v0 = blockIdx.y * NG;
     const int u = u0 + cell;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
     if (threadIdx.x == 0) s_rmin = INT_MAX, s_rmax = INT_MIN;
     __syncthreads();
-    if (threadIdx.x < 2 * kCs2G) {  // lanes 2g, 2g + 1: the end cells of view g
+    if (threadIdx.x < 2 * NG) {  // lanes 2g, 2g + 1: the end cells of view g
         const int view = min(v0 + (threadIdx.x >> 1), nangles - 1);
         const int cu = (threadIdx.x & 1) ? min(u0 + T - 1, det - 1) : u0;
         const float2 sv = tsrc[view], o = tu0[view], d = tdu[view];
@@ -502,7 +507,8 @@ __global__ void __launch_bounds__(T * VS)
         // column p (texel coordinate - 1/2) of the ray on row q (the same)
         const float dp = cls_y ? dx : dy, dq = cls_y ? dy : dx;
         const float sp = (cls_y ? sv.x : sv.y) - 0.5f, sq = (cls_y ? sv.y : sv.x) - 0.5f;
-        const float dq_other = __shfl_xor_sync(0xffu, dq, 1);
+        constexpr unsigned kCorners = 2 * NG == 32 ? 0xffffffffu : (1u << (2 * NG)) - 1u;
+        const float dq_other = __shfl_xor_sync(kCorners, dq, 1);
         const float b = (dq > 0.f) != (dq_other > 0.f) ? ((threadIdx.x & 1) ? 1.f : -1.f)
                                                         : fminf(fmaxf(dp / dq, -1.f), 1.f);
         s_cor[threadIdx.x][0] = sp - sq * b;
@@ -542,7 +548,7 @@ __global__ void __launch_bounds__(T * VS)
             const float ra = (float)(rmin + ci * K), rb = ra + (float)K;
             float lo = FLT_MAX, hi = -FLT_MAX;
 #pragma unroll
-            for (int c = 0; c < 2 * kCs2G; ++c) {
+            for (int c = 0; c < 2 * NG; ++c) {
                 const float c0 = fmaf(s_cor[c][1], ra, s_cor[c][0]);
                 const float c1 = fmaf(s_cor[c][1], rb, s_cor[c][0]);
                 lo = fminf(lo, fminf(c0, c1));
@@ -671,7 +677,10 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
     // views [v0, v0 + nv): the kernel sees offset tables and sinogram rows
     if (nv < 0) nv = p.nangles - v0;
     if (nv <= 0) return CG_OK;
-    const int groups = ceil_div(nv, kCs2G);
+    const int ng = rows == 438 || rows == 439 || rows == 440 || rows == 447 ? 8
+                   : rows == 448 || rows == 449 || rows == 450   ? 16
+                                                                 : kCs2G;  // views per bundle
+    const int groups = ceil_div(nv, ng);
     if (groups > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     if (std::max(p.pitchA(), p.pitchB()) >= 32768)
         return set_error(CG_ERR_INVALID, "volume too wide for the chunked forward");
@@ -696,6 +705,13 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
         case 418: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2>, 8, 256, 128, 2);
         case 414: return go(k_fwd2d_cslab<4, 256, 128, true, true, 2>, 4, 256, 128, 2);
         case 428: return go(k_fwd2d_cslab<8, 512, 256, true, true, 2>, 8, 512, 256, 2);
+        case 438: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8>, 8, 256, 128, 2);
+        case 448: return go(k_fwd2d_cslab<8, 256, 64, true, true, 4, 16>, 8, 256, 64, 4);
+        case 439: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 4>, 8, 256, 128, 2);
+        case 447: return go(k_fwd2d_cslab<8, 256, 64, true, true, 4, 8>, 8, 256, 64, 4);
+        case 440: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 5>, 8, 256, 128, 2);
+        case 449: return go(k_fwd2d_cslab<8, 256, 64, true, true, 4, 16, 3>, 8, 256, 64, 4);
+        case 450: return go(k_fwd2d_cslab<8, 256, 128, true, true, 4, 16, 2>, 8, 256, 128, 4);
         case 404: return go(k_fwd2d_cslab<4, 256, 128, true, true>, 4, 256, 128);
         default: return set_error(CG_ERR_INVALID, "unknown chunk shape");
     }
