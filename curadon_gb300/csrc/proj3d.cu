@@ -892,6 +892,20 @@ __global__ void __launch_bounds__(256, MINB)
 
 // ------------------------------------------------------------ launchers
 
+// cudaMalloc that reports an out-of-memory failure as false (clearing the
+// error) and other failures as a thrown status through *rc.
+static bool try_malloc_or_oom(void **ptr, size_t bytes, int *rc) {
+    const cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e == cudaSuccess) return true;
+    *ptr = nullptr;
+    if (e == cudaErrorMemoryAllocation) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    *rc = set_error(CG_ERR_CUDA, cudaGetErrorString(e));
+    return false;
+}
+
 int ensure_plan3d_scratch(Plan3d &p, bool fwd, bool bwd) {
     if (fwd && !p.d_volA) {
         const size_t n = (size_t)(p.X + 2 * kP3) * (p.Y + 2 * kP3) * (p.Z + 2 * kP3);
@@ -903,9 +917,16 @@ int ensure_plan3d_scratch(Plan3d &p, bool fwd, bool bwd) {
         // one of the two re-laid projections, as the plan's variant reads it
         const size_t n = (size_t)(p.U + 2 * kP3) * (p.V + 2 * kP3) * p.nangles;
         p.sinoP_elems = n;
-        const bool quads = p.reads_quads();
-        if (quads && !p.d_sinoQ) CG_TRY_CUDA(cudaMalloc(&p.d_sinoQ, n * sizeof(float4)));
-        if (!quads && !p.d_sinoP)
+        if (p.reads_quads() && !p.d_sinoQ) {
+            int rc = CG_OK;
+            if (!try_malloc_or_oom((void **)&p.d_sinoQ, n * sizeof(float4), &rc)) {
+                if (rc) return rc;
+                // no room for the 16-byte quads: the general kernel on 8-byte
+                // pairs (half the memory) from now on
+                p.algo_bwd = 0, p.bwd_packed = 2;
+            }
+        }
+        if (!p.reads_quads() && !p.d_sinoP)
             CG_TRY_CUDA(cudaMalloc(&p.d_sinoP, n * sizeof(float2)));
     }
     return CG_OK;
@@ -933,8 +954,23 @@ int launch_forward3d_quad(Plan3d &p, const float *vol, float *sino, cudaStream_t
     // the kernel's offsets are 32-bit: larger volumes take the texture unit
     if (n >= (1ull << 32)) return launch_forward3d_texture(p, vol, sino, s, true);
     if (!p.d_volQA) {
-        CG_TRY_CUDA(cudaMalloc(&p.d_volQA, n * sizeof(float4)));
-        CG_TRY_CUDA(cudaMalloc(&p.d_volQB, n * sizeof(float4)));
+        int rc = CG_OK;
+        if (!try_malloc_or_oom((void **)&p.d_volQA, n * sizeof(float4), &rc) ||
+            !try_malloc_or_oom((void **)&p.d_volQB, n * sizeof(float4), &rc)) {
+            if (p.d_volQA) cudaFree(p.d_volQA);
+            p.d_volQA = nullptr;
+            if (rc) return rc;
+            // no room for the two quad copies: algorithm 4 continues as the
+            // register forward (the same samples and weights, 8-byte pair
+            // copies), algorithm 5 as the texture forward
+            if (p.algo_fwd == 4) {
+                p.algo_fwd = 0;
+                if ((rc = ensure_plan3d_scratch(p, true, false))) return rc;
+                return launch_forward3d(p, vol, sino, s);
+            }
+            p.algo_fwd = 1;
+            return launch_forward3d_texture(p, vol, sino, s, true);
+        }
     }
     k_relayout3d_qa<<<ceil_div((long long)n, 256), 256, 0, s>>>(vol, p.X, p.Y, p.Z, p.d_volQA);
     CG_TRY_CUDA(cudaGetLastError());

@@ -257,3 +257,40 @@ def test_forward_quad_variants(cuda_device, monkeypatch, variant):
     ph = ellipsoids_3d(shape, 5).numpy()
     s = run_fwd(geom, ph, cuda_device)
     check_fwd(s, oracle.fwd3d(g, ph, sino0=np.full(geom.sinogram_shape(), SENTINEL)))
+
+
+def test_quad_buffers_fall_back_when_memory_is_short(cuda_device):
+    """With the device nearly full, the default forward (mixed quads) and
+    backprojection (axial quads) cannot allocate their 16-byte quad copies:
+    the forward continues on the texture unit and the backprojection on the
+    general kernel with 8-byte pairs, with the same results (no out-of-memory
+    error)."""
+    n, nangles, det = 96, 64, 128
+    g = cone_config(n, nangles, det)
+    ph = ellipsoids_3d(n, 6).numpy()
+    ref_geom = make(g, cuda_device)
+    s_ref = run_fwd(ref_geom, ph, cuda_device)
+    sin = np.where(s_ref == SENTINEL, 0.0, s_ref).astype(np.float32)
+    b_ref = run_bwd(ref_geom, sin, cuda_device, np.zeros(ph.shape, np.float32))
+
+    geom = make(g, cuda_device)
+    v = torch.as_tensor(ph, device=cuda_device).contiguous()
+    s = torch.full(geom.sinogram_shape(), SENTINEL, device=cuda_device)
+    b = torch.zeros_like(v)
+    st = torch.as_tensor(sin, device=cuda_device)
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    free, _ = torch.cuda.mem_get_info()
+    # leave about 24 MB: room for the texture array and the pair copies, not
+    # for the quad copies (2 x 33 MB) or the projection quads (18 MB)
+    filler = torch.empty(max(0, free - (24 << 20)), dtype=torch.uint8, device=cuda_device)
+    try:
+        forward(v, s, geom)
+        backward(st, b, geom)
+        torch.cuda.synchronize()
+    finally:
+        del filler
+        torch.cuda.empty_cache()
+    assert geom.plan.algorithm == ("texture", "registers")
+    check_fwd(s.cpu().numpy(), s_ref)
+    assert rel_l2(b.cpu().numpy(), b_ref) < TOL
