@@ -104,10 +104,11 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
                 // same with 2 threads per cell, each on 2 of the 4 views), 438
                 // (8 views per bundle, 2 threads per cell on 4 each), 448 (16
                 // views per 64-cell bundle, 4 threads per cell on 4 each), 439
-                // (438 at <= 64 registers), 447 (8 views per 64-cell bundle, 4
-                // threads per cell on 2 each)
+                // (438 at <= 64 registers), 441 (439 with half-warps of 8 cells x
+                // 2 view groups), 447 (8 views per 64-cell bundle, 4 threads per
+                // cell on 2 each)
                 for (int k : {4, 104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438, 439,
-                              440, 447, 448, 449, 450})
+                              440, 441, 447, 448, 449, 450})
                     if (val == "cslab" + std::to_string(k)) p2->fwd_chunk_rows = k;
             }
             for (int k = 1; k < 8; ++k)
@@ -516,7 +517,8 @@ int cg_plan2d_create(cg_plan2d **plan, int device, uint32_t vol_prec, const uint
     p->vol_bits = (int)vol_prec, p->det_bits = (int)det_prec;
     // measured on GB300 (n-sweep): the chunked forward (shape 439) is 2.5 %
     // faster than the texture unit at 1024^2, 9 % at 1280^2, 13 % at 1536^2,
-    // 17 % at 2048^2; 20-44 % slower at 768^2 and below
+    // 17 % at 2048^2 (shape 441: another 4 %); 20-44 % slower at 768^2 and
+    // below
     if ((long long)p->W * p->H >= 1024LL * 1024) p->algo_fwd = 4;
     apply_algo_env(p.get(), nullptr);
     int rc = CG_OK;

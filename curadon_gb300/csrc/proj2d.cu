@@ -465,7 +465,7 @@ struct RowAcc {
 // adjoint is this forward's transpose up to the order of summation.  A chunk
 // whose window does not fit reads global memory.
 template <int K, int S, int T, bool PK, bool REUSE = false, int VS = 1, int NG = kCs2G,
-          int MB = 0>
+          int MB = 0, int MAP = 0>
 __global__ void __launch_bounds__(T * VS, MB)
     k_fwd2d_cslab(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
                   float *__restrict__ sino, const float2 *__restrict__ tsrc,
@@ -490,9 +490,16 @@ __global__ void __launch_bounds__(T * VS, MB)
     static_assert(2 * NG <= 32, "corner lanes within one warp");
     // VS > 1: a warp holds 16 adjacent cells x 2 view groups; cells advance
     // every 16 * VS threads
+    // MAP = 1 (VS = 2): each half-warp holds 8 cells x 2 view groups, so the
+    // 64-bit shared loads of one half span ~8 columns (no bank conflicts)
+    static_assert(MAP == 0 || VS == 2, "the half-warp map is for two threads per cell");
     const int cell = VS == 1 ? (int)threadIdx.x
-                             : (int)((threadIdx.x / (16 * VS)) * 16 + (threadIdx.x & 15));
-    const int gb = VS == 1 ? 0 : (int)((threadIdx.x >> 4) % VS) * GV;
+                     : MAP == 1 ? (int)((threadIdx.x >> 5) * 16 + (threadIdx.x & 7) +
+                                        8 * ((threadIdx.x >> 4) & 1))
+                                : (int)((threadIdx.x / (16 * VS)) * 16 + (threadIdx.x & 15));
+    const int gb = VS == 1     ? 0
+                   : MAP == 1 ? (int)((threadIdx.x >> 3) & 1) * GV
+                              : (int)((threadIdx.x >> 4) % VS) * GV;
     const int u0 = blockIdx.x * T, v0 = blockIdx.y * NG;
     const int u = u0 + cell;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -677,7 +684,7 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
     // views [v0, v0 + nv): the kernel sees offset tables and sinogram rows
     if (nv < 0) nv = p.nangles - v0;
     if (nv <= 0) return CG_OK;
-    const int ng = rows == 438 || rows == 439 || rows == 440 || rows == 447 ? 8
+    const int ng = rows == 438 || rows == 439 || rows == 440 || rows == 441 || rows == 447 ? 8
                    : rows == 448 || rows == 449 || rows == 450   ? 16
                                                                  : kCs2G;  // views per bundle
     const int groups = ceil_div(nv, ng);
@@ -710,6 +717,7 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
         case 439: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 4>, 8, 256, 128, 2);
         case 447: return go(k_fwd2d_cslab<8, 256, 64, true, true, 4, 8>, 8, 256, 64, 4);
         case 440: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 5>, 8, 256, 128, 2);
+        case 441: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 4, 1>, 8, 256, 128, 2);
         case 449: return go(k_fwd2d_cslab<8, 256, 64, true, true, 4, 16, 3>, 8, 256, 64, 4);
         case 450: return go(k_fwd2d_cslab<8, 256, 128, true, true, 4, 16, 2>, 8, 256, 128, 4);
         case 404: return go(k_fwd2d_cslab<4, 256, 128, true, true>, 4, 256, 128);
