@@ -105,10 +105,11 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
                 // (8 views per bundle, 2 threads per cell on 4 each), 448 (16
                 // views per 64-cell bundle, 4 threads per cell on 4 each), 439
                 // (438 at <= 64 registers), 441 (439 with half-warps of 8 cells x
-                // 2 view groups), 447 (8 views per 64-cell bundle, 4 threads per
-                // cell on 2 each)
+                // 2 view groups), 442 / 443 (441 with 12 / 16-row chunks), 444 (443
+                // with 192-pair windows at <= 64 registers), 447 (8
+                // views per 64-cell bundle, 4 threads per cell on 2 each)
                 for (int k : {4, 104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438, 439,
-                              440, 441, 447, 448, 449, 450})
+                              440, 441, 442, 443, 444, 447, 448, 449, 450})
                     if (val == "cslab" + std::to_string(k)) p2->fwd_chunk_rows = k;
             }
             for (int k = 1; k < 8; ++k)

@@ -120,11 +120,11 @@ struct Plan2d {
     int bwd_split_sixteenths = 3;
     cudaStream_t aux = nullptr;       // internal stream, created on first use
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    // chunked forward: chunk shape; 441 = 8-row chunks, bundles of 8 views x
-    // 128 cells, two threads per cell on 4 views each, each half-warp on 8
-    // cells x 2 view groups, packed sums, pair reuse, <= 64 registers (-15 %
-    // at n=2048 against 408: 4-view bundles, one thread per cell)
-    int fwd_chunk_rows = 441;
+    // chunked forward: chunk shape; 443 = 16-row chunks, bundles of 8 views
+    // x 128 cells, two threads per cell on 4 views each, each half-warp on 8
+    // cells x 2 view groups, packed sums, pair reuse, 3 blocks/SM (-16 % at
+    // n=2048 against 408: 8-row chunks, 4-view bundles, one thread per cell)
+    int fwd_chunk_rows = 443;
     // staged backprojector variant: 27 = 4 blocks/SM, packed FP32 pairs of
     // rows, floor taken by FP32 adds, windows copied with cp.async (default,
     // measured fastest); 24 = the same with register copies; 25 / 26 = 24

@@ -684,7 +684,9 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
     // views [v0, v0 + nv): the kernel sees offset tables and sinogram rows
     if (nv < 0) nv = p.nangles - v0;
     if (nv <= 0) return CG_OK;
-    const int ng = rows == 438 || rows == 439 || rows == 440 || rows == 441 || rows == 447 ? 8
+    const int ng = rows == 438 || rows == 439 || rows == 440 || rows == 441 || rows == 442 ||
+                           rows == 443 || rows == 444 || rows == 447
+                       ? 8
                    : rows == 448 || rows == 449 || rows == 450   ? 16
                                                                  : kCs2G;  // views per bundle
     const int groups = ceil_div(nv, ng);
@@ -718,6 +720,9 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
         case 447: return go(k_fwd2d_cslab<8, 256, 64, true, true, 4, 8>, 8, 256, 64, 4);
         case 440: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 5>, 8, 256, 128, 2);
         case 441: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 4, 1>, 8, 256, 128, 2);
+        case 442: return go(k_fwd2d_cslab<12, 256, 128, true, true, 2, 8, 4, 1>, 12, 256, 128, 2);
+        case 443: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 1>, 16, 256, 128, 2);
+        case 444: return go(k_fwd2d_cslab<16, 192, 128, true, true, 2, 8, 4, 1>, 16, 192, 128, 2);
         case 449: return go(k_fwd2d_cslab<8, 256, 64, true, true, 4, 16, 3>, 8, 256, 64, 4);
         case 450: return go(k_fwd2d_cslab<8, 256, 128, true, true, 4, 16, 2>, 8, 256, 128, 4);
         case 404: return go(k_fwd2d_cslab<4, 256, 128, true, true>, 4, 256, 128);

@@ -334,7 +334,7 @@ def test_staged_backprojector_shapes(cuda_device, monkeypatch, shape):
 
 
 @pytest.mark.parametrize("shape", [4, 104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438,
-                                   439, 440, 441, 447, 448, 449, 450])
+                                   439, 440, 441, 442, 443, 444, 447, 448, 449, 450])
 def test_chunked_forward_shapes(cuda_device, monkeypatch, shape):
     """Every compiled shape of the chunked forward (CURADON_GB300_ALGO
     fwd2d=cslab<shape>: rows per chunk, bundle width, packed sums, pair reuse,
