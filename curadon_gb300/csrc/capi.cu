@@ -64,8 +64,8 @@ void free_plan3d(Plan3d *p) {
 // from CURADON_GB300_ALGO: comma-separated key=value tokens, e.g.
 // "fwd2d=tex,bwd2d_minb=4".  Keys: fwd2d = alu | tex | slab | cslab |
 // cslab<shape> | hyb<1..7> | split<0..16>; bwd2d = alu | tex | smem |
-// split<0..16>; bwd2d_minb = 3 | 4 | 5 | 14 | 24 | 25 | 26 | 27 | 28 (staged
-// backprojector shapes); adj2d = pair | quad; fwd3d = alu | tex3 | tex2l | slab | quad |
+// split<0..16>; bwd2d_minb = 3 | 4 | 5 | 14 | 24 | 25 | 26 | 27 | 28 | 37 | 38
+// (staged backprojector shapes; 37 / 38: 27 / 28 on absolute-position pairs); adj2d = pair | quad; fwd3d = alu | tex3 | tex2l | slab | quad |
 // mixed; fwd3d_tex = 0..8 (texture warps of 8 in forward 5);
 // fwd3d_block = BXxBYxBZ;
 // bwd3d = scalar | pk | pkmagic | quad (backward 0) | ax8m5 | ax8 | ax16 |
@@ -107,9 +107,11 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
                 // (438 at <= 64 registers), 441 (439 with half-warps of 8 cells x
                 // 2 view groups), 442 / 443 (441 with 12 / 16-row chunks), 444 (443
                 // with 192-pair windows at <= 64 registers), 447 (8
-                // views per 64-cell bundle, 4 threads per cell on 2 each)
+                // views per 64-cell bundle, 4 threads per cell on 2 each), 451 / 453
+                // (441 / 443 with interleaved view groups), 463 / 473 (443 / 453
+                // reading absolute-position pairs)
                 for (int k : {4, 104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438, 439,
-                              440, 441, 442, 443, 444, 447, 448, 449, 450})
+                              440, 441, 442, 443, 444, 447, 448, 449, 450, 451, 453, 463, 473})
                     if (val == "cslab" + std::to_string(k)) p2->fwd_chunk_rows = k;
             }
             for (int k = 1; k < 8; ++k)
@@ -128,7 +130,7 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
             if (val == "quad") p2->adj_quad = 1;
         }
         if (p2 && key == "bwd2d_minb")
-            for (int k : {3, 4, 5, 14, 24, 25, 26, 27, 28})
+            for (int k : {3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38})
                 if (val == std::to_string(k)) p2->bwd_min_blocks = k;
         if (p3 && key == "fwd3d") {
             if (val == "alu") p3->algo_fwd = 0;
@@ -516,11 +518,10 @@ int cg_plan2d_create(cg_plan2d **plan, int device, uint32_t vol_prec, const uint
     p->det = (int)det_count, p->ds = det_spacing, p->doff = det_offset;
     p->nangles = (int)nangles, p->pitch = det_pitch, p->COR = COR;
     p->vol_bits = (int)vol_prec, p->det_bits = (int)det_prec;
-    // measured on GB300 (n-sweep): the chunked forward (shape 439) is 2.5 %
-    // faster than the texture unit at 1024^2, 9 % at 1280^2, 13 % at 1536^2,
-    // 17 % at 2048^2 (shape 441: another 4 %); 20-44 % slower at 768^2 and
-    // below
-    if ((long long)p->W * p->H >= 1024LL * 1024) p->algo_fwd = 4;
+    // measured on GB300 (n-sweep): the chunked forward (shape 473) is 6 %
+    // faster than the texture unit at 768^2, 13 % at 896^2, 19 % at 1024^2,
+    // 34 % at 2048^2; even at 640^2, 16 % slower at 512^2
+    if ((long long)p->W * p->H >= 768LL * 768) p->algo_fwd = 4;
     apply_algo_env(p.get(), nullptr);
     int rc = CG_OK;
     auto fail = [&](int code) {
@@ -578,7 +579,7 @@ int cg_plan2d_create_vec(cg_plan2d **plan, int device, uint32_t vol_prec,
     CG_REQUIRE(guard.ok(), "cannot select device");
     p->device = device;
     p->vec = true;
-    if ((long long)p->W * p->H >= 1024LL * 1024) p->algo_fwd = 4;
+    if ((long long)p->W * p->H >= 768LL * 768) p->algo_fwd = 4;
     apply_algo_env(p.get(), nullptr);
     p->algo_bwd = 2;  // the staged backprojector is the one driven by the projective table
     int rc = CG_OK;

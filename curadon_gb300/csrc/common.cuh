@@ -109,7 +109,7 @@ struct Plan2d {
     // share of the views;
     // backprojection 0 = registers, 1 = texture unit, 2 = shared-memory rows.
     // Defaults: the fastest measured on GB300 (2D n-sweep); the forward
-    // becomes chunked for volumes of 1024^2 pixels and more (cg_plan2d_create).
+    // becomes chunked for volumes of 768^2 pixels and more (cg_plan2d_create).
     int algo_fwd = 1, algo_bwd = 2;
     int tex_eighths = 4;              // hybrid forward: share of warps on the texture unit
     // split forward (algorithm 5): sixteenths of the views projected by the
@@ -120,17 +120,21 @@ struct Plan2d {
     int bwd_split_sixteenths = 3;
     cudaStream_t aux = nullptr;       // internal stream, created on first use
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    // chunked forward: chunk shape; 443 = 16-row chunks, bundles of 8 views
-    // x 128 cells, two threads per cell on 4 views each, each half-warp on 8
-    // cells x 2 view groups, packed sums, pair reuse, 3 blocks/SM (-16 % at
-    // n=2048 against 408: 8-row chunks, 4-view bundles, one thread per cell)
-    int fwd_chunk_rows = 443;
-    // staged backprojector variant: 27 = 4 blocks/SM, packed FP32 pairs of
-    // rows, floor taken by FP32 adds, windows copied with cp.async (default,
-    // measured fastest); 24 = the same with register copies; 25 / 26 = 24
+    // chunked forward: chunk shape; 473 = 16-row chunks, bundles of 8 views
+    // x 128 cells, two threads per cell on 4 interleaved views each, each
+    // half-warp on 8 cells x 2 adjacent views, packed sums, pair reuse,
+    // absolute-position pairs, 3 blocks/SM (-16 % at n=2048 against 443, the
+    // same with view groups 4 views apart and (v, d) pairs; -28 % against 408:
+    // 8-row chunks, 4-view bundles, one thread per cell)
+    int fwd_chunk_rows = 473;
+    // staged backprojector variant: 38 = 4 blocks/SM, packed FP32 pairs of
+    // rows, floor taken by FP32 adds, windows copied with cp.async, view loop
+    // unrolled 4 times, absolute-position sinogram pairs (default, measured
+    // fastest: -6.5 % against 27, the same unrolled twice on (t, d) pairs);
+    // 37 = 38 unrolled twice; 24 = 27 with register copies; 25 / 26 = 24
     // with the view loop unrolled 4 / 1 times; 28 = 27 unrolled 4 times; 14 =
     // 24 with the conversion unit's floor; 3, 4, 5 = scalar at 3..5 blocks/SM
-    int bwd_min_blocks = 27;
+    int bwd_min_blocks = 38;
 
     // row pitches of layA / layB in pairs, even so every row starts on 16 bytes
     int pitchA() const { return (W + 2 * kPad + 1) & ~1; }
@@ -226,6 +230,8 @@ void free_plan3d(Plan3d *p);
 
 int launch_plan2d_tables(Plan2d &p, cudaStream_t s);
 int launch_relayout2d(const Plan2d &p, const float *vol, cudaStream_t s);
+bool cslab_abs(int rows);
+bool bwd_abs(int min_blocks);
 int launch_forward2d(const Plan2d &p, float *sino, cudaStream_t s);
 // Raises a kernel's dynamic shared-memory limit to `bytes` on the current
 // device, once per (device, kernel): later calls, e.g. inside a CUDA-graph

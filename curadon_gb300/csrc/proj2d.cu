@@ -77,6 +77,10 @@ __global__ void k_plan2d_tables(int n, const float *__restrict__ ang,
 constexpr int kTile = 32;
 
 // Writes layA and layB for the 32 x 32 tile (bx, by) of padded texel space.
+// ABS: the pairs (v[c] - (c - C) d[c], d[c]) with C = W / 2 (layA) or H / 2
+// (layB), so that the linear sample at column coordinate p is e + (p - C) d
+// with no fraction to form (the chunked forward's absolute-position form).
+template <bool ABS = false>
 __device__ __forceinline__ void relayout2d_tile(const float *__restrict__ vol, int W, int H,
                                                 float2 *__restrict__ A, float2 *__restrict__ B,
                                                 int pa, int pb, int bx, int by) {
@@ -91,24 +95,32 @@ __device__ __forceinline__ void relayout2d_tile(const float *__restrict__ vol, i
     const int tx = threadIdx.x;
     for (int j = threadIdx.y; j < kTile; j += blockDim.y) {
         const int y = y0 + j, x = x0 + tx;
-        if (y < H + kPad && x < W + kPad)
+        if (y < H + kPad && x < W + kPad) {
+            const float v = tile[j][tx], d = tile[j][tx + 1] - v;
             A[(size_t)(y + kPad) * pa + (x + kPad)] =
-                make_float2(tile[j][tx], tile[j][tx + 1] - tile[j][tx]);
+                make_float2(ABS ? fmaf(-(float)(x - W / 2), d, v) : v, d);
+        }
     }
     for (int i = threadIdx.y; i < kTile; i += blockDim.y) {
         const int x = x0 + i, y = y0 + tx;
-        if (x < W + kPad && y < H + kPad)
+        if (x < W + kPad && y < H + kPad) {
+            const float v = tile[tx][i], d = tile[tx + 1][i] - v;
             B[(size_t)(x + kPad) * pb + (y + kPad)] =
-                make_float2(tile[tx][i], tile[tx + 1][i] - tile[tx][i]);
+                make_float2(ABS ? fmaf(-(float)(y - H / 2), d, v) : v, d);
+        }
     }
 }
 
+template <bool ABS>
 __global__ void __launch_bounds__(256)
     k_relayout2d(const float *__restrict__ vol, int W, int H, float2 *__restrict__ A,
                  float2 *__restrict__ B, int pa, int pb) {
-    relayout2d_tile(vol, W, H, A, B, pa, pb, blockIdx.x, blockIdx.y);
+    relayout2d_tile<ABS>(vol, W, H, A, B, pa, pb, blockIdx.x, blockIdx.y);
 }
 
+// ABS: (t[k] - (k - det / 2) d[k], d[k]), the staged backprojector's
+// absolute-position form (a sample at cell coordinate u is e + (u - det / 2) d).
+template <bool ABS = false>
 __device__ __forceinline__ void relayout_sino2d_elem(const float *__restrict__ sino, int det,
                                                      int nangles, float2 *__restrict__ S,
                                                      long long idx) {
@@ -119,12 +131,15 @@ __device__ __forceinline__ void relayout_sino2d_elem(const float *__restrict__ s
     const float *row = sino + (size_t)a * det;
     const float t0 = (k >= 0 && k < det) ? row[k] : 0.f;
     const float t1 = (k + 1 >= 0 && k + 1 < det) ? row[k + 1] : 0.f;
-    S[idx] = make_float2(t0, t1 - t0);
+    const float d = t1 - t0;
+    S[idx] = make_float2(ABS ? fmaf(-(float)(k - det / 2), d, t0) : t0, d);
 }
 
+template <bool ABS>
 __global__ void k_relayout_sino2d(const float *__restrict__ sino, int det, int nangles,
                                   float2 *__restrict__ S) {
-    relayout_sino2d_elem(sino, det, nangles, S, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+    relayout_sino2d_elem<ABS>(sino, det, nangles, S,
+                              (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ------------------------------------------------------------ forward
@@ -397,6 +412,14 @@ int launch_slab(const Plan2d &p, float *sino, cudaStream_t s) {
 
 }  // namespace
 
+// True for the chunked forward's shapes that read the absolute-position
+// layouts (relayout2d_tile<true>).
+bool cslab_abs(int rows) { return rows == 463 || rows == 473; }
+
+// True for the staged backprojector's shapes that read the absolute-position
+// sinogram pairs (relayout_sino2d_elem<true>).
+bool bwd_abs(int min_blocks) { return min_blocks == 37 || min_blocks == 38; }
+
 // True when the slab forward supports the plan's sizes.
 bool slab_supported(const Plan2d &p) {
     const size_t smem = sizeof(float2) * kSlabRing * (size_t)std::max(p.pitchA(), p.pitchB());
@@ -444,6 +467,21 @@ struct RowAcc {
     __device__ __forceinline__ float sum_hi() const { return PK ? hi.x + hi.y : hi.x; }
 };
 
+// Column index floor(p) - c0 clamped to [0, cmax] and the weight of the
+// pair's second term: the fraction p - floor(p) for (v, d) pairs, p itself
+// for the absolute-position form (e, d).
+template <bool ABS>
+__device__ __forceinline__ unsigned cs_column(float p, int c0, unsigned cmax, float &w) {
+    if constexpr (ABS) {
+        w = p;
+        return min((unsigned)(__float2int_rd(p) - c0), cmax);
+    } else {
+        const float pf = floorf(p);
+        w = p - pf;
+        return min((unsigned)((int)pf - c0), cmax);
+    }
+}
+
 // Bundle = kCs2G views x T adjacent detector cells x ray class (blockIdx.z:
 // 0 = y-stepping rays on layA, 1 = x-stepping rays on layB); thread t owns
 // cell u0 + t of every view.  The block walks its layout's rows in chunks of
@@ -465,7 +503,7 @@ struct RowAcc {
 // adjoint is this forward's transpose up to the order of summation.  A chunk
 // whose window does not fit reads global memory.
 template <int K, int S, int T, bool PK, bool REUSE = false, int VS = 1, int NG = kCs2G,
-          int MB = 0, int MAP = 0>
+          int MB = 0, int MAP = 0, bool ABS = false>
 __global__ void __launch_bounds__(T * VS, MB)
     k_fwd2d_cslab(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
                   float *__restrict__ sino, const float2 *__restrict__ tsrc,
@@ -492,14 +530,18 @@ __global__ void __launch_bounds__(T * VS, MB)
     // every 16 * VS threads
     // MAP = 1 (VS = 2): each half-warp holds 8 cells x 2 view groups, so the
     // 64-bit shared loads of one half span ~8 columns (no bank conflicts)
+    // MAP = 2: the same lanes, views interleaved (group j takes views j, j + 2,
+    // ...), so the two groups of a half-warp are one view apart, not NG / 2
     static_assert(MAP == 0 || VS == 2, "the half-warp map is for two threads per cell");
     const int cell = VS == 1 ? (int)threadIdx.x
-                     : MAP == 1 ? (int)((threadIdx.x >> 5) * 16 + (threadIdx.x & 7) +
+                     : MAP >= 1 ? (int)((threadIdx.x >> 5) * 16 + (threadIdx.x & 7) +
                                         8 * ((threadIdx.x >> 4) & 1))
                                 : (int)((threadIdx.x / (16 * VS)) * 16 + (threadIdx.x & 15));
     const int gb = VS == 1     ? 0
-                   : MAP == 1 ? (int)((threadIdx.x >> 3) & 1) * GV
+                   : MAP >= 1 ? (int)((threadIdx.x >> 3) & 1) * GV
                               : (int)((threadIdx.x >> 4) % VS) * GV;
+    // bundle view of the thread's ray g
+    auto bview = [&](int g) { return MAP == 2 ? gb / GV + g * VS : gb + g; };
     const int u0 = blockIdx.x * T, v0 = blockIdx.y * NG;
     const int u = u0 + cell;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -521,6 +563,10 @@ __global__ void __launch_bounds__(T * VS, MB)
         s_cor[threadIdx.x][0] = sp - sq * b;
         s_cor[threadIdx.x][1] = b;
     }
+    // ABS: columns are kept relative to C = pmaxi / 2 (the layout's pairs
+    // are (v - (c - C) d, d)), a sample is e + p d with p the relative column
+    const int ic = ABS ? pmaxi / 2 : 0;
+    const float pc = (float)ic;
     // per ray: column at its first row (p), step per row (V), row sums
     float p[GV], V[GV];
     RowAcc<PK> acc[GV];
@@ -528,7 +574,7 @@ __global__ void __launch_bounds__(T * VS, MB)
     int my_min = INT_MAX, my_max = INT_MIN;
 #pragma unroll
     for (int g = 0; g < GV; ++g) {
-        const int view = v0 + gb + g;
+        const int view = v0 + bview(g);
         acc[g].zero(), len[g] = 0, rlo[g] = 0, p[g] = V[g] = 0.f;
         if (view >= nangles || u >= det) continue;
         FanRay r;
@@ -539,7 +585,7 @@ __global__ void __launch_bounds__(T * VS, MB)
         if (n <= 0) continue;
         const int lo = r.sq > 0 ? iq : iq - (n - 1);
         V[g] = r.sq > 0 ? r.vp : -r.vp;
-        p[g] = r.sq > 0 ? r.p : fmaf((float)(n - 1), r.vp, r.p);
+        p[g] = (r.sq > 0 ? r.p : fmaf((float)(n - 1), r.vp, r.p)) - pc;
         rlo[g] = lo, len[g] = n;
         my_min = min(my_min, lo), my_max = max(my_max, lo + n - 1);
     }
@@ -615,9 +661,8 @@ __global__ void __launch_bounds__(T * VS, MB)
                     float2 hi_prev = make_float2(0.f, 0.f);
 #pragma unroll
                     for (int k = 0; k < K; ++k) {
-                        const float pf = floorf(p[g]);
-                        const float fp = p[g] - pf;
-                        const unsigned c = min((unsigned)((int)pf - c0), cmax);
+                        float fp;
+                        const unsigned c = cs_column<ABS>(p[g], c0 - ic, cmax, fp);
                         const float2 hi = b0[(k + 1) * S + c];
                         float2 lo;
                         if (REUSE && c == c_prev) lo = hi_prev;
@@ -630,9 +675,8 @@ __global__ void __launch_bounds__(T * VS, MB)
 #pragma unroll
                     for (int k = 0; k < K; ++k) {
                         if ((unsigned)(rel + k) < (unsigned)len[g]) {
-                            const float pf = floorf(p[g]);
-                            const float fp = p[g] - pf;
-                            const unsigned c = min((unsigned)((int)pf - c0), cmax);
+                            float fp;
+                            const unsigned c = cs_column<ABS>(p[g], c0 - ic, cmax, fp);
                             const float2 lo = b0[k * S + c], hi = b0[(k + 1) * S + c];
                             acc[g].add(fp, lo, hi);
                             p[g] += V[g];
@@ -646,9 +690,8 @@ __global__ void __launch_bounds__(T * VS, MB)
             for (int g = 0; g < GV; ++g) {
                 const int ra = max(r0, rlo[g]), rb = min(r0 + K - 1, rlo[g] + len[g] - 1);
                 for (int r = ra; r <= rb; ++r) {
-                    const float pf = floorf(p[g]);
-                    const float fp = p[g] - pf;
-                    const unsigned c = min((unsigned)((int)pf + kPad), gcap);
+                    float fp;
+                    const unsigned c = cs_column<ABS>(p[g], -kPad - ic, gcap, fp);
                     const float2 *rowp = lay + (size_t)(r + kPad) * pitch;
                     const float2 lo = __ldg(rowp + c), hi = __ldg(rowp + pitch + c);
                     acc[g].add(fp, lo, hi);
@@ -661,7 +704,7 @@ __global__ void __launch_bounds__(T * VS, MB)
 
 #pragma unroll
     for (int g = 0; g < GV; ++g) {
-        const int view = v0 + gb + g;
+        const int view = v0 + bview(g);
         if (view >= nangles || u >= det) continue;
         FanRay r;
         float out;
@@ -685,7 +728,8 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
     if (nv < 0) nv = p.nangles - v0;
     if (nv <= 0) return CG_OK;
     const int ng = rows == 438 || rows == 439 || rows == 440 || rows == 441 || rows == 442 ||
-                           rows == 443 || rows == 444 || rows == 447
+                           rows == 443 || rows == 444 || rows == 447 || rows == 451 ||
+                           rows == 453 || rows == 463 || rows == 473
                        ? 8
                    : rows == 448 || rows == 449 || rows == 450   ? 16
                                                                  : kCs2G;  // views per bundle
@@ -722,6 +766,10 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
         case 441: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 4, 1>, 8, 256, 128, 2);
         case 442: return go(k_fwd2d_cslab<12, 256, 128, true, true, 2, 8, 4, 1>, 12, 256, 128, 2);
         case 443: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 1>, 16, 256, 128, 2);
+        case 453: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 2>, 16, 256, 128, 2);
+        case 463: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 1, true>, 16, 256, 128, 2);
+        case 473: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 2, true>, 16, 256, 128, 2);
+        case 451: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 4, 2>, 8, 256, 128, 2);
         case 444: return go(k_fwd2d_cslab<16, 192, 128, true, true, 2, 8, 4, 1>, 16, 192, 128, 2);
         case 449: return go(k_fwd2d_cslab<8, 256, 64, true, true, 4, 16, 3>, 8, 256, 64, 4);
         case 450: return go(k_fwd2d_cslab<8, 256, 128, true, true, 4, 16, 2>, 8, 256, 128, 4);
@@ -813,7 +861,10 @@ constexpr int kSmWin = 128;   // pairs of one view's row staged for a tile
 // with the per-view terms of each thread's column hoisted, then one
 // reciprocal, one 8-byte shared load and two FMAs.  The same table describes
 // an arbitrary per-view source / detector placement (vector geometry).
-template <bool PK, bool MAGIC = false, int VU = 2, bool CPA = false>
+// ABS: the sinogram pairs are (e, d) = (t - (k - det / 2) d, d) and a sample
+// at cell coordinate ub is e + (ub - det / 2) d: the lateral coordinate is
+// formed relative to det / 2 and serves as the weight, no fraction.
+template <bool PK, bool MAGIC = false, int VU = 2, bool CPA = false, bool ABS = false>
 __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                                                 const float2 *__restrict__ S,
                                                 const float4 *__restrict__ proj, int W, int H,
@@ -828,6 +879,9 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
     const int y0 = yt + threadIdx.y;
     const float ex = (float)W / 2.0f, ey = (float)H / 2.0f;
     const float edm = (float)det / 2.0f - 0.5f;
+    // sampling offset and index shift: ub - C and floor(ub - C) + C
+    const int cq = ABS ? det / 2 : 0;
+    const float edq = edm - (float)cq;
     const float inv = __fdividef(1.0f, ds);
     const float X = ((float)x - ex) * sx + ox + 0.5f;
     // rows r and r + 1 of the thread's column as one pair (the packed loop's
@@ -904,7 +958,7 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                     // operations per row as the scalar loop below)
                     const float2 ay = make_float2(a.y, a.y), by = make_float2(b.y, b.y);
                     const float2 A2 = make_float2(A, A), B2 = make_float2(B, B);
-                    const float2 e2 = make_float2(edm, edm);
+                    const float2 e2 = make_float2(edq, edq);
 #pragma unroll
                     for (int r = 0; r < kSmRows; r += 2) {
                         const float2 Yr = Y2[r >> 1];
@@ -921,15 +975,16 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                             // window and is clamped.  f = ub + (1.5 * 2^23 - t).
                             const float2 M2 = make_float2(12582912.0f, 12582912.0f);
                             const float2 t = __fadd2_rd(ub, M2);
-                            f = __fadd2_rn(ub, __ffma2_rn(t, make_float2(-1.f, -1.f), M2));
-                            const unsigned base = 0x4B400000u + (unsigned)k0;
+                            f = ABS ? ub
+                                    : __fadd2_rn(ub, __ffma2_rn(t, make_float2(-1.f, -1.f), M2));
+                            const unsigned base = 0x4B400000u + (unsigned)(k0 - cq);
                             l0 = min(__float_as_uint(t.x) - base, (unsigned)(kSmWin - 1));
                             l1 = min(__float_as_uint(t.y) - base, (unsigned)(kSmWin - 1));
                         } else {
                             const float2 kf = make_float2(floorf(ub.x), floorf(ub.y));
-                            f = __fadd2_rn(ub, make_float2(-kf.x, -kf.y));
-                            l0 = min((unsigned)((int)kf.x - k0), (unsigned)(kSmWin - 1));
-                            l1 = min((unsigned)((int)kf.y - k0), (unsigned)(kSmWin - 1));
+                            f = ABS ? ub : __fadd2_rn(ub, make_float2(-kf.x, -kf.y));
+                            l0 = min((unsigned)((int)kf.x + cq - k0), (unsigned)(kSmWin - 1));
+                            l1 = min((unsigned)((int)kf.y + cq - k0), (unsigned)(kSmWin - 1));
                         }
                         const float2 t0 = sr[l0], t1 = sr[l1];
                         const float2 v = make_float2(fmaf(f.x, t0.y, t0.x), fmaf(f.y, t1.y, t1.x));
@@ -941,10 +996,11 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                         const float den = fmaf(a.y, Yv(r), A);
                         const float yi = fmaf(b.y, Yv(r), B);
                         const float w = __fdividef(1.0f, den);
-                        const float ub = fmaf(w, yi, edm);
+                        const float ub = fmaf(w, yi, edq);
                         const float kf = floorf(ub);
-                        const float f = ub - kf;
-                        const unsigned li = min((unsigned)((int)kf - k0), (unsigned)(kSmWin - 1));
+                        const float f = ABS ? ub : ub - kf;
+                        const unsigned li =
+                            min((unsigned)((int)kf + cq - k0), (unsigned)(kSmWin - 1));
                         const float2 t = sr[li];
                         fma_acc(r, fmaf(f, t.y, t.x), w);
                     }
@@ -956,10 +1012,11 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                     const float den = fmaf(a.y, Yv(r), A);
                     const float yi = fmaf(b.y, Yv(r), B);
                     const float w = __fdividef(1.0f, den);
-                    const float ub = fmaf(w, yi, edm);
+                    const float ub = fmaf(w, yi, edq);
                     const float kf = floorf(ub);
-                    const float f = ub - kf;
-                    const unsigned col = min((unsigned)((int)kf + kPad), (unsigned)(det + kPad));
+                    const float f = ABS ? ub : ub - kf;
+                    const unsigned col =
+                        min((unsigned)((int)kf + cq + kPad), (unsigned)(det + kPad));
                     const float2 t = __ldg(row + col);
                     fma_acc(r, fmaf(f, t.y, t.x), w);
                 }
@@ -977,13 +1034,13 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
 }
 
 // MINB: resident blocks per SM the register allocation must allow
-template <int MINB, bool PK, bool MAGIC = false, int VU = 2, bool CPA = false>
+template <int MINB, bool PK, bool MAGIC = false, int VU = 2, bool CPA = false, bool ABS = false>
 __global__ void __launch_bounds__(256, MINB)
     k_bwd2d_smem(float *__restrict__ vol, const float2 *__restrict__ S,
                  const float4 *__restrict__ proj, int W, int H, int det, int nangles, float sx,
                  float sy, float ox, float oy, float ds) {
-    bwd2d_smem_tile<PK, MAGIC, VU, CPA>(vol, S, proj, W, H, det, nangles, sx, sy, ox, oy, ds,
-                                        blockIdx.x, blockIdx.y);
+    bwd2d_smem_tile<PK, MAGIC, VU, CPA, ABS>(vol, S, proj, W, H, det, nangles, sx, sy, ox, oy,
+                                             ds, blockIdx.x, blockIdx.y);
 }
 
 }  // namespace
@@ -1031,19 +1088,21 @@ __global__ void __launch_bounds__(256)
     const int i = batch_problem(start, count, blockIdx.x);
     const Prob2d &q = probs[i];
     const long long idx = (long long)(blockIdx.x - start[i]) * blockDim.x + threadIdx.x;
-    relayout_sino2d_elem(q.sino, q.det, q.nangles, q.sinoP, idx);
+    relayout_sino2d_elem<true>(q.sino, q.det, q.nangles, q.sinoP, idx);
 }
 
 // The staged tile of the single-problem default (packed rows, round-down
-// floor, cp.async windows), so results equal it bit for bit.
+// floor, cp.async windows, view loop unrolled 4 times, absolute-position
+// pairs), so results equal it bit for bit.
 __global__ void __launch_bounds__(256, 4)
     k_batch_bwd2d(const Prob2d *__restrict__ probs, const int *__restrict__ start, int count) {
     const int i = batch_problem(start, count, blockIdx.x);
     const Prob2d &q = probs[i];
     const int local = blockIdx.x - start[i];
     const int gx = (q.W + 31) / 32;
-    bwd2d_smem_tile<true, true, 2, true>(q.vol, q.sinoP, q.bproj, q.W, q.H, q.det, q.nangles,
-                                         q.sx, q.sy, q.ox, q.oy, q.ds, local % gx, local / gx);
+    bwd2d_smem_tile<true, true, 4, true, true>(q.vol, q.sinoP, q.bproj, q.W, q.H, q.det,
+                                               q.nangles, q.sx, q.sy, q.ox, q.oy, q.ds,
+                                               local % gx, local / gx);
 }
 
 }  // namespace
@@ -1087,8 +1146,11 @@ int launch_plan2d_tables(Plan2d &p, cudaStream_t s) {
 
 int launch_relayout2d(const Plan2d &p, const float *vol, cudaStream_t s) {
     dim3 grid(ceil_div(p.W + 2 * kPad, kTile), ceil_div(p.H + 2 * kPad, kTile));
-    k_relayout2d<<<grid, dim3(32, 8), 0, s>>>(vol, p.W, p.H, p.d_layA, p.d_layB, p.pitchA(),
-                                              p.pitchB());
+    // the chunked forward's absolute-position shapes read the ABS form
+    const bool abs_form = (p.algo_fwd == 4 || p.algo_fwd == 5) && cslab_abs(p.fwd_chunk_rows);
+    auto kernel = abs_form ? k_relayout2d<true> : k_relayout2d<false>;
+    kernel<<<grid, dim3(32, 8), 0, s>>>(vol, p.W, p.H, p.d_layA, p.d_layB, p.pitchA(),
+                                        p.pitchB());
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }
@@ -1105,7 +1167,10 @@ int launch_forward2d(const Plan2d &p, float *sino, cudaStream_t s) {
 
 int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s) {
     const long long n = (long long)p.pitchS() * p.nangles;
-    k_relayout_sino2d<<<ceil_div(n, 256), 256, 0, s>>>(sino, p.det, p.nangles, p.d_sinoP);
+    // the staged backprojector's absolute-position shapes read the ABS form
+    const bool abs_form = (p.algo_bwd == 2 || p.algo_bwd == 3) && bwd_abs(p.bwd_min_blocks);
+    auto kernel = abs_form ? k_relayout_sino2d<true> : k_relayout_sino2d<false>;
+    kernel<<<ceil_div(n, 256), 256, 0, s>>>(sino, p.det, p.nangles, p.d_sinoP);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }
@@ -1127,9 +1192,11 @@ int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s, int rows
         case 25: go(k_bwd2d_smem<4, true, true, 4>); break;
         case 26: go(k_bwd2d_smem<4, true, true, 1>); break;
         case 27: go(k_bwd2d_smem<4, true, true, 2, true>); break;
+        case 37: go(k_bwd2d_smem<4, true, true, 2, true, true>); break;
+        case 38: go(k_bwd2d_smem<4, true, true, 4, true, true>); break;
         case 28: go(k_bwd2d_smem<4, true, true, 4, true>); break;
         case 24: go(k_bwd2d_smem<4, true, true>); break;
-        default: go(k_bwd2d_smem<4, true, true, 2, true>); break;
+        default: go(k_bwd2d_smem<4, true, true, 4, true, true>); break;
     }
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
