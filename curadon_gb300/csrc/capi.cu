@@ -64,8 +64,9 @@ void free_plan3d(Plan3d *p) {
 // from CURADON_GB300_ALGO: comma-separated key=value tokens, e.g.
 // "fwd2d=tex,bwd2d_minb=4".  Keys: fwd2d = alu | tex | slab | cslab |
 // cslab<shape> | hyb<1..7> | split<0..16>; bwd2d = alu | tex | smem |
-// split<0..16>; bwd2d_minb = 3 | 4 | 5 | 14 | 24 | 25 | 26 | 27 | 28 | 37 | 38
-// (staged backprojector shapes; 37 / 38: 27 / 28 on absolute-position pairs); adj2d = pair | quad; fwd3d = alu | tex3 | tex2l | slab | quad |
+// split<0..16>; bwd2d_minb = 3 | 4 | 5 | 14 | 24 | 25 | 26 | 27 | 28 | 37 | 38 |
+// 48 (staged backprojector shapes; 37 / 38: 27 / 28 on absolute-position
+// pairs; 48: 38 with 8 x 4-pixel warps); adj2d = pair | quad; fwd3d = alu | tex3 | tex2l | slab | quad |
 // mixed; fwd3d_tex = 0..8 (texture warps of 8 in forward 5);
 // fwd3d_block = BXxBYxBZ;
 // bwd3d = scalar | pk | pkmagic | quad (backward 0) | ax8m5 | ax8 | ax16 |
@@ -109,9 +110,10 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
                 // with 192-pair windows at <= 64 registers), 447 (8
                 // views per 64-cell bundle, 4 threads per cell on 2 each), 451 / 453
                 // (441 / 443 with interleaved view groups), 463 / 473 (443 / 453
-                // reading absolute-position pairs)
+                // reading absolute-position pairs), 474 (473 without pair reuse)
                 for (int k : {4, 104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438, 439,
-                              440, 441, 442, 443, 444, 447, 448, 449, 450, 451, 453, 463, 473})
+                              440, 441, 442, 443, 444, 447, 448, 449, 450, 451, 453, 463, 473,
+                              474})
                     if (val == "cslab" + std::to_string(k)) p2->fwd_chunk_rows = k;
             }
             for (int k = 1; k < 8; ++k)
@@ -130,7 +132,7 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
             if (val == "quad") p2->adj_quad = 1;
         }
         if (p2 && key == "bwd2d_minb")
-            for (int k : {3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38})
+            for (int k : {3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38, 48})
                 if (val == std::to_string(k)) p2->bwd_min_blocks = k;
         if (p3 && key == "fwd3d") {
             if (val == "alu") p3->algo_fwd = 0;

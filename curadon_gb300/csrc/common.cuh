@@ -120,21 +120,23 @@ struct Plan2d {
     int bwd_split_sixteenths = 3;
     cudaStream_t aux = nullptr;       // internal stream, created on first use
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    // chunked forward: chunk shape; 473 = 16-row chunks, bundles of 8 views
+    // chunked forward: chunk shape; 474 = 16-row chunks, bundles of 8 views
     // x 128 cells, two threads per cell on 4 interleaved views each, each
-    // half-warp on 8 cells x 2 adjacent views, packed sums, pair reuse,
-    // absolute-position pairs, 3 blocks/SM (-16 % at n=2048 against 443, the
-    // same with view groups 4 views apart and (v, d) pairs; -28 % against 408:
-    // 8-row chunks, 4-view bundles, one thread per cell)
-    int fwd_chunk_rows = 473;
-    // staged backprojector variant: 38 = 4 blocks/SM, packed FP32 pairs of
+    // half-warp on 8 cells x 2 adjacent views, packed sums, absolute-position
+    // pairs, both pairs loaded per sample, 3 blocks/SM (-2 % against 473, the
+    // same taking the lower pair from the previous sample where the column
+    // did not move; -18 % at n=2048 against 443, 473 with view groups 4 views
+    // apart and (v, d) pairs)
+    int fwd_chunk_rows = 474;
+    // staged backprojector variant: 48 = 4 blocks/SM, packed FP32 pairs of
     // rows, floor taken by FP32 adds, windows copied with cp.async, view loop
-    // unrolled 4 times, absolute-position sinogram pairs (default, measured
-    // fastest: -6.5 % against 27, the same unrolled twice on (t, d) pairs);
-    // 37 = 38 unrolled twice; 24 = 27 with register copies; 25 / 26 = 24
+    // unrolled 4 times, absolute-position sinogram pairs, warps on 8 x 4
+    // pixels (default, measured fastest: -2 % against 38, the same with warps
+    // on 32 x 1 pixels; 38 is -6.5 % against 27, the same unrolled twice on
+    // (t, d) pairs); 37 = 38 unrolled twice; 24 = 27 with register copies; 25 / 26 = 24
     // with the view loop unrolled 4 / 1 times; 28 = 27 unrolled 4 times; 14 =
     // 24 with the conversion unit's floor; 3, 4, 5 = scalar at 3..5 blocks/SM
-    int bwd_min_blocks = 38;
+    int bwd_min_blocks = 48;
 
     // row pitches of layA / layB in pairs, even so every row starts on 16 bytes
     int pitchA() const { return (W + 2 * kPad + 1) & ~1; }
@@ -311,6 +313,16 @@ __device__ __forceinline__ FloorSplit floor_split(float x, int base) {
     const float t = __fadd_rn(__fadd_rn(x, -0.5f), kMagic);
     const float k = __fadd_rn(t, -kMagic);
     return {__fadd_rn(x, -k), __float_as_uint(t) - (0x4B400000u + (unsigned)base)};
+}
+
+// 1 / x by the hardware's approximate reciprocal alone (PTX rcp.approx.ftz:
+// one special-function instruction, relative error within 2^-22.9, subnormal
+// results flushed to zero), for per-sample perspective weights whose
+// denominators are well inside the normal range.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 }
 
 }  // namespace cg

@@ -414,11 +414,11 @@ int launch_slab(const Plan2d &p, float *sino, cudaStream_t s) {
 
 // True for the chunked forward's shapes that read the absolute-position
 // layouts (relayout2d_tile<true>).
-bool cslab_abs(int rows) { return rows == 463 || rows == 473; }
+bool cslab_abs(int rows) { return rows == 463 || rows == 473 || rows == 474; }
 
 // True for the staged backprojector's shapes that read the absolute-position
 // sinogram pairs (relayout_sino2d_elem<true>).
-bool bwd_abs(int min_blocks) { return min_blocks == 37 || min_blocks == 38; }
+bool bwd_abs(int min_blocks) { return min_blocks == 37 || min_blocks == 38 || min_blocks == 48; }
 
 // True when the slab forward supports the plan's sizes.
 bool slab_supported(const Plan2d &p) {
@@ -729,7 +729,7 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
     if (nv <= 0) return CG_OK;
     const int ng = rows == 438 || rows == 439 || rows == 440 || rows == 441 || rows == 442 ||
                            rows == 443 || rows == 444 || rows == 447 || rows == 451 ||
-                           rows == 453 || rows == 463 || rows == 473
+                           rows == 453 || rows == 463 || rows == 473 || rows == 474
                        ? 8
                    : rows == 448 || rows == 449 || rows == 450   ? 16
                                                                  : kCs2G;  // views per bundle
@@ -769,6 +769,7 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
         case 453: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 2>, 16, 256, 128, 2);
         case 463: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 1, true>, 16, 256, 128, 2);
         case 473: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 2, true>, 16, 256, 128, 2);
+        case 474: return go(k_fwd2d_cslab<16, 256, 128, true, false, 2, 8, 3, 2, true>, 16, 256, 128, 2);
         case 451: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 4, 2>, 8, 256, 128, 2);
         case 444: return go(k_fwd2d_cslab<16, 192, 128, true, true, 2, 8, 4, 1>, 16, 192, 128, 2);
         case 449: return go(k_fwd2d_cslab<8, 256, 64, true, true, 4, 16, 3>, 8, 256, 64, 4);
@@ -864,7 +865,11 @@ constexpr int kSmWin = 128;   // pairs of one view's row staged for a tile
 // ABS: the sinogram pairs are (e, d) = (t - (k - det / 2) d, d) and a sample
 // at cell coordinate ub is e + (ub - det / 2) d: the lateral coordinate is
 // formed relative to det / 2 and serves as the weight, no fraction.
-template <bool PK, bool MAGIC = false, int VU = 2, bool CPA = false, bool ABS = false>
+// MAPQ: each warp covers 8 x 4 pixels (per row group) instead of 32 x 1, so
+// a half-warp's 16 lateral coordinates span fewer cells of the window row
+// (fewer shared-memory bank conflicts where the magnification is high).
+template <bool PK, bool MAGIC = false, int VU = 2, bool CPA = false, bool ABS = false,
+          bool MAPQ = false>
 __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                                                 const float2 *__restrict__ S,
                                                 const float4 *__restrict__ proj, int W, int H,
@@ -875,8 +880,8 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
     __shared__ int skmin[kSmViews];
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const int xt = bx * 32, yt = by * (8 * kSmRows);
-    const int x = xt + threadIdx.x;
-    const int y0 = yt + threadIdx.y;
+    const int x = xt + (MAPQ ? (int)((threadIdx.y & 3) * 8 + (threadIdx.x & 7)) : (int)threadIdx.x);
+    const int y0 = yt + (MAPQ ? (int)((threadIdx.y >> 2) * 4 + (threadIdx.x >> 3)) : (int)threadIdx.y);
     const float ex = (float)W / 2.0f, ey = (float)H / 2.0f;
     const float edm = (float)det / 2.0f - 0.5f;
     // sampling offset and index shift: ub - C and floor(ub - C) + C
@@ -964,7 +969,7 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                         const float2 Yr = Y2[r >> 1];
                         const float2 den = __ffma2_rn(ay, Yr, A2);
                         const float2 yi = __ffma2_rn(by, Yr, B2);
-                        const float2 w = make_float2(__fdividef(1.0f, den.x), __fdividef(1.0f, den.y));
+                        const float2 w = make_float2(rcp_approx(den.x), rcp_approx(den.y));
                         const float2 ub = __ffma2_rn(w, yi, e2);
                         float2 f;
                         unsigned l0, l1;
@@ -995,7 +1000,7 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                     for (int r = 0; r < kSmRows; ++r) {
                         const float den = fmaf(a.y, Yv(r), A);
                         const float yi = fmaf(b.y, Yv(r), B);
-                        const float w = __fdividef(1.0f, den);
+                        const float w = rcp_approx(den);
                         const float ub = fmaf(w, yi, edq);
                         const float kf = floorf(ub);
                         const float f = ABS ? ub : ub - kf;
@@ -1011,7 +1016,7 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                 for (int r = 0; r < kSmRows; ++r) {
                     const float den = fmaf(a.y, Yv(r), A);
                     const float yi = fmaf(b.y, Yv(r), B);
-                    const float w = __fdividef(1.0f, den);
+                    const float w = rcp_approx(den);
                     const float ub = fmaf(w, yi, edq);
                     const float kf = floorf(ub);
                     const float f = ABS ? ub : ub - kf;
@@ -1034,13 +1039,14 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
 }
 
 // MINB: resident blocks per SM the register allocation must allow
-template <int MINB, bool PK, bool MAGIC = false, int VU = 2, bool CPA = false, bool ABS = false>
+template <int MINB, bool PK, bool MAGIC = false, int VU = 2, bool CPA = false, bool ABS = false,
+          bool MAPQ = false>
 __global__ void __launch_bounds__(256, MINB)
     k_bwd2d_smem(float *__restrict__ vol, const float2 *__restrict__ S,
                  const float4 *__restrict__ proj, int W, int H, int det, int nangles, float sx,
                  float sy, float ox, float oy, float ds) {
-    bwd2d_smem_tile<PK, MAGIC, VU, CPA, ABS>(vol, S, proj, W, H, det, nangles, sx, sy, ox, oy,
-                                             ds, blockIdx.x, blockIdx.y);
+    bwd2d_smem_tile<PK, MAGIC, VU, CPA, ABS, MAPQ>(vol, S, proj, W, H, det, nangles, sx, sy, ox,
+                                                   oy, ds, blockIdx.x, blockIdx.y);
 }
 
 }  // namespace
@@ -1093,16 +1099,16 @@ __global__ void __launch_bounds__(256)
 
 // The staged tile of the single-problem default (packed rows, round-down
 // floor, cp.async windows, view loop unrolled 4 times, absolute-position
-// pairs), so results equal it bit for bit.
+// pairs, 8 x 4-pixel warps), so results equal it bit for bit.
 __global__ void __launch_bounds__(256, 4)
     k_batch_bwd2d(const Prob2d *__restrict__ probs, const int *__restrict__ start, int count) {
     const int i = batch_problem(start, count, blockIdx.x);
     const Prob2d &q = probs[i];
     const int local = blockIdx.x - start[i];
     const int gx = (q.W + 31) / 32;
-    bwd2d_smem_tile<true, true, 4, true, true>(q.vol, q.sinoP, q.bproj, q.W, q.H, q.det,
-                                               q.nangles, q.sx, q.sy, q.ox, q.oy, q.ds,
-                                               local % gx, local / gx);
+    bwd2d_smem_tile<true, true, 4, true, true, true>(q.vol, q.sinoP, q.bproj, q.W, q.H, q.det,
+                                                     q.nangles, q.sx, q.sy, q.ox, q.oy, q.ds,
+                                                     local % gx, local / gx);
 }
 
 }  // namespace
@@ -1194,9 +1200,10 @@ int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s, int rows
         case 27: go(k_bwd2d_smem<4, true, true, 2, true>); break;
         case 37: go(k_bwd2d_smem<4, true, true, 2, true, true>); break;
         case 38: go(k_bwd2d_smem<4, true, true, 4, true, true>); break;
+        case 48: go(k_bwd2d_smem<4, true, true, 4, true, true, true>); break;
         case 28: go(k_bwd2d_smem<4, true, true, 4, true>); break;
         case 24: go(k_bwd2d_smem<4, true, true>); break;
-        default: go(k_bwd2d_smem<4, true, true, 4, true, true>); break;
+        default: go(k_bwd2d_smem<4, true, true, 4, true, true, true>); break;
     }
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;

@@ -711,7 +711,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
                 for (int k = 0; k < kBZ; k += 2) {
                     const float2 t = __fmul2_rn(
-                        N2, make_float2(__fdividef(1.0f, DZ.x), __fdividef(1.0f, DZ.y)));
+                        N2, make_float2(rcp_approx(DZ.x), rcp_approx(DZ.y)));
                     const float2 ub = __ffma2_rn(DX, t, SU), vb = __ffma2_rn(DY, t, SV);
                     float2 wu, wv;
                     unsigned cu0, cu1, cv0, cv1;
@@ -763,7 +763,7 @@ __global__ void __launch_bounds__(256)
             } else {
 #pragma unroll
                 for (int k = 0; k < kBZ; ++k) {
-                    const float t = __fdividef(num, dirz);
+                    const float t = num * rcp_approx(dirz);
                     const float ub = fmaf(dirx, t, su), vb = fmaf(diry, t, sv);
                     const int iu = __float2int_rd(ub), iv = __float2int_rd(vb);
                     const float wu = ub - (float)iu, wv = vb - (float)iv;

@@ -314,7 +314,7 @@ def test_split_backward_shares_and_graph(cuda_device, monkeypatch, k):
     assert torch.equal(out, b)
 
 
-@pytest.mark.parametrize("shape", [3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38])
+@pytest.mark.parametrize("shape", [3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38, 48])
 def test_staged_backprojector_shapes(cuda_device, monkeypatch, shape):
     """Every compiled shape of the staged backprojector (CURADON_GB300_ALGO
     bwd2d_minb=...: blocks per SM, packed rows, floor by FP32 adds, view-loop
@@ -335,7 +335,7 @@ def test_staged_backprojector_shapes(cuda_device, monkeypatch, shape):
 
 @pytest.mark.parametrize("shape", [4, 104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438,
                                    439, 440, 441, 442, 443, 444, 447, 448, 449, 450, 451, 453,
-                                   463, 473])
+                                   463, 473, 474])
 def test_chunked_forward_shapes(cuda_device, monkeypatch, shape):
     """Every compiled shape of the chunked forward (CURADON_GB300_ALGO
     fwd2d=cslab<shape>: rows per chunk, bundle width, packed sums, pair reuse,
