@@ -152,6 +152,19 @@ class plan_2d:
             self._h, _algo_index(forward, FORWARD_2D, "forward"),
             _algo_index(backward, BACKWARD_2D, "backward")))
 
+    @property
+    def shapes(self):
+        """(chunked-forward shape, staged-backprojector variant) of this plan."""
+        f, b = C.c_int(), C.c_int()
+        check(self._L.cg_plan2d_get_shapes(self._h, C.byref(f), C.byref(b)))
+        return f.value, b.value
+
+    def set_shapes(self, forward=None, backward=None):
+        """Selects the chunked forward's kernel shape and the staged
+        backprojector's variant (``cg_plan2d_set_shapes``; None keeps)."""
+        check(self._L.cg_plan2d_set_shapes(self._h, -1 if forward is None else int(forward),
+                                           -1 if backward is None else int(backward)))
+
     def tables(self):
         """(sources, u_origins, delta_us), each (nangles, 2) float32."""
         out = [np.zeros(2 * self.nangles, np.float32) for _ in range(3)]

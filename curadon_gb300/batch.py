@@ -9,9 +9,11 @@ The buffers stay bound, so both calls can be captured in a CUDA graph
 (``torch.cuda.graph``) and an iteration loop replayed without launch
 overhead.  The forward is the texture-unit ray march (``forward="texture"``,
 default: one array copy per problem, then one launch) or the FP32 register
-march (``forward="registers"``); the backprojection is the staged one; their
-results equal the single-problem operators with those algorithms bit for
-bit.  No counterpart in the reference, which runs one problem per call.
+march (``forward="registers"``); ``forward="auto"`` times both on the bound
+problems once and keeps the faster (the sinograms' contents are restored
+afterwards).  The backprojection is the staged one; results equal the
+single-problem operators with those algorithms bit for bit.  No
+counterpart in the reference, which runs one problem per call.
 """
 from __future__ import annotations
 
@@ -32,8 +34,8 @@ class Batch2d:
 
     def __init__(self, geoms: Sequence[FanGeometry], volumes: Sequence[torch.Tensor],
                  sinograms: Sequence[torch.Tensor], forward: str = "texture"):
-        if forward not in self.FORWARD:
-            raise ValueError(f"batched forward must be one of {self.FORWARD}")
+        if forward not in self.FORWARD + ("auto",):
+            raise ValueError(f"batched forward must be one of {self.FORWARD + ('auto',)}")
         if not (len(geoms) == len(volumes) == len(sinograms)) or not geoms:
             raise ValueError("geoms, volumes and sinograms must be non-empty and of one length")
         dev = volumes[0].device
@@ -62,10 +64,41 @@ class Batch2d:
         h = C.c_void_p()
         check(self._L.cg_batch2d_create(C.byref(h), hp, vp, sp, n))
         self._h = h
-        check(self._L.cg_batch2d_set_forward(h, self.FORWARD.index(forward)))
         self._keep = (list(geoms), list(volumes), list(sinograms), plans)
         self.device = dev
         self.count = n
+        self.tuned_ms: dict[str, float] = {}
+        if forward == "auto":
+            self._tune_forward()
+        else:
+            check(self._L.cg_batch2d_set_forward(h, self.FORWARD.index(forward)))
+
+    def _tune_forward(self, reps: int = 3) -> None:
+        """Times every batched forward on the bound problems (CUDA events on
+        the current stream, median of ``reps`` after one warm-up) and keeps
+        the fastest; the bound sinograms are restored."""
+        sinos = self._keep[2]
+        saved = [s.clone() for s in sinos]
+        best = None
+        for i, name in enumerate(self.FORWARD):
+            check(self._L.cg_batch2d_set_forward(self._h, i))
+            self.forward()
+            ts = []
+            for _ in range(reps):
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record()
+                self.forward()
+                b.record()
+                b.synchronize()
+                ts.append(a.elapsed_time(b))
+            t = sorted(ts)[len(ts) // 2]
+            self.tuned_ms[name] = t
+            if best is None or t < best[0]:
+                best = (t, i)
+        check(self._L.cg_batch2d_set_forward(self._h, best[1]))
+        for s, c in zip(sinos, saved):
+            s.copy_(c)
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(256)
     k_adj3d(void *__restrict__ A, void *__restrict__ B, const float *__restrict__ sino,
             const float4 *__restrict__ torg, const float4 *__restrict__ tdu,
             const float4 *__restrict__ tdv, const float4 *__restrict__ tsrc, int X, int Y, int Z,
-            int U, int V, int P, int utiles) {
+            int U, int V, int P, int utiles, bool exact_t) {
     int iu, iv, view;
     if constexpr (BAND) {
         const int lin = blockIdx.x;
@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(256)
             atomicAdd(p00 + (size_t)pa * pb, make_float2(c01 * (1.f - wa), c01 * wa));
             atomicAdd(p00 + (size_t)pa * pb + pa, make_float2(c11 * (1.f - wa), c11 * wa));
         }
-        t += h;
+        t = march_next(t, k, tmin, h, exact_t);
     }
     if constexpr (QUAD && MERGE) {
         if (held_at != ~(size_t)0) atomicAdd(static_cast<float4 *>(L) + held_at, held);
@@ -329,7 +329,8 @@ int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s) {
         auto kq = p.adj_merge ? (band ? k_adj3d<true, true, true> : k_adj3d<true, false, true>)
                               : (band ? k_adj3d<true, true> : k_adj3d<true, false>);
         kq<<<grid, dim3(32, 8), 0, s>>>(p.d_quadA, p.d_quadB, sino, p.d_forg, p.d_fdu, p.d_fdv,
-                                        p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V, p.nangles, utiles);
+                                        p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V, p.nangles, utiles,
+                                        p.exact_t);
         CG_TRY_CUDA(cudaGetLastError());
         k_fold3d_quad<<<ceil_div(n, 256), 256, 0, s>>>(vol, p.d_quadA, p.d_quadB, p.X, p.Y, p.Z);
         CG_TRY_CUDA(cudaGetLastError());
@@ -339,7 +340,8 @@ int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s) {
     CG_TRY_CUDA(cudaMemsetAsync(p.d_volB, 0, p.volB_elems * sizeof(float2), s));
     auto kp = band ? k_adj3d<false, true> : k_adj3d<false, false>;
     kp<<<grid, dim3(32, 8), 0, s>>>(p.d_volA, p.d_volB, sino, p.d_forg, p.d_fdu, p.d_fdv,
-                                    p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V, p.nangles, utiles);
+                                    p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V, p.nangles, utiles,
+                                    p.exact_t);
     CG_TRY_CUDA(cudaGetLastError());
     k_fold3d<<<ceil_div(n, 256), 256, 0, s>>>(vol, p.d_volA, p.d_volB, p.X, p.Y, p.Z);
     CG_TRY_CUDA(cudaGetLastError());

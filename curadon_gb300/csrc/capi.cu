@@ -60,6 +60,20 @@ void free_plan3d(Plan3d *p) {
         if (q) cudaFree(q);
 }
 
+// Compiled kernel shapes of the chunked 2D forward (launch_forward2d_cslab)
+// and variants of the staged 2D backprojector (launch_backward2d_smem).
+constexpr int kFwdChunkShapes[] = {4,   104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438, 439,
+                                   440, 441, 442, 443, 444, 447, 448, 449, 450, 451, 453, 463, 473,
+                                   474};
+constexpr int kBwdStagedVariants[] = {3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38, 48};
+
+template <size_t N>
+bool listed(const int (&list)[N], int v) {
+    for (int k : list)
+        if (k == v) return true;
+    return false;
+}
+
 // Overrides of a new plan's algorithms for measurement and testing, read
 // from CURADON_GB300_ALGO: comma-separated key=value tokens, e.g.
 // "fwd2d=tex,bwd2d_minb=4".  Keys: fwd2d = alu | tex | slab | cslab |
@@ -71,7 +85,8 @@ void free_plan3d(Plan3d *p) {
 // fwd3d_block = BXxBYxBZ;
 // bwd3d = scalar | pk | pkmagic | quad (backward 0) | ax8m5 | ax8 | ax16 |
 // ax16m4 (backward 1); adj3d = pair | quad; adj3d_order = band | view;
-// adj3d_merge = 0 | 1.
+// adj3d_merge = 0 | 1; t3d = step | exact (running-sum or drift-free sample
+// parameters of the 3D ray marches).
 // Unknown tokens are
 // ignored; without the variable every plan starts at the measured defaults.
 void apply_algo_env(Plan2d *p2, Plan3d *p3) {
@@ -111,9 +126,7 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
                 // views per 64-cell bundle, 4 threads per cell on 2 each), 451 / 453
                 // (441 / 443 with interleaved view groups), 463 / 473 (443 / 453
                 // reading absolute-position pairs), 474 (473 without pair reuse)
-                for (int k : {4, 104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438, 439,
-                              440, 441, 442, 443, 444, 447, 448, 449, 450, 451, 453, 463, 473,
-                              474})
+                for (int k : kFwdChunkShapes)
                     if (val == "cslab" + std::to_string(k)) p2->fwd_chunk_rows = k;
             }
             for (int k = 1; k < 8; ++k)
@@ -132,7 +145,7 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
             if (val == "quad") p2->adj_quad = 1;
         }
         if (p2 && key == "bwd2d_minb")
-            for (int k : {3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38, 48})
+            for (int k : kBwdStagedVariants)
                 if (val == std::to_string(k)) p2->bwd_min_blocks = k;
         if (p3 && key == "fwd3d") {
             if (val == "alu") p3->algo_fwd = 0;
@@ -152,6 +165,10 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
                 if (val == general[i]) p3->algo_bwd = 0, p3->bwd_packed = i;
                 if (val == runs[i]) p3->algo_bwd = 1, p3->bwd_axial = i;
             }
+        }
+        if (p3 && key == "t3d") {
+            if (val == "step") p3->exact_t = false;
+            if (val == "exact") p3->exact_t = true;
         }
         if (p3 && key == "adj3d_merge") {
             if (val == "0") p3->adj_merge = false;
@@ -358,6 +375,9 @@ int make_plan3d(cg_plan3d **out, int device, const uint64_t vol_shape[3], const 
     // forward 5: 4 of 8 warps on the texture unit from 300^3 voxels (512^3:
     // -2 % against 3), 3 below (256^3 and 128^3: -2 % against 4)
     if ((long long)p->X * p->Y * p->Z >= 27000000LL) p->fwd_tex_warps = 4;
+    // drift-free sample parameters where the running sum drifts measurably
+    // (rays of ~900 samples and more)
+    p->exact_t = std::max(p->X, std::max(p->Y, p->Z)) >= 512;
     apply_algo_env(nullptr, p.get());
     Cone c;
     c.shape_f = {{(float)vol_shape[2], (float)vol_shape[1], (float)vol_shape[0]}};
@@ -647,6 +667,25 @@ int cg_plan2d_get_algorithm(const cg_plan2d *plan, int *forward, int *backward) 
     clear_error();
     CG_REQUIRE(plan && forward && backward, "NULL argument");
     *forward = plan->algo_fwd, *backward = plan->algo_bwd;
+    return CG_OK;
+}
+
+int cg_plan2d_set_shapes(cg_plan2d *plan, int forward_shape, int backward_variant) {
+    clear_error();
+    CG_REQUIRE(plan, "plan is NULL");
+    CG_REQUIRE(forward_shape == -1 || listed(kFwdChunkShapes, forward_shape),
+               "unknown chunked-forward shape");
+    CG_REQUIRE(backward_variant == -1 || listed(kBwdStagedVariants, backward_variant),
+               "unknown staged-backprojector variant");
+    if (forward_shape >= 0) plan->fwd_chunk_rows = forward_shape;
+    if (backward_variant >= 0) plan->bwd_min_blocks = backward_variant;
+    return CG_OK;
+}
+
+int cg_plan2d_get_shapes(const cg_plan2d *plan, int *forward_shape, int *backward_variant) {
+    clear_error();
+    CG_REQUIRE(plan && forward_shape && backward_variant, "NULL argument");
+    *forward_shape = plan->fwd_chunk_rows, *backward_variant = plan->bwd_min_blocks;
     return CG_OK;
 }
 

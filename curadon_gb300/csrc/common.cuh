@@ -189,6 +189,11 @@ struct Plan3d {
     // merge consecutive samples' shared quad element into one atomic
     // (-11 % at 128^3, -10 % at 256^3)
     bool adj_merge = true;
+    // ray-march sample parameters t_k = tmin + k h by one FMA instead of the
+    // reference's running sum t += h, whose rounding accumulates along long
+    // rays (on from 512 voxels along an axis: against the FP64 oracle the
+    // running sum leaves rays of a 512^3 volume up to 2.5e-3 off, relative)
+    bool exact_t = false;
 
     // texture-unit variants (allocated on first use)
     cudaArray_t arr3 = nullptr, arrA = nullptr, arrB = nullptr;
@@ -313,6 +318,13 @@ __device__ __forceinline__ FloorSplit floor_split(float x, int base) {
     const float t = __fadd_rn(__fadd_rn(x, -0.5f), kMagic);
     const float k = __fadd_rn(t, -kMagic);
     return {__fadd_rn(x, -k), __float_as_uint(t) - (0x4B400000u + (unsigned)base)};
+}
+
+// Sample parameter of ray-march step k + 1: the reference's running sum t + h
+// (forward_3d.hpp:85-92), or with `exact` tmin + (k + 1) h by one FMA, so
+// that no rounding accumulates along the ray.
+__device__ __forceinline__ float march_next(float t, int k, float tmin, float h, bool exact) {
+    return exact ? fmaf((float)(k + 1), h, tmin) : t + h;
 }
 
 // 1 / x by the hardware's approximate reciprocal alone (PTX rcp.approx.ftz:

@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(256)
     k_fwd3d(const float2 *__restrict__ A, const float2 *__restrict__ B, float *__restrict__ sino,
             const float4 *__restrict__ torg, const float4 *__restrict__ tdu,
             const float4 *__restrict__ tdv, const float4 *__restrict__ tsrc, int X, int Y, int Z,
-            int U, int V) {
+            int U, int V, bool exact_t) {
     const int iu = blockIdx.x * blockDim.x + threadIdx.x;
     const int iv = blockIdx.y * blockDim.y + threadIdx.y;
     const int view = blockIdx.z;
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(256)
         const float m0 = fmaf(wb, l10 - l00, l00);
         const float m1 = fmaf(wb, l11 - l01, l01);
         acc += fmaf(wc, m1 - m0, m0);
-        t += h;
+        t = march_next(t, k, tmin, h, exact_t);
     }
     sino[((size_t)view * V + iv) * U + iu] = acc;
 }
@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(256)
                  float *__restrict__ sino, const float4 *__restrict__ torg,
                  const float4 *__restrict__ tdu, const float4 *__restrict__ tdv,
                  const float4 *__restrict__ tsrc, int X, int Y, int Z, int U, int V, int P,
-                 int utiles, cudaTextureObject_t tex, int tex_warps) {
+                 int utiles, cudaTextureObject_t tex, int tex_warps, bool exact_t) {
     const int lin = blockIdx.x;
     const int ut = lin % utiles, rest = lin / utiles;
     const int view = rest % P, band = rest / P;
@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(256)
             if (!(t <= r.tmax)) break;
             acc += tex3D<float>(tex, fmaf(r.dx, t, r.sx) + 0.5f, fmaf(r.dy, t, r.sy) + 0.5f,
                                 fmaf(r.dz, t, r.sz) + 0.5f);
-            t += r.h;
+            t = march_next(t, k, r.tmin, r.h, exact_t);
         }
         sino[((size_t)view * V + iv) * U + iu] = acc;
         return;
@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(256)
         const float l1 = fmaf(wa, q1.y, q1.x), g1 = fmaf(wa, q1.w, q1.z);
         const float m0 = fmaf(wb, g0, l0), m1 = fmaf(wb, g1, l1);
         acc += fmaf(wc, m1 - m0, m0);
-        t += r.h;
+        t = march_next(t, k, r.tmin, r.h, exact_t);
     }
     sino[((size_t)view * V + iv) * U + iu] = acc;
 }
@@ -944,7 +944,7 @@ int launch_forward3d(const Plan3d &p, const float *vol, float *sino, cudaStream_
     if (p.nangles > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     dim3 grid(ceil_div(p.U, 32), ceil_div(p.V, 8), p.nangles);
     k_fwd3d<<<grid, dim3(32, 8), 0, s>>>(p.d_volA, p.d_volB, sino, p.d_forg, p.d_fdu, p.d_fdv,
-                                         p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V);
+                                         p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V, p.exact_t);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }
@@ -990,7 +990,7 @@ int launch_forward3d_quad(Plan3d &p, const float *vol, float *sino, cudaStream_t
     }
     k_fwd3d_quad<<<(unsigned)blocks, 256, 0, s>>>(p.d_volQA, p.d_volQB, sino, p.d_forg, p.d_fdu,
                                                   p.d_fdv, p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V,
-                                                  p.nangles, utiles, tex, tex_warps);
+                                                  p.nangles, utiles, tex, tex_warps, p.exact_t);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }

@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(256)
     k_fwd3d_tex3(cudaTextureObject_t tex, float *__restrict__ sino,
                  const float4 *__restrict__ torg, const float4 *__restrict__ tdu,
                  const float4 *__restrict__ tdv, const float4 *__restrict__ tsrc, int X, int Y,
-                 int Z, int U, int V, int P) {
+                 int Z, int U, int V, int P, bool exact_t) {
     const int iu = blockIdx.x * blockDim.x + threadIdx.x;
     const int iv = blockIdx.y * blockDim.y + threadIdx.y;
     const int view = blockIdx.z * blockDim.z + threadIdx.z;
@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(256)
         if (!(t <= r.tmax)) break;
         acc += tex3D<float>(tex, fmaf(r.dx, t, r.sx) + 0.5f, fmaf(r.dy, t, r.sy) + 0.5f,
                             fmaf(r.dz, t, r.sz) + 0.5f);
-        t += r.h;
+        t = march_next(t, k, r.tmin, r.h, exact_t);
     }
     sino[((size_t)view * V + iv) * U + iu] = acc;
 }
@@ -536,7 +536,7 @@ int launch_forward3d_texture(Plan3d &p, const float *vol, float *sino, cudaStrea
         int rc = copy_to_array(p.arr3, vol, p.X, p.Y, p.Z, s);
         if (rc) return rc;
         k_fwd3d_tex3<<<grid, block, 0, s>>>(p.tex3, sino, p.d_forg, p.d_fdu, p.d_fdv, p.d_fsrc,
-                                            p.X, p.Y, p.Z, p.U, p.V, p.nangles);
+                                            p.X, p.Y, p.Z, p.U, p.V, p.nangles, p.exact_t);
         CG_TRY_CUDA(cudaGetLastError());
         return CG_OK;
     }

@@ -111,6 +111,20 @@ int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by);
 int cg_plan2d_set_algorithm(cg_plan2d *plan, int forward, int backward);
 int cg_plan2d_get_algorithm(const cg_plan2d *plan, int *forward, int *backward);
 
+/* Kernel shape of the chunked forward (used by forward algorithms 4 and 5)
+ * and variant of the staged backprojector (backward algorithms 2 and 3); -1
+ * keeps the current one.  Shapes: 4, 104, 108, 204, 304, 308, 404, 408, 414,
+ * 418, 428, 438-444, 447-451, 453, 463, 473, 474 (default); variants: 3, 4,
+ * 5, 14, 24-28, 37, 38, 48 (default).  Every shape computes the reference's
+ * samples and weights; they differ in rows per chunk, views per bundle,
+ * threads per cell, pair layout and register bounds, so the fastest depends
+ * on the geometry (no reference counterpart: the reference has one kernel
+ * per direction, forward_2d.hpp:21-79 and backward_2d.hpp:21-100).  Used by
+ * the autotuner (curadon_gb300.autotune).  CG_ERR_INVALID for an unknown
+ * shape. */
+int cg_plan2d_set_shapes(cg_plan2d *plan, int forward_shape, int backward_variant);
+int cg_plan2d_get_shapes(const cg_plan2d *plan, int *forward_shape, int *backward_variant);
+
 /* Copies the plan's per-view tables to host arrays of 2 * nangles floats each
  * (x, y interleaved): source position, direction to detector cell 0 and
  * per-cell step, in voxel-index units (plan_2d::sources/u_origins/delta_us,

@@ -117,6 +117,22 @@ def test_dot_product_3d_per_forward_algorithm(cuda_device, algo):
     assert dot_test(geom, x, y, cuda_device) < 1e-5
 
 
+@pytest.mark.parametrize("algo", ["registers", "quad"])
+def test_dot_product_3d_exact_parameters(cuda_device, monkeypatch, algo):
+    """With drift-free sample parameters (t3d=exact, the default from 512
+    voxels along an axis) the forward and the matched adjoint still take the
+    same samples."""
+    g = cone_config(40, 36, 64)
+    monkeypatch.setenv("CURADON_GB300_ALGO", "t3d=exact")
+    geom = ConeGeometry(**g)
+    geom.exact_plan.set_algorithm(forward=algo)
+    monkeypatch.delenv("CURADON_GB300_ALGO")
+    rng = np.random.default_rng(8)
+    x = rng.uniform(0, 1, (40, 40, 40)).astype(np.float32)
+    y = rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32)
+    assert dot_test(geom, x, y, cuda_device) < 1e-5
+
+
 def test_adjoint_accumulates(cuda_device):
     g = cone_config(24, 12, 40)
     geom = ConeGeometry(**g)

@@ -294,3 +294,45 @@ def test_quad_buffers_fall_back_when_memory_is_short(cuda_device):
     assert geom.plan.algorithm == ("texture", "registers")
     check_fwd(s.cpu().numpy(), s_ref)
     assert rel_l2(b.cpu().numpy(), b_ref) < TOL
+
+
+@pytest.mark.parametrize("n,nangles,det", [(256, 360, 384), (512, 720, 768)])
+def test_fp32_drift_along_rays(cuda_device, monkeypatch, n, nangles, det):
+    """FP32 ray marches against the FP64 oracle on two views (0 and pi) of
+    the 256^3 and 512^3 problems, quad forward (FP32 weights, no texture
+    quantisation), with the reference's running sample parameter t += h
+    ("step") and with t_k = tmin + k h ("exact", the default from 512
+    voxels along an axis).  The running sum's rounding shifts the samples
+    along the ray (at 256^3 up to 2.2e-4 of a ray's integral, relative);
+    the exact parameters remove that drift.  What remains are a few rays
+    whose FP32 sample count ceil((tmax - tmin) |d|) rounds to the other
+    integer than in FP64 (the reference's set-up in FP32 operations) and
+    so hold one sample more or less, ~1e-3 of their integral: the test
+    bounds the 99.9th percentile of the per-ray error, the maximum is
+    printed."""
+    g = cone_config(n, nangles, det)
+    g["angles"] = np.asarray(g["angles"])[:: nangles // 2].copy()
+    ph = ellipsoids_3d(n, n).numpy()
+    ref = None
+    err = {}
+    for mode in ("step", "exact"):
+        monkeypatch.setenv("CURADON_GB300_ALGO", f"t3d={mode}")
+        geom = make(g, cuda_device)
+        geom.plan.set_algorithm(forward="quad")
+        monkeypatch.delenv("CURADON_GB300_ALGO")
+        s = run_fwd(geom, ph, cuda_device)
+        if ref is None:
+            ref = oracle.fwd3d(g, ph, sino0=np.full(geom.sinogram_shape(), SENTINEL))
+        both = (s != SENTINEL) & (ref != SENTINEL)
+        e = rel_l2(s[both], ref[both])
+        big = both & (np.abs(ref) > 1e-2 * np.abs(ref[both]).max())
+        r = np.abs(s[big] - ref[big]) / np.abs(ref[big])
+        p999 = np.quantile(r, 0.999)
+        err[mode] = (e, p999)
+        print(f"n={n} {mode}: FP32 vs FP64 rel-L2 {e:.2e} max-abs "
+              f"{max_abs(s[both], ref[both]):.2e} per-ray relative 99.9 % {p999:.2e} "
+              f"max {r.max():.2e}")
+        assert e < 1e-4
+    assert err["exact"][0] <= err["step"][0]
+    assert err["exact"][1] <= err["step"][1]
+    assert err["exact"][0] < 4e-5 and err["exact"][1] < 1e-4
