@@ -30,6 +30,7 @@ SIGNATURES = [
     ("cg_plan2d_set_algorithm", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("cg_plan2d_get_algorithm", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("cg_plan2d_set_shapes", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    ("cg_wait_timeouts", C.c_int, [C.POINTER(C.c_ulonglong)]),
     ("cg_plan2d_get_shapes", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("cg_plan2d_tables", C.c_int, [C.c_void_p, f32p, f32p, f32p]),
     ("cg_forward_2d", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -25,7 +25,7 @@ from ._lib import CuradonError
 
 # (algorithm name, kernel shape or None); shapes are compiled chunk shapes of
 # the chunked forward and variants of the staged backprojector
-FORWARD_CANDIDATES = (("texture", None), ("chunked", 474), ("chunked", 473),
+FORWARD_CANDIDATES = (("texture", None), ("chunked", 484), ("chunked", 474),
                       ("chunked", 443))
 BACKWARD_CANDIDATES = (("shared", 48), ("shared", 38), ("shared", 27), ("texture", None))
 

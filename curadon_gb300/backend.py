@@ -221,6 +221,14 @@ def _check_2d(vol, sino, plan: plan_2d):
                          f"{(plan.nangles, plan.det_count)}")
 
 
+def wait_timeouts() -> int:
+    """Bounded waits that gave up in this library's kernels on the current
+    device since the last call (``cg_wait_timeouts``); 0 when all is well."""
+    n = C.c_ulonglong()
+    check(load().cg_wait_timeouts(C.byref(n)))
+    return n.value
+
+
 def forward_2d(volume, sinogram, plan: plan_2d):
     """Overwrites ``sinogram`` (nangles, det) with the projection of ``volume``."""
     _check_2d(volume, sinogram, plan)

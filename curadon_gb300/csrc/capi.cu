@@ -64,7 +64,7 @@ void free_plan3d(Plan3d *p) {
 // and variants of the staged 2D backprojector (launch_backward2d_smem).
 constexpr int kFwdChunkShapes[] = {4,   104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438, 439,
                                    440, 441, 442, 443, 444, 447, 448, 449, 450, 451, 453, 463, 473,
-                                   474};
+                                   474, 484};
 constexpr int kBwdStagedVariants[] = {3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38, 48};
 
 template <size_t N>
@@ -125,7 +125,8 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
                 // with 192-pair windows at <= 64 registers), 447 (8
                 // views per 64-cell bundle, 4 threads per cell on 2 each), 451 / 453
                 // (441 / 443 with interleaved view groups), 463 / 473 (443 / 453
-                // reading absolute-position pairs), 474 (473 without pair reuse)
+                // reading absolute-position pairs), 474 (473 without pair reuse),
+                // 484 (474 staged by bulk copies on mbarriers)
                 for (int k : kFwdChunkShapes)
                     if (val == "cslab" + std::to_string(k)) p2->fwd_chunk_rows = k;
             }
@@ -431,6 +432,12 @@ extern "C" {
 const char *cg_last_error(void) { return g_last_error.c_str(); }
 
 int cg_version(void) { return 1 * 10000 + 0 * 100 + 0; }
+
+int cg_wait_timeouts(unsigned long long *count) {
+    clear_error();
+    CG_REQUIRE(count, "count is NULL");
+    return cg::take_wait_timeouts(count);
+}
 
 namespace {
 

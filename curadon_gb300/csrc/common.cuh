@@ -120,14 +120,16 @@ struct Plan2d {
     int bwd_split_sixteenths = 3;
     cudaStream_t aux = nullptr;       // internal stream, created on first use
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    // chunked forward: chunk shape; 474 = 16-row chunks, bundles of 8 views
-    // x 128 cells, two threads per cell on 4 interleaved views each, each
-    // half-warp on 8 cells x 2 adjacent views, packed sums, absolute-position
-    // pairs, both pairs loaded per sample, 3 blocks/SM (-2 % against 473, the
-    // same taking the lower pair from the previous sample where the column
-    // did not move; -18 % at n=2048 against 443, 473 with view groups 4 views
-    // apart and (v, d) pairs)
-    int fwd_chunk_rows = 474;
+    // chunked forward: chunk shape; 484 = 16-row chunks staged by bulk
+    // copies of the tensor memory access unit on mbarriers, bundles of 8
+    // views x 128 cells, two threads per cell on 4 interleaved views each,
+    // each half-warp on 8 cells x 2 adjacent views, packed sums,
+    // absolute-position pairs, both pairs loaded per sample, 3 blocks/SM
+    // (-5.6 % at n=2048 against 474, the same staged by per-lane cp.async;
+    // 474 is -2 % against 473, which takes the lower pair from the previous
+    // sample where the column did not move, and -18 % against 443, 473 with
+    // view groups 4 views apart and (v, d) pairs)
+    int fwd_chunk_rows = 484;
     // staged backprojector variant: 48 = 4 blocks/SM, packed FP32 pairs of
     // rows, floor taken by FP32 adds, windows copied with cp.async, view loop
     // unrolled 4 times, absolute-position sinogram pairs, warps on 8 x 4
@@ -237,6 +239,9 @@ void free_plan3d(Plan3d *p);
 
 int launch_plan2d_tables(Plan2d &p, cudaStream_t s);
 int launch_relayout2d(const Plan2d &p, const float *vol, cudaStream_t s);
+// Reads and clears the count of bounded waits that gave up in this
+// library's kernels on the current device (cg_wait_timeouts).
+int take_wait_timeouts(unsigned long long *count);
 bool cslab_abs(int rows);
 bool bwd_abs(int min_blocks);
 int launch_forward2d(const Plan2d &p, float *sino, cudaStream_t s);
@@ -320,6 +325,50 @@ __device__ __forceinline__ FloorSplit floor_split(float x, int base) {
     return {__fadd_rn(x, -k), __float_as_uint(t) - (0x4B400000u + (unsigned)base)};
 }
 
+// ---- bulk copies by the tensor-memory-access unit, completed on an mbarrier
+// (PTX cp.async.bulk / mbarrier, sm_90 and later).  Addresses are 32-bit
+// shared-window addresses.
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+// makes the barriers' initialisation visible to the asynchronous proxy
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+// orders this thread's earlier shared-memory accesses before later bulk copies
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+// the barrier's one expected arrival, announcing `bytes` of copies
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+// global -> shared copy of `bytes` (a multiple of 16; both addresses 16-byte
+// aligned), counted against the barrier's transaction bytes
+__device__ __forceinline__ void bulk_copy_g2s(unsigned dst, const void *src, unsigned bytes,
+                                              unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::
+            "r"(dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+// waits for the barrier's phase `parity` to complete, at most `limit` tries;
+// false when it gave up
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int limit) {
+    for (int i = 0; i < limit; ++i) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
 // Sample parameter of ray-march step k + 1: the reference's running sum t + h
 // (forward_3d.hpp:85-92), or with `exact` tmin + (k + 1) h by one FMA, so
 // that no rounding accumulates along the ray.

@@ -412,9 +412,20 @@ int launch_slab(const Plan2d &p, float *sino, cudaStream_t s) {
 
 }  // namespace
 
+__device__ unsigned long long g_wait_timeouts = 0;
+
+int take_wait_timeouts(unsigned long long *count) {
+    CG_TRY_CUDA(cudaMemcpyFromSymbol(count, g_wait_timeouts, sizeof(*count)));
+    const unsigned long long zero = 0;
+    CG_TRY_CUDA(cudaMemcpyToSymbol(g_wait_timeouts, &zero, sizeof(zero)));
+    return CG_OK;
+}
+
 // True for the chunked forward's shapes that read the absolute-position
 // layouts (relayout2d_tile<true>).
-bool cslab_abs(int rows) { return rows == 463 || rows == 473 || rows == 474; }
+bool cslab_abs(int rows) {
+    return rows == 463 || rows == 473 || rows == 474 || rows == 484;
+}
 
 // True for the staged backprojector's shapes that read the absolute-position
 // sinogram pairs (relayout_sino2d_elem<true>).
@@ -502,8 +513,12 @@ __device__ __forceinline__ unsigned cs_column(float p, int c0, unsigned cmax, fl
 // stepping towards smaller rows are summed in reverse), so the matched
 // adjoint is this forward's transpose up to the order of summation.  A chunk
 // whose window does not fit reads global memory.
+// Waits (mbarrier tries) before a bulk copy counts as lost: far beyond any
+// copy's latency; the kernel then records the timeout and goes on.
+constexpr int kWaitTries = 1 << 22;
+
 template <int K, int S, int T, bool PK, bool REUSE = false, int VS = 1, int NG = kCs2G,
-          int MB = 0, int MAP = 0, bool ABS = false>
+          int MB = 0, int MAP = 0, bool ABS = false, bool TMA = false>
 __global__ void __launch_bounds__(T * VS, MB)
     k_fwd2d_cslab(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
                   float *__restrict__ sino, const float2 *__restrict__ tsrc,
@@ -637,15 +652,61 @@ __global__ void __launch_bounds__(T * VS, MB)
         }
     };
 
-    if (nch > 0) stage(0, 0);
-    asm volatile("cp.async.commit_group;\n" ::);
-    for (int ci = 0; ci < nch; ++ci) {
-        asm volatile("cp.async.wait_group 0;\n" ::);
+    // TMA: the chunk's K + 1 window rows come by bulk copies of the tensor
+    // memory access unit, one per row issued by lanes of warp 0, completed on
+    // the buffer's mbarrier (one arrival carrying the bytes); the barrier at
+    // the top of each chunk still guards the buffer being refilled
+    __shared__ __align__(8) unsigned long long s_bar[2];
+    const unsigned bar0 = (unsigned)__cvta_generic_to_shared(&s_bar[0]);
+    auto stage_tma = [&](int ci, int buf) {
+        const int win = ci < kCs2MaxChunks ? s_win[ci] : -1;
+        if (win < 0 || warp != 0) return;
+        const int c0 = win >> 16, wx = win & 0xffff, r0 = rmin + ci * K;
+        const unsigned bar = bar0 + 8u * (unsigned)buf;
+        const unsigned row_bytes = (unsigned)wx * (unsigned)sizeof(float2);
+        if (lane == 0) {
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(bar, (unsigned)(K + 1) * row_bytes);
+        }
+        __syncwarp();
+        const unsigned base = (unsigned)__cvta_generic_to_shared(cwin + buf * kBuf);
+        for (int row = lane; row <= K; row += 32) {
+            const int q = min(r0 + row, qmax + 1);
+            bulk_copy_g2s(base + (unsigned)(row * S) * (unsigned)sizeof(float2),
+                          lay + (size_t)(q + kPad) * pitch + c0, row_bytes, bar);
+        }
+    };
+    unsigned phases = 0;  // TMA: completed phases of each buffer's barrier, mod 2
+    if constexpr (TMA) {
+        if (threadIdx.x == 0) {
+            mbar_init(bar0, 1);
+            mbar_init(bar0 + 8u, 1);
+            mbar_fence_init();
+        }
         __syncthreads();
-        if (ci + 1 < nch) stage(ci + 1, (ci + 1) & 1);
+        if (nch > 0) stage_tma(0, 0);
+    } else {
+        if (nch > 0) stage(0, 0);
         asm volatile("cp.async.commit_group;\n" ::);
+    }
+    for (int ci = 0; ci < nch; ++ci) {
+        if constexpr (!TMA) asm volatile("cp.async.wait_group 0;\n" ::);
+        __syncthreads();
+        if constexpr (TMA) {
+            if (ci + 1 < nch) stage_tma(ci + 1, (ci + 1) & 1);
+        } else {
+            if (ci + 1 < nch) stage(ci + 1, (ci + 1) & 1);
+            asm volatile("cp.async.commit_group;\n" ::);
+        }
         const int r0 = rmin + ci * K;
         const int win = ci < kCs2MaxChunks ? s_win[ci] : -1;
+        if (TMA && win >= 0) {
+            const int b = ci & 1;
+            if (!mbar_wait(bar0 + 8u * (unsigned)b, (phases >> b) & 1u, kWaitTries) &&
+                threadIdx.x == 0)
+                atomicAdd(&g_wait_timeouts, 1ull);
+            phases ^= 1u << b;
+        }
         if (win >= 0) {
             const int c0 = (win >> 16) - kPad, wx = win & 0xffff;
             const unsigned cmax = (unsigned)(wx - 1);
@@ -700,7 +761,7 @@ __global__ void __launch_bounds__(T * VS, MB)
             }
         }
     }
-    asm volatile("cp.async.wait_group 0;\n" ::);
+    if constexpr (!TMA) asm volatile("cp.async.wait_group 0;\n" ::);
 
 #pragma unroll
     for (int g = 0; g < GV; ++g) {
@@ -729,7 +790,8 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
     if (nv <= 0) return CG_OK;
     const int ng = rows == 438 || rows == 439 || rows == 440 || rows == 441 || rows == 442 ||
                            rows == 443 || rows == 444 || rows == 447 || rows == 451 ||
-                           rows == 453 || rows == 463 || rows == 473 || rows == 474
+                           rows == 453 || rows == 463 || rows == 473 || rows == 474 ||
+                           rows == 484
                        ? 8
                    : rows == 448 || rows == 449 || rows == 450   ? 16
                                                                  : kCs2G;  // views per bundle
@@ -770,6 +832,7 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
         case 463: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 1, true>, 16, 256, 128, 2);
         case 473: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 2, true>, 16, 256, 128, 2);
         case 474: return go(k_fwd2d_cslab<16, 256, 128, true, false, 2, 8, 3, 2, true>, 16, 256, 128, 2);
+        case 484: return go(k_fwd2d_cslab<16, 256, 128, true, false, 2, 8, 3, 2, true, true>, 16, 256, 128, 2);
         case 451: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 4, 2>, 8, 256, 128, 2);
         case 444: return go(k_fwd2d_cslab<16, 192, 128, true, true, 2, 8, 4, 1>, 16, 192, 128, 2);
         case 449: return go(k_fwd2d_cslab<8, 256, 64, true, true, 4, 16, 3>, 8, 256, 64, 4);

@@ -46,6 +46,13 @@ const char *cg_last_error(void);
 /* ABI version: major * 10000 + minor * 100 + patch. */
 int cg_version(void);
 
+/* Number of bounded waits (on asynchronous copies) that gave up in this
+ * library's kernels on the current device since the last call, which the
+ * call then clears.  Every wait in a kernel has an iteration limit so that a
+ * lost copy cannot hang the GPU; a nonzero count means results computed
+ * since the last call are not to be trusted.  No reference counterpart. */
+int cg_wait_timeouts(unsigned long long *count);
+
 /* ------------------------------------------------------------------ 2D -- */
 
 typedef struct cg_plan2d cg_plan2d;
@@ -114,7 +121,7 @@ int cg_plan2d_get_algorithm(const cg_plan2d *plan, int *forward, int *backward);
 /* Kernel shape of the chunked forward (used by forward algorithms 4 and 5)
  * and variant of the staged backprojector (backward algorithms 2 and 3); -1
  * keeps the current one.  Shapes: 4, 104, 108, 204, 304, 308, 404, 408, 414,
- * 418, 428, 438-444, 447-451, 453, 463, 473, 474 (default); variants: 3, 4,
+ * 418, 428, 438-444, 447-451, 453, 463, 473, 474, 484 (default); variants: 3, 4,
  * 5, 14, 24-28, 37, 38, 48 (default).  Every shape computes the reference's
  * samples and weights; they differ in rows per chunk, views per bundle,
  * threads per cell, pair layout and register bounds, so the fastest depends

@@ -335,7 +335,7 @@ def test_staged_backprojector_shapes(cuda_device, monkeypatch, shape):
 
 @pytest.mark.parametrize("shape", [4, 104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438,
                                    439, 440, 441, 442, 443, 444, 447, 448, 449, 450, 451, 453,
-                                   463, 473, 474])
+                                   463, 473, 474, 484])
 def test_chunked_forward_shapes(cuda_device, monkeypatch, shape):
     """Every compiled shape of the chunked forward (CURADON_GB300_ALGO
     fwd2d=cslab<shape>: rows per chunk, bundle width, packed sums, pair reuse,
@@ -352,6 +352,31 @@ def test_chunked_forward_shapes(cuda_device, monkeypatch, shape):
     e = rel_l2(s, oracle.fwd2d(g, ph))
     print(f"shape {shape} fwd rel-L2 {e:.2e}")
     assert e < TOL
+
+
+@pytest.mark.parametrize("n", [1024, 2048])
+def test_tma_staging_equals_cp_async_staging(cuda_device, monkeypatch, n):
+    """Shape 484 stages the chunk windows with bulk copies of the tensor
+    memory access unit (mbarrier completion) instead of per-lane cp.async
+    (shape 474); the arithmetic is the same, so the sinograms must be equal
+    bit for bit, and no bounded wait may have given up."""
+    from curadon_gb300.backend import wait_timeouts
+
+    g = fan_config(n, n // 2)
+    ph = torch.as_tensor(ellipses_2d(n, 7).numpy(), device=cuda_device).contiguous()
+    out = {}
+    wait_timeouts()
+    for shape in (474, 484):
+        monkeypatch.setenv("CURADON_GB300_ALGO", f"fwd2d=cslab{shape}")
+        geom = FanGeometry(**g, device=cuda_device.index or 0)
+        geom.plan
+        monkeypatch.delenv("CURADON_GB300_ALGO")
+        s = torch.zeros(geom.sinogram_shape(), device=cuda_device)
+        forward(ph, s, geom)
+        torch.cuda.synchronize()
+        out[shape] = s
+    assert wait_timeouts() == 0
+    assert torch.equal(out[474], out[484])
 
 
 def test_full_size_backprojection_cross_check(cuda_device):
