@@ -66,3 +66,31 @@ def test_fbp_reconstructs_phantom(cuda_device):
     b = (x - x.mean()).flatten()
     corr = float((a @ b) / (a.norm() * b.norm()))
     assert corr > 0.9, corr
+
+
+@pytest.mark.gpu
+def test_packed_filter_equals_scalar_filter(cuda_device, tmp_path):
+    """The filter runs on pairs of rows with packed FMAs; its accumulation
+    order per output is that of the one-row kernel (selected in a child
+    process by CURADON_GB300_FILTER=scalar), so the results are equal bit
+    for bit, odd row counts included."""
+    import os
+    import subprocess
+    import sys
+
+    import torch
+
+    from curadon_gb300.fbp import filter_sinogram
+
+    rng = np.random.default_rng(5)
+    s = rng.uniform(0, 1, (37, 1449)).astype(np.float32)
+    np.save(tmp_path / "s.npy", s)
+    out = filter_sinogram(torch.as_tensor(s, device=cuda_device), "shepp-logan").cpu().numpy()
+    code = ("import numpy as np, torch, sys\n"
+            "from curadon_gb300.fbp import filter_sinogram\n"
+            f"s = np.load(r'{tmp_path / 's.npy'}')\n"
+            "o = filter_sinogram(torch.as_tensor(s, device='cuda'), 'shepp-logan').cpu().numpy()\n"
+            f"np.save(r'{tmp_path / 'o.npy'}', o)\n")
+    env = dict(os.environ, CURADON_GB300_FILTER="scalar")
+    subprocess.run([sys.executable, "-c", code], check=True, env=env, timeout=300)
+    assert np.array_equal(out, np.load(tmp_path / "o.npy"))
