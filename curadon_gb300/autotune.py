@@ -27,7 +27,7 @@ from ._lib import CuradonError
 # the chunked forward and variants of the staged backprojector
 FORWARD_CANDIDATES = (("texture", None), ("chunked", 484), ("chunked", 474),
                       ("chunked", 443))
-BACKWARD_CANDIDATES = (("shared", 48), ("shared", 38), ("shared", 27), ("texture", None))
+BACKWARD_CANDIDATES = (("shared", 68), ("shared", 48), ("shared", 27), ("texture", None))
 
 _cache: dict[tuple, dict] = {}
 

@@ -65,7 +65,7 @@ void free_plan3d(Plan3d *p) {
 constexpr int kFwdChunkShapes[] = {4,   104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438, 439,
                                    440, 441, 442, 443, 444, 447, 448, 449, 450, 451, 453, 463, 473,
                                    474, 484};
-constexpr int kBwdStagedVariants[] = {3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38, 48};
+constexpr int kBwdStagedVariants[] = {3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38, 48, 68};
 
 template <size_t N>
 bool listed(const int (&list)[N], int v) {
@@ -79,8 +79,8 @@ bool listed(const int (&list)[N], int v) {
 // "fwd2d=tex,bwd2d_minb=4".  Keys: fwd2d = alu | tex | slab | cslab |
 // cslab<shape> | hyb<1..7> | split<0..16>; bwd2d = alu | tex | smem |
 // split<0..16>; bwd2d_minb = 3 | 4 | 5 | 14 | 24 | 25 | 26 | 27 | 28 | 37 | 38 |
-// 48 (staged backprojector shapes; 37 / 38: 27 / 28 on absolute-position
-// pairs; 48: 38 with 8 x 4-pixel warps); adj2d = pair | quad; fwd3d = alu | tex3 | tex2l | slab | quad |
+// 48 | 68 (staged backprojector shapes; 37 / 38: 27 / 28 on absolute-position
+// pairs; 48: 38 with 8 x 4-pixel warps; 68: 48 with rows by bulk copies); adj2d = pair | quad; fwd3d = alu | tex3 | tex2l | slab | quad |
 // mixed; fwd3d_tex = 0..8 (texture warps of 8 in forward 5);
 // fwd3d_block = BXxBYxBZ;
 // bwd3d = scalar | pk | pkmagic | quad (backward 0) | ax8m5 | ax8 | ax16 |

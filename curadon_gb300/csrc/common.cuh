@@ -130,15 +130,18 @@ struct Plan2d {
     // sample where the column did not move, and -18 % against 443, 473 with
     // view groups 4 views apart and (v, d) pairs)
     int fwd_chunk_rows = 484;
-    // staged backprojector variant: 48 = 4 blocks/SM, packed FP32 pairs of
-    // rows, floor taken by FP32 adds, windows copied with cp.async, view loop
-    // unrolled 4 times, absolute-position sinogram pairs, warps on 8 x 4
-    // pixels (default, measured fastest: -2 % against 38, the same with warps
-    // on 32 x 1 pixels; 38 is -6.5 % against 27, the same unrolled twice on
-    // (t, d) pairs); 37 = 38 unrolled twice; 24 = 27 with register copies; 25 / 26 = 24
+    // staged backprojector variant: 68 = 4 blocks/SM, packed FP32 pairs of
+    // rows, floor taken by FP32 adds, window rows by bulk copies of the tensor
+    // memory access unit (pair-wise cp.async where a window reaches past the
+    // row), view loop unrolled 4 times, absolute-position sinogram pairs,
+    // warps on 8 x 4 pixels (default, measured fastest: -5 % against 48, the
+    // same staged pair by pair with cp.async; 48 is -2 % against 38, the same
+    // with warps on 32 x 1 pixels; 38 is -6.5 % against 27, the same unrolled
+    // twice on (t, d) pairs); 37 = 38 unrolled twice; 24 = 27 with register
+    // copies; 25 / 26 = 24
     // with the view loop unrolled 4 / 1 times; 28 = 27 unrolled 4 times; 14 =
     // 24 with the conversion unit's floor; 3, 4, 5 = scalar at 3..5 blocks/SM
-    int bwd_min_blocks = 48;
+    int bwd_min_blocks = 68;
 
     // row pitches of layA / layB in pairs, even so every row starts on 16 bytes
     int pitchA() const { return (W + 2 * kPad + 1) & ~1; }

@@ -429,7 +429,9 @@ bool cslab_abs(int rows) {
 
 // True for the staged backprojector's shapes that read the absolute-position
 // sinogram pairs (relayout_sino2d_elem<true>).
-bool bwd_abs(int min_blocks) { return min_blocks == 37 || min_blocks == 38 || min_blocks == 48; }
+bool bwd_abs(int min_blocks) {
+    return min_blocks == 37 || min_blocks == 38 || min_blocks == 48 || min_blocks == 68;
+}
 
 // True when the slab forward supports the plan's sizes.
 bool slab_supported(const Plan2d &p) {
@@ -931,16 +933,27 @@ constexpr int kSmWin = 128;   // pairs of one view's row staged for a tile
 // MAPQ: each warp covers 8 x 4 pixels (per row group) instead of 32 x 1, so
 // a half-warp's 16 lateral coordinates span fewer cells of the window row
 // (fewer shared-memory bank conflicts where the magnification is high).
+// BULK: each view's window row (kSmWin + 2 pairs, started on a 16-byte
+// boundary) comes by one bulk copy of the tensor memory access unit, issued
+// by a lane of warp 0 and completed on an mbarrier; rows whose window
+// reaches past the padded sinogram row are copied pair by pair with the
+// index clamp as before.
 template <bool PK, bool MAGIC = false, int VU = 2, bool CPA = false, bool ABS = false,
-          bool MAPQ = false>
+          bool MAPQ = false, bool BULK = false>
 __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                                                 const float2 *__restrict__ S,
                                                 const float4 *__restrict__ proj, int W, int H,
                                                 int det, int nangles, float sx, float sy, float ox,
                                                 float oy, float ds, int bx, int by) {
-    __shared__ float2 srow[kSmViews][kSmWin];
+    constexpr int kRow = BULK ? kSmWin + 2 : kSmWin;  // pairs per staged row
+    static_assert(kRow * sizeof(float2) % 16 == 0, "bulk rows are multiples of 16 bytes");
+    __shared__ __align__(16) float2 srow[kSmViews][kRow];
     __shared__ float4 sA[kSmViews], sB[kSmViews];
     __shared__ int skmin[kSmViews];
+    __shared__ int sbulk[kSmViews];
+    __shared__ __align__(8) unsigned long long s_bar;
+    const unsigned bar = (unsigned)__cvta_generic_to_shared(&s_bar);
+    unsigned phase = 0;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     const int xt = bx * 32, yt = by * (8 * kSmRows);
     const int x = xt + (MAPQ ? (int)((threadIdx.y & 3) * 8 + (threadIdx.x & 7)) : (int)threadIdx.x);
@@ -970,6 +983,12 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
         else acc2[r >> 1].x = fmaf(a, b, acc2[r >> 1].x);
     };
     const int pitch = det + 2 * kPad;
+    if constexpr (BULK) {
+        if (tid == 0) {
+            mbar_init(bar, 1);
+            mbar_fence_init();
+        }
+    }
     for (int v0 = 0; v0 < nangles; v0 += kSmViews) {
         const int nv = min(kSmViews, nangles - v0);
         __syncthreads();
@@ -990,15 +1009,62 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
             }
             // the window bound holds when the tile lies wholly in front of the
             // source (den > 0 at every corner, hence on the whole tile)
-            int k0 = INT_MIN;
+            int k0 = INT_MIN, bulk = 0;
             if (dmin > 0.f && lo >= -1e6f && hi <= 1e6f) {
                 const int a0 = (int)floorf(lo) - 1, a1 = (int)floorf(hi) + 1;
-                if (a1 - a0 + 1 <= kSmWin) k0 = a0;
+                if (a1 - a0 + 1 <= kSmWin) {
+                    if constexpr (BULK) {
+                        // start one pair earlier where needed so that the first
+                        // staged pair (element (v0 + tid) pitch + kPad + k0) is
+                        // even, i.e. on 16 bytes; the window then spans
+                        // [k0, k0 + kSmWin + 1]
+                        const int par = (int)(((long long)(v0 + tid) * pitch) & 1);
+                        k0 = a0 - ((a0 ^ par) & 1);
+                        bulk = k0 >= -kPad && k0 + kRow <= det + kPad;
+                    } else {
+                        k0 = a0;
+                    }
+                }
             }
             skmin[tid] = k0;
+            sbulk[tid] = bulk;
         }
         __syncthreads();
-        for (int e = tid; e < nv * kSmWin; e += 256) {
+        if constexpr (BULK) {
+            // warp 0: the bulk rows, one copy per lane, on the block's barrier
+            if (tid < 32) {
+                const bool mine = tid < nv && sbulk[tid];
+                const unsigned nb = __popc(__ballot_sync(0xffffffffu, mine));
+                if (tid == 0) {
+                    fence_proxy_async_smem();
+                    mbar_arrive_expect_tx(bar, nb * (unsigned)(kRow * sizeof(float2)));
+                }
+                __syncwarp();
+                if (mine) {
+                    fence_proxy_async_smem();
+                    bulk_copy_g2s((unsigned)__cvta_generic_to_shared(&srow[tid][0]),
+                                  S + (size_t)(v0 + tid) * pitch + kPad + skmin[tid],
+                                  (unsigned)(kRow * sizeof(float2)), bar);
+                }
+            }
+            // every warp: the other rows pair by pair (warp w: rows w, w + 8, ...)
+            const int w = tid >> 5, ln = tid & 31;
+            for (int j = w; j < nv; j += 8) {
+                const int k0 = skmin[j];
+                if (k0 == INT_MIN || sbulk[j]) continue;
+                for (int i = ln; i < kRow; i += 32) {
+                    const int k = min(max(k0 + i, -kPad), det);
+                    const unsigned d = (unsigned)__cvta_generic_to_shared(&srow[j][i]);
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d),
+                                 "l"(S + (size_t)(v0 + j) * pitch + kPad + k));
+                }
+            }
+            asm volatile("cp.async.wait_all;\n" ::);
+            if (!mbar_wait(bar, phase, kWaitTries) && tid == 0)
+                atomicAdd(&g_wait_timeouts, 1ull);
+            phase ^= 1u;
+        }
+        for (int e = tid; !BULK && e < nv * kSmWin; e += 256) {
             const int j = e / kSmWin, i = e - j * kSmWin;
             const int k0 = skmin[j];
             if (k0 == INT_MIN) continue;
@@ -1046,13 +1112,13 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                             f = ABS ? ub
                                     : __fadd2_rn(ub, __ffma2_rn(t, make_float2(-1.f, -1.f), M2));
                             const unsigned base = 0x4B400000u + (unsigned)(k0 - cq);
-                            l0 = min(__float_as_uint(t.x) - base, (unsigned)(kSmWin - 1));
-                            l1 = min(__float_as_uint(t.y) - base, (unsigned)(kSmWin - 1));
+                            l0 = min(__float_as_uint(t.x) - base, (unsigned)(kRow - 1));
+                            l1 = min(__float_as_uint(t.y) - base, (unsigned)(kRow - 1));
                         } else {
                             const float2 kf = make_float2(floorf(ub.x), floorf(ub.y));
                             f = ABS ? ub : __fadd2_rn(ub, make_float2(-kf.x, -kf.y));
-                            l0 = min((unsigned)((int)kf.x + cq - k0), (unsigned)(kSmWin - 1));
-                            l1 = min((unsigned)((int)kf.y + cq - k0), (unsigned)(kSmWin - 1));
+                            l0 = min((unsigned)((int)kf.x + cq - k0), (unsigned)(kRow - 1));
+                            l1 = min((unsigned)((int)kf.y + cq - k0), (unsigned)(kRow - 1));
                         }
                         const float2 t0 = sr[l0], t1 = sr[l1];
                         const float2 v = make_float2(fmaf(f.x, t0.y, t0.x), fmaf(f.y, t1.y, t1.x));
@@ -1068,7 +1134,7 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                         const float kf = floorf(ub);
                         const float f = ABS ? ub : ub - kf;
                         const unsigned li =
-                            min((unsigned)((int)kf + cq - k0), (unsigned)(kSmWin - 1));
+                            min((unsigned)((int)kf + cq - k0), (unsigned)(kRow - 1));
                         const float2 t = sr[li];
                         fma_acc(r, fmaf(f, t.y, t.x), w);
                     }
@@ -1103,13 +1169,13 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
 
 // MINB: resident blocks per SM the register allocation must allow
 template <int MINB, bool PK, bool MAGIC = false, int VU = 2, bool CPA = false, bool ABS = false,
-          bool MAPQ = false>
+          bool MAPQ = false, bool BULK = false>
 __global__ void __launch_bounds__(256, MINB)
     k_bwd2d_smem(float *__restrict__ vol, const float2 *__restrict__ S,
                  const float4 *__restrict__ proj, int W, int H, int det, int nangles, float sx,
                  float sy, float ox, float oy, float ds) {
-    bwd2d_smem_tile<PK, MAGIC, VU, CPA, ABS, MAPQ>(vol, S, proj, W, H, det, nangles, sx, sy, ox,
-                                                   oy, ds, blockIdx.x, blockIdx.y);
+    bwd2d_smem_tile<PK, MAGIC, VU, CPA, ABS, MAPQ, BULK>(vol, S, proj, W, H, det, nangles, sx,
+                                                         sy, ox, oy, ds, blockIdx.x, blockIdx.y);
 }
 
 }  // namespace
@@ -1161,17 +1227,18 @@ __global__ void __launch_bounds__(256)
 }
 
 // The staged tile of the single-problem default (packed rows, round-down
-// floor, cp.async windows, view loop unrolled 4 times, absolute-position
-// pairs, 8 x 4-pixel warps), so results equal it bit for bit.
+// floor, window rows by bulk copies, view loop unrolled 4 times,
+// absolute-position pairs, 8 x 4-pixel warps), so results equal it bit for
+// bit.
 __global__ void __launch_bounds__(256, 4)
     k_batch_bwd2d(const Prob2d *__restrict__ probs, const int *__restrict__ start, int count) {
     const int i = batch_problem(start, count, blockIdx.x);
     const Prob2d &q = probs[i];
     const int local = blockIdx.x - start[i];
     const int gx = (q.W + 31) / 32;
-    bwd2d_smem_tile<true, true, 4, true, true, true>(q.vol, q.sinoP, q.bproj, q.W, q.H, q.det,
-                                                     q.nangles, q.sx, q.sy, q.ox, q.oy, q.ds,
-                                                     local % gx, local / gx);
+    bwd2d_smem_tile<true, true, 4, true, true, true, true>(q.vol, q.sinoP, q.bproj, q.W, q.H,
+                                                           q.det, q.nangles, q.sx, q.sy, q.ox,
+                                                           q.oy, q.ds, local % gx, local / gx);
 }
 
 }  // namespace
@@ -1264,9 +1331,10 @@ int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s, int rows
         case 37: go(k_bwd2d_smem<4, true, true, 2, true, true>); break;
         case 38: go(k_bwd2d_smem<4, true, true, 4, true, true>); break;
         case 48: go(k_bwd2d_smem<4, true, true, 4, true, true, true>); break;
+        case 68: go(k_bwd2d_smem<4, true, true, 4, true, true, true, true>); break;
         case 28: go(k_bwd2d_smem<4, true, true, 4, true>); break;
         case 24: go(k_bwd2d_smem<4, true, true>); break;
-        default: go(k_bwd2d_smem<4, true, true, 4, true, true, true>); break;
+        default: go(k_bwd2d_smem<4, true, true, 4, true, true, true, true>); break;
     }
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;

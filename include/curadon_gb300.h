@@ -122,7 +122,7 @@ int cg_plan2d_get_algorithm(const cg_plan2d *plan, int *forward, int *backward);
  * and variant of the staged backprojector (backward algorithms 2 and 3); -1
  * keeps the current one.  Shapes: 4, 104, 108, 204, 304, 308, 404, 408, 414,
  * 418, 428, 438-444, 447-451, 453, 463, 473, 474, 484 (default); variants: 3, 4,
- * 5, 14, 24-28, 37, 38, 48 (default).  Every shape computes the reference's
+ * 5, 14, 24-28, 37, 38, 48, 68 (default).  Every shape computes the reference's
  * samples and weights; they differ in rows per chunk, views per bundle,
  * threads per cell, pair layout and register bounds, so the fastest depends
  * on the geometry (no reference counterpart: the reference has one kernel

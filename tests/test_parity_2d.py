@@ -314,7 +314,7 @@ def test_split_backward_shares_and_graph(cuda_device, monkeypatch, k):
     assert torch.equal(out, b)
 
 
-@pytest.mark.parametrize("shape", [3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38, 48])
+@pytest.mark.parametrize("shape", [3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38, 48, 68])
 def test_staged_backprojector_shapes(cuda_device, monkeypatch, shape):
     """Every compiled shape of the staged backprojector (CURADON_GB300_ALGO
     bwd2d_minb=...: blocks per SM, packed rows, floor by FP32 adds, view-loop
@@ -377,6 +377,35 @@ def test_tma_staging_equals_cp_async_staging(cuda_device, monkeypatch, n):
         out[shape] = s
     assert wait_timeouts() == 0
     assert torch.equal(out[474], out[484])
+
+
+@pytest.mark.parametrize("n,nangles", [(1024, 512), (2048, 300), (333, 77)])
+def test_bulk_staged_backprojector_equals_pairwise_staging(cuda_device, monkeypatch, n,
+                                                           nangles):
+    """Variant 68 stages the window rows with bulk copies (one per view,
+    started on 16 bytes, so one pair wider) instead of pair by pair
+    (variant 48); the samples and sums are the same, so the volumes must be
+    equal bit for bit, and no bounded wait may have given up.  Odd detector
+    widths put every other view row on an odd element."""
+    from curadon_gb300.backend import wait_timeouts
+
+    g = fan_config(n, nangles)
+    rng = np.random.default_rng(n)
+    sino = torch.as_tensor(rng.uniform(0, 1, (nangles, g["det_shape"])).astype(np.float32),
+                           device=cuda_device)
+    out = {}
+    wait_timeouts()
+    for variant in (48, 68):
+        monkeypatch.setenv("CURADON_GB300_ALGO", f"bwd2d=smem,bwd2d_minb={variant}")
+        geom = FanGeometry(**g, device=cuda_device.index or 0)
+        geom.plan
+        monkeypatch.delenv("CURADON_GB300_ALGO")
+        v = torch.zeros(tuple(geom.vol_shape), device=cuda_device)
+        backward(sino, v, geom)
+        torch.cuda.synchronize()
+        out[variant] = v
+    assert wait_timeouts() == 0
+    assert torch.equal(out[48], out[68])
 
 
 def test_full_size_backprojection_cross_check(cuda_device):
