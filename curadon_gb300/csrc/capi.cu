@@ -547,10 +547,10 @@ int cg_plan2d_create(cg_plan2d **plan, int device, uint32_t vol_prec, const uint
     p->det = (int)det_count, p->ds = det_spacing, p->doff = det_offset;
     p->nangles = (int)nangles, p->pitch = det_pitch, p->COR = COR;
     p->vol_bits = (int)vol_prec, p->det_bits = (int)det_prec;
-    // measured on GB300 (n-sweep): the chunked forward (shape 473) is 6 %
-    // faster than the texture unit at 768^2, 13 % at 896^2, 19 % at 1024^2,
-    // 34 % at 2048^2; even at 640^2, 16 % slower at 512^2
-    if ((long long)p->W * p->H >= 768LL * 768) p->algo_fwd = 4;
+    // measured on GB300 (n-sweep): the chunked forward (shape 484) takes 5 %
+    // less time than the texture unit at 704^2, 11 % at 768^2, 25 % at
+    // 1024^2, 39 % at 2048^2; even at 640^2, 5 % more at 512^2
+    if ((long long)p->W * p->H >= 704LL * 704) p->algo_fwd = 4;
     apply_algo_env(p.get(), nullptr);
     int rc = CG_OK;
     auto fail = [&](int code) {
@@ -608,7 +608,7 @@ int cg_plan2d_create_vec(cg_plan2d **plan, int device, uint32_t vol_prec,
     CG_REQUIRE(guard.ok(), "cannot select device");
     p->device = device;
     p->vec = true;
-    if ((long long)p->W * p->H >= 768LL * 768) p->algo_fwd = 4;
+    if ((long long)p->W * p->H >= 704LL * 704) p->algo_fwd = 4;
     apply_algo_env(p.get(), nullptr);
     p->algo_bwd = 2;  // the staged backprojector is the one driven by the projective table
     int rc = CG_OK;

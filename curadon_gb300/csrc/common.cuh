@@ -109,7 +109,7 @@ struct Plan2d {
     // share of the views;
     // backprojection 0 = registers, 1 = texture unit, 2 = shared-memory rows.
     // Defaults: the fastest measured on GB300 (2D n-sweep); the forward
-    // becomes chunked for volumes of 768^2 pixels and more (cg_plan2d_create).
+    // becomes chunked for volumes of 704^2 pixels and more (cg_plan2d_create).
     int algo_fwd = 1, algo_bwd = 2;
     int tex_eighths = 4;              // hybrid forward: share of warps on the texture unit
     // split forward (algorithm 5): sixteenths of the views projected by the

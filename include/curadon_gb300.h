@@ -113,7 +113,7 @@ int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by);
  * reference does; the other algorithms filter in FP32, and cg_adjoint_2d is
  * the transpose of forward algorithms 0, 3 and 4 (exact for 0 and 3; 4 takes
  * the same samples and weights, summed in another order).  A new plan starts
- * at the fastest measured combination: forward 4 from 768^2 pixels, else 1;
+ * at the fastest measured combination: forward 4 from 704^2 pixels, else 1;
  * backward 2. */
 int cg_plan2d_set_algorithm(cg_plan2d *plan, int forward, int backward);
 int cg_plan2d_get_algorithm(const cg_plan2d *plan, int *forward, int *backward);
