@@ -36,19 +36,6 @@ sys.path.insert(0, str(ROOT))
 
 import numpy as np  # noqa: E402
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
-# the ncu captures summarised in profiles/, by workload and kernel; None
-# where not captured.
-NCU_TRAFFIC = {
-    ("fan2048", "k_fwd2d_cslab"): 83_357_440,  # profiles/k_fwd2d_cslab_fan2048.md capture
-    ("fan2048", "k_bwd2d_smem"): 64_185_344,   # profiles/k_bwd2d_smem_fan2048.md
-    ("fan2048", "k_fwd2d_tex"): 17_007_744,    # the texture-unit forward (algorithm 1)
-    ("cone256", "k_fwd3d_quad"): 2_015_147_008,  # profiles/k_fwd3d_quad_cone256.md (algorithm 5)
-    ("cone256", "k_bwd3d_ax"): 500_470_784,      # profiles/k_bwd3d_ax_cone256.md
-    ("cone256", "k_fwd3d_tex3"): 1_281_753_856,  # profiles/k_bwd3d_cone256.md
-    ("cone256", "k_bwd3d"): 504_137_984,
-}
-
 # Main kernel of each operator by the plan's algorithm name.
 KERNELS = {
     ("fan", "forward", "texture"): "k_fwd2d_tex", ("fan", "forward", "chunked"): "k_fwd2d_cslab",
@@ -70,9 +57,14 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference", "reference-gpu"])
     p.add_argument("--workload", default="fan2048",
                    help="fan<n> (n-sweep: n x n, n views), cone256 / cone512, serve "
-                        "(served reconstruction stream vs the plain loop) or batch (64 "
-                        "jittered problems, batched gradient descent vs the plain loop)")
+                        "(served reconstruction stream vs the plain loop), batch (64 "
+                        "jittered problems, batched gradient descent vs the plain loop) or "
+                        "sweep (the 2D n-sweep against the reference's CUDA operators)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--sweep-sizes", default="64,128,256,512,1024,2048",
+                   help="image sizes of --workload sweep")
+    p.add_argument("--no-reference-gpu", action="store_true",
+                   help="skip the reference's own CUDA operators beside ours (default run)")
     p.add_argument("--batch-forward", default="texture", choices=["texture", "registers"],
                    help="forward algorithm of the batch workload")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
@@ -142,12 +134,40 @@ def fan_sample_count(g) -> int:
     return total
 
 
-def cone_sample_estimate(g) -> int:
-    n = g["vol_shape"][0]
-    nangles = len(g["angles"])
-    det = g["det_shape"][0]
-    # rays through the volume ~ detector cells covering its shadow, ~n samples each
-    return int(nangles * det * det * 0.6 * n)
+def cone_sample_count(g, views: int = 8) -> int:
+    """Interpolated samples of one 3D forward (sum over rays that hit of
+    nsteps + 1, nsteps = ceil((tmax - tmin) ceil(|dir|))), evaluated in
+    float64 on ``views`` views spread over the circular orbit and scaled to
+    all views (every view of a circular orbit casts the same rays, rotated)."""
+    Z, Y, X = (int(v) for v in g["vol_shape"])
+    V, U = (int(v) for v in g["det_shape"])
+    sv, su = (float(v) for v in g["det_spacing"])
+    dso, dsd = float(g["DSO"]), float(g["DSD"])
+    ang = np.asarray(g["angles"], np.float64)
+    pick = ang[np.linspace(0, len(ang) - 1, min(views, len(ang))).astype(int)]
+    u = -su * U / 2 + su * 0.5 + su * np.arange(U)
+    v = -sv * V / 2 + sv * 0.5 + sv * np.arange(V)
+    uu, vv = np.meshgrid(u, v)
+    ext = np.array([X, Y, Z], np.float64)
+    total = 0
+    for phi in pick:
+        c, s_ = np.cos(phi), np.sin(phi)
+        # rotation about y (rotation.hpp:7-28 with theta = psi = 0)
+        rot = lambda x, y, z: (x * c + z * s_, y, -x * s_ + z * c)  # noqa: E731
+        src = np.array(rot(0.0, 0.0, -dso)) + ext / 2 - 0.5
+        det = np.stack(rot(uu, vv, np.full_like(uu, dsd - dso)), 0) + (ext / 2 - 0.5)[:, None, None]
+        d = det - src[:, None, None]
+        ns = np.ceil(np.sqrt((d * d).sum(0)))
+        tmin = np.full(uu.shape, np.finfo(np.float32).tiny)
+        tmax = np.full(uu.shape, np.finfo(np.float32).max, np.float64)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            for k in range(3):
+                t1, t2 = (-1.0 - src[k]) / d[k], (ext[k] + 1 - src[k]) / d[k]
+                tmin = np.fmin(np.fmax(t1, tmin), np.fmax(t2, tmin))
+                tmax = np.fmax(np.fmin(t1, tmax), np.fmin(t2, tmax))
+        hit = tmin <= tmax
+        total += int((np.ceil((tmax[hit] - tmin[hit]) * ns[hit]) + 1).sum())
+    return int(round(total * len(ang) / len(pick)))
 
 
 # ------------------------------------------------------------ clocks
@@ -239,17 +259,14 @@ def kernels_per_step(wl, geom) -> int:
     return f + b
 
 
-def run_ours(args, rank, world, local_rank):
+def make_problem(wl, dev, local_rank=0):
+    """(geometry, volume, sinogram, backprojection buffer) of a workload on
+    ``dev``, the volume a seeded phantom."""
     import torch
 
     import curadon_gb300 as cg
-    from curadon_gb300 import _build
     from curadon_gb300.phantom import ellipses_2d, ellipsoids_3d
 
-    _build.build()
-    dev = torch.device("cuda", local_rank)
-    torch.cuda.set_device(dev)
-    wl = workload(args.workload)
     g = wl["geom"]
     if wl["kind"] == "fan":
         geom = cg.FanGeometry(**g, device=local_rank)
@@ -258,19 +275,150 @@ def run_ours(args, rank, world, local_rank):
         geom = cg.ConeGeometry(**g, device=local_rank)
         vol = ellipsoids_3d(wl["n"], wl["seed"], device=dev).contiguous()
     sino = torch.zeros(geom.sinogram_shape(), device=dev)
-    vbp = torch.zeros_like(vol)
+    return geom, vol, sino, torch.zeros_like(vol)
+
+
+def time_steps(fwd, bwd, steps: int, warmup: int, flush, stream):
+    """Per-step forward and backprojection times (ms, CUDA events on
+    ``stream``, L2 flushed before each step outside the events)."""
+    import torch
+
+    for _ in range(warmup):
+        fwd(), bwd()
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+    for k in range(steps):
+        flush.zero_()
+        e0, e1, e2 = ev[k]
+        e0.record(stream)
+        fwd()
+        e1.record(stream)
+        bwd()
+        e2.record(stream)
+    torch.cuda.synchronize()
+    return ([ev[k][0].elapsed_time(ev[k][1]) for k in range(steps)],
+            [ev[k][1].elapsed_time(ev[k][2]) for k in range(steps)])
+
+
+def reference_ops():
+    """The reference's own CUDA operators (the oracle/_ref shim over its
+    header-only library, compiled for sm_103a), or (None, reason)."""
+    try:
+        import oracle
+        from oracle import build_ref
+
+        if build_ref.build() is None or not oracle.ref_available():
+            return None, "reference headers not staged, shim not built"
+        return oracle.RefOps(), ""
+    except Exception as e:  # reported in the JSON line, never fatal
+        return None, f"reference shim unavailable: {e}"
+
+
+def time_reference_gpu(ref, wl, vol, steps: int, warmup: int, flush, stream):
+    """Times the reference's operators on ``vol`` exactly as this library's
+    are timed: CUDA events on ``stream`` around each call, L2 flushed before
+    each step.  The reference's calls are synchronous and run on its own
+    streams, so an event pair spans the whole call, its host-side set-up
+    (texture arrays, geometry upload, synchronisations) included, as its
+    users see it.  Returns per-step forward / backprojection ms and the
+    sinogram it computed."""
+    import torch
+
+    g = wl["geom"]
+    dev = vol.device
+    if wl["kind"] == "fan":
+        h, n = ref.plan2d(g)
+        sino = torch.zeros((n, g["det_shape"]), device=dev)
+        vbp = torch.zeros_like(vol)
+
+        def fwd():
+            ref.forward2d(h, vol.data_ptr(), sino.data_ptr())
+
+        def bwd():
+            vbp.zero_()
+            ref.backward2d(h, vbp.data_ptr(), sino.data_ptr())
+    else:
+        h = None
+        sino = torch.zeros((len(g["angles"]), *g["det_shape"]), device=dev)
+        vbp = torch.zeros_like(vol)
+
+        def fwd():
+            ref.forward3d(g, vol.data_ptr(), sino.data_ptr())
+
+        def bwd():
+            vbp.zero_()
+            ref.backward3d(g, vbp.data_ptr(), sino.data_ptr())
+    try:
+        tf, tb = time_steps(fwd, bwd, steps, warmup, flush, stream)
+    finally:
+        if h is not None:
+            ref.destroy2d(h)
+    return tf, tb, sino
+
+
+def roofline_of(wl, ms_fwd, ms_bwd, algos, peaks):
+    """Roofline of the dominant operator: compulsory bytes per call over its
+    event-timed duration against the measured HBM copy peak, with the
+    interpolation rate and gather bandwidth beside it."""
+    g = wl["geom"]
+    if wl["kind"] == "fan":
+        nvox = wl["n"] * wl["n"]
+        nrays = len(g["angles"]) * g["det_shape"]
+        s_fwd = fan_sample_count(g)
+        gather = {"forward": 16, "backward": 8}
+        note = ("gather-bound (L1 / shared-memory data path and issue), not HBM-bound: the "
+                "compulsory bytes fit in L2; samples_per_s is the efficiency figure")
+    else:
+        nvox = wl["n"] ** 3
+        nrays = len(g["angles"]) * g["det_shape"][0] * g["det_shape"][1]
+        s_fwd = cone_sample_count(g)
+        gather = {"forward": 32, "backward": 16}
+        note = (f"gather-bound (L1 load and texture pipes), not HBM-bound: the {nvox * 4 >> 20} "
+                "MiB volume is read once per call and each block's working set (a band of "
+                "detector rows across many views) stays in L2; samples_per_s is the "
+                "efficiency figure")
+    s_bwd = nvox * len(g["angles"])
+    b_alg = {"forward": 4 * (nvox + nrays), "backward": 4 * (nrays + 2 * nvox)}
+    dom = "forward" if ms_fwd >= ms_bwd else "backward"
+    t_dom = (ms_fwd if dom == "forward" else ms_bwd) / 1e3
+    kernel = KERNELS.get((wl["kind"], dom, algos[dom]), dom)
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    achieved = b_alg[dom] / t_dom / 1e9
+    samples = s_fwd if dom == "forward" else s_bwd
+    return {"bound": "hbm", "kernel": kernel, "operator": dom,
+            "achieved": round(achieved, 3), "peak": peak, "peak_source": peak_src,
+            "unit": "GB/s", "frac": achieved / peak,
+            # DRAM bytes per launch come from an ncu capture of the same
+            # kernel, kept with the profiles, not from this run
+            "traffic": None, "algorithmic_bytes": b_alg[dom],
+            "samples_per_s": samples / t_dom,
+            "gather_GBps": samples * gather[dom] / t_dom / 1e9, "note": note}
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    import curadon_gb300 as cg
+    from curadon_gb300 import _build
+    from curadon_gb300.backend import raise_on_wait_timeouts
+
+    _build.build()
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    wl = workload(args.workload)
+    geom, vol, sino, vbp = make_problem(wl, dev, local_rank)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
     launches_per_step = kernels_per_step(wl, geom)
 
-    def step():
+    def fwd():
         cg.forward(vol, sino, geom)
+
+    def bwd():
         vbp.zero_()
         cg.backward(sino, vbp, geom)
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
 
     sampler = ClockSampler(local_rank) if rank == 0 else None
     if sampler:
@@ -279,21 +427,9 @@ def run_ours(args, rank, world, local_rank):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
-    for k in range(args.steps):
-        flush.zero_()
-        e0, e1, e2 = ev[k]
-        e0.record(stream)
-        cg.forward(vol, sino, geom)
-        e1.record(stream)
-        vbp.zero_()
-        cg.backward(sino, vbp, geom)
-        e2.record(stream)
-    torch.cuda.synchronize()
+    t_fwd, t_bwd = time_steps(fwd, bwd, args.steps, args.warmup, flush, stream)
     if world > 1:
         torch.distributed.barrier()
-    t_fwd = [ev[k][0].elapsed_time(ev[k][1]) for k in range(args.steps)]
-    t_bwd = [ev[k][1].elapsed_time(ev[k][2]) for k in range(args.steps)]
     total_ms = sum(t_fwd) + sum(t_bwd)
 
     # end to end: pinned host volume in, sinogram and backprojection out
@@ -329,6 +465,7 @@ def run_ours(args, rank, world, local_rank):
         torch.distributed.barrier()
     e2e_ms = sum(a.elapsed_time(b) for a, b in e_ev)
     clocks = sampler.stop() if sampler else None
+    raise_on_wait_timeouts()
 
     total_ms, e2e_ms, fwd_ms, bwd_ms = reduce_max([total_ms, e2e_ms, sum(t_fwd), sum(t_bwd)],
                                                   world, dev)
@@ -339,44 +476,12 @@ def run_ours(args, rank, world, local_rank):
     value = ops / (total_ms / 1e3)
     ms_fwd = fwd_ms / args.steps
     ms_bwd = bwd_ms / args.steps
-
-    # roofline of the dominant operator: compulsory bytes per call / its time
-    if wl["kind"] == "fan":
-        nvox = wl["n"] * wl["n"]
-        nrays = len(g["angles"]) * g["det_shape"]
-        s_fwd = fan_sample_count(g)
-        s_bwd = nvox * len(g["angles"])
-        gather = {"forward": 16, "backward": 8}
-    else:
-        nvox = wl["n"] ** 3
-        nrays = len(g["angles"]) * g["det_shape"][0] * g["det_shape"][1]
-        s_fwd = cone_sample_estimate(g)
-        s_bwd = nvox * len(g["angles"])
-        gather = {"forward": 32, "backward": 16}
-    b_alg = {"forward": 4 * (nvox + nrays), "backward": 4 * (nrays + 2 * nvox)}
-    dom = "forward" if ms_fwd >= ms_bwd else "backward"
-    t_dom = (ms_fwd if dom == "forward" else ms_bwd) / 1e3
-    algos = dict(zip(("forward", "backward"), geom.plan.algorithm))
-    kernel = KERNELS.get((wl["kind"], dom, algos[dom]), dom)
     peaks = {}
     try:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
     except (OSError, ValueError):
         pass
-    peak = peaks.get("hbm_gbs")
-    peak_src = "measured" if peak else "fallback"
-    peak = peak or 6800.0
-    achieved = b_alg[dom] / t_dom / 1e9
-    samples = s_fwd if dom == "forward" else s_bwd
-    traffic = NCU_TRAFFIC.get((wl["name"], kernel))
-    roofline = {"bound": "hbm", "kernel": kernel, "operator": dom,
-                "achieved": round(achieved, 3), "peak": peak,
-                "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "algorithmic_bytes": b_alg[dom],
-                "samples_per_s": samples / t_dom,
-                "gather_GBps": samples * gather[dom] / t_dom / 1e9,
-                "note": "gather-bound (L1/issue), not HBM-bound: the compulsory bytes are "
-                        "L2-resident; samples_per_s is the efficiency figure"}
+    algos = dict(zip(("forward", "backward"), geom.plan.algorithm))
 
     line = {
         "metric": "fwd/bwd proj ops/s", "value": value, "unit": "ops/s", "n_gpus": world,
@@ -388,13 +493,91 @@ def run_ours(args, rank, world, local_rank):
         "fwd_ops_s": args.steps * world / (fwd_ms / 1e3),
         "bwd_ops_s": args.steps * world / (bwd_ms / 1e3),
         "ms_forward": ms_fwd, "ms_backward": ms_bwd,
+        "algorithms": algos,
         "e2e": {"value": ops / (e2e_ms / 1e3), "unit": "ops/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches_per_step * args.steps,
-        "roofline": roofline,
+        "roofline": roofline_of(wl, ms_fwd, ms_bwd, algos, peaks),
         "clocks": clocks,
     }
+    if world == 1 and not args.no_reference_gpu:
+        line.update(reference_gpu_comparison(args, wl, vol, sino, flush, stream, ms_fwd,
+                                             ms_bwd))
+        if wl["name"] != "cone512":
+            line["cone512"] = cone512_comparison(args, dev, flush, stream)
     return line
+
+
+def reference_gpu_comparison(args, wl, vol, sino, flush, stream, ms_fwd, ms_bwd):
+    """The reference's own CUDA operators on the same workload, the same
+    steps and the same clock (the drop-in comparison), and the relative L2
+    distance between its sinogram and ours."""
+    ref, why = reference_ops()
+    if ref is None:
+        return {"reference_gpu": {"unavailable": why}}
+    tf, tb, s_ref = time_reference_gpu(ref, wl, vol, args.steps, args.warmup, flush, stream)
+    rf, rb = sum(tf) / len(tf), sum(tb) / len(tb)
+    rel = float((sino - s_ref).norm() / s_ref.norm())
+    return {
+        "reference_gpu": {"ms_forward": rf, "ms_backward": rb, "ms_per_step": rf + rb,
+                          "ops_s": 2e3 / (rf + rb), "steps": args.steps,
+                          "warmup": args.warmup,
+                          "timing": "CUDA events around each synchronous reference call, "
+                                    "L2 flushed before each step (as this library's)",
+                          "forward_rel_l2_vs_ours": rel},
+        "ref_gpu_ms_forward": rf, "ref_gpu_ms_backward": rb,
+        "vs_ref_gpu": {"forward": rf / ms_fwd, "backward": rb / ms_bwd,
+                       "step": (rf + rb) / (ms_fwd + ms_bwd)},
+    }
+
+
+def cone512_comparison(args, dev, flush, stream):
+    """The 3D 512^3 workload (720 views, 768^2 cells): this library's default
+    operators and the reference's, a few steps each, with the SM clock
+    sampled meanwhile."""
+    import torch
+
+    import curadon_gb300 as cg
+    from curadon_gb300.backend import raise_on_wait_timeouts
+
+    wl = workload("cone512")
+    steps, warmup = 5, 2
+    sampler = ClockSampler(dev.index or 0)
+    sampler.start()
+    time.sleep(0.2)
+    geom, vol, sino, vbp = make_problem(wl, dev, dev.index or 0)
+
+    def fwd():
+        cg.forward(vol, sino, geom)
+
+    def bwd():
+        vbp.zero_()
+        cg.backward(sino, vbp, geom)
+
+    tf, tb = time_steps(fwd, bwd, steps, warmup, flush, stream)
+    raise_on_wait_timeouts()
+    mf, mb = sum(tf) / steps, sum(tb) / steps
+    algos = dict(zip(("forward", "backward"), geom.plan.algorithm))
+    out = {"workload": wl["config"]["workload"], "steps": steps, "warmup": warmup,
+           "ms_forward": mf, "ms_backward": mb, "ms_per_step": mf + mb,
+           "ops_s": 2e3 / (mf + mb), "algorithms": algos,
+           "samples_per_s_forward": cone_sample_count(wl["geom"]) / (mf / 1e3)}
+    ref, why = reference_ops()
+    if ref is None:
+        out["reference_gpu"] = {"unavailable": why}
+    else:
+        del geom  # the reference allocates its own arrays
+        torch.cuda.empty_cache()
+        rf_, rb_, s_ref = time_reference_gpu(ref, wl, vol, steps, warmup, flush, stream)
+        rf, rb = sum(rf_) / steps, sum(rb_) / steps
+        hit = s_ref != 0
+        rel = float((sino[hit] - s_ref[hit]).norm() / s_ref[hit].norm())
+        out["reference_gpu"] = {"ms_forward": rf, "ms_backward": rb, "ms_per_step": rf + rb,
+                                "ops_s": 2e3 / (rf + rb), "forward_rel_l2_vs_ours": rel}
+        out["vs_ref_gpu"] = {"forward": rf / mf, "backward": rb / mb,
+                             "step": (rf + rb) / (mf + mb)}
+    out["clocks"] = sampler.stop()
+    return out
 
 
 # ------------------------------------------------------------ CPU (oracle)
@@ -444,19 +627,39 @@ def cpu_sample(wl, budget_s: float, threads: int):
 
 
 def run_reference_cpu(args, rank, world):
+    """The reference has no CPU path: its operators as restated by the FP64
+    oracle on all host cores.  Each timed step is one full forward and one
+    full backprojection of the workload; warm-up steps run on an eighth of
+    the views (they only warm the threads and caches)."""
     if rank != 0:
         return None
+    import oracle
+    from curadon_gb300.phantom import ellipses_2d, ellipsoids_3d
+
     wl = workload(args.workload)
+    g = wl["geom"]
+    kind = wl["kind"]
     threads = os.cpu_count() or 1
+    if kind == "fan":
+        vol = ellipses_2d(wl["n"], wl["seed"]).numpy()
+        fwd, bwd = oracle.fwd2d, oracle.bwd2d
+    else:
+        vol = ellipsoids_3d(wl["n"], wl["seed"]).numpy()
+        fwd, bwd = oracle.fwd3d, oracle.bwd3d
+    nviews = len(g["angles"])
+    warm = _sub_geom(g, kind, max(1, nviews // 8))
+    for _ in range(args.warmup):
+        bwd(warm, fwd(warm, vol, nthreads=threads).astype(np.float32), nthreads=threads)
     per_step = []
-    desc = ""
-    budget = 2.0
-    for k in range(args.warmup + args.steps):
-        ops_s, desc = cpu_sample(wl, budget, threads)
-        if k >= args.warmup:
-            per_step.append(2.0 / ops_s)
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        s = fwd(g, vol, nthreads=threads)
+        bwd(g, s.astype(np.float32), nthreads=threads)
+        per_step.append(time.perf_counter() - t0)
     total = sum(per_step)
     value = 2 * args.steps / total
+    desc = (f"full forward + backprojection per step ({nviews} views), FP64 oracle, "
+            f"{threads} threads (the reference has no CPU path; its operators restated)")
     return {
         "impl": "reference", "metric": "fwd/bwd proj ops/s", "value": value, "unit": "ops/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -464,80 +667,121 @@ def run_reference_cpu(args, rank, world):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded ellipse phantom)",
         "config": dict(wl["config"], parallelism="host cores"),
         "cpu_baseline": {"value": value, "unit": "ops/s", "cores": threads, "kind": "port",
-                         "sample": desc + " (the reference has no CPU path; its operators "
-                                          "restated by the oracle)"},
+                         "sample": desc},
         "e2e": {"value": value, "unit": "ops/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
 
 
 def run_reference_gpu(args, rank, world, local_rank):
+    """The reference's own CUDA operators (the oracle/_ref shim) alone, with
+    this library's clock: CUDA events around each synchronous call."""
     if rank != 0:
         return None
     import torch
 
-    import oracle
-    from oracle import build_ref
+    ref, why = reference_ops()
+    if ref is None:
+        return {"impl": "reference-gpu", "unavailable": why}
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    wl = workload(args.workload)
     from curadon_gb300.phantom import ellipses_2d, ellipsoids_3d
 
-    if build_ref.build() is None or not oracle.ref_available():
-        return {"impl": "reference-gpu", "unavailable": "reference headers not staged/built"}
-    ref = oracle.RefOps()
-    dev = torch.device("cuda", local_rank)
-    wl = workload(args.workload)
-    g = wl["geom"]
-    tf, tb = [], []
-    if wl["kind"] == "fan":
-        vol = ellipses_2d(wl["n"], wl["seed"], device=dev).contiguous()
-        h, n = ref.plan2d(g)
-        sino = torch.zeros((n, g["det_shape"]), device=dev)
-        vbp = torch.zeros_like(vol)
-
-        def fwd():
-            ref.forward2d(h, vol.data_ptr(), sino.data_ptr())
-
-        def bwd():
-            vbp.zero_()
-            ref.backward2d(h, vbp.data_ptr(), sino.data_ptr())
-    else:
-        vol = ellipsoids_3d(wl["n"], wl["seed"], device=dev).contiguous()
-        n = len(g["angles"])
-        sino = torch.zeros((n, *g["det_shape"]), device=dev)
-        vbp = torch.zeros_like(vol)
-
-        def fwd():
-            ref.forward3d(g, vol.data_ptr(), sino.data_ptr())
-
-        def bwd():
-            vbp.zero_()
-            ref.backward3d(g, vbp.data_ptr(), sino.data_ptr())
+    vol = (ellipses_2d(wl["n"], wl["seed"], device=dev) if wl["kind"] == "fan"
+           else ellipsoids_3d(wl["n"], wl["seed"], device=dev)).contiguous()
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
-    for _ in range(args.warmup):
-        fwd(), bwd()
-    torch.cuda.synchronize()
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        fwd()
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        bwd()
-        torch.cuda.synchronize()
-        t2 = time.perf_counter()
-        tf.append(t1 - t0)
-        tb.append(t2 - t1)
-    total = sum(tf) + sum(tb)
+    tf, tb, _ = time_reference_gpu(ref, wl, vol, args.steps, args.warmup, flush,
+                                   torch.cuda.current_stream(dev))
+    total = (sum(tf) + sum(tb)) / 1e3
     return {
         "impl": "reference-gpu", "metric": "fwd/bwd proj ops/s",
         "value": 2 * args.steps / total, "unit": "ops/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded ellipse phantom)", "config": wl["config"],
-        "fwd_ops_s": args.steps / sum(tf), "bwd_ops_s": args.steps / sum(tb),
-        "ms_forward": sum(tf) / args.steps * 1e3, "ms_backward": sum(tb) / args.steps * 1e3,
-        "timing": "wall clock around each synchronous reference call (its own protocol)",
+        "fwd_ops_s": args.steps / (sum(tf) / 1e3), "bwd_ops_s": args.steps / (sum(tb) / 1e3),
+        "ms_forward": sum(tf) / args.steps, "ms_backward": sum(tb) / args.steps,
+        "timing": "CUDA events around each synchronous reference call, L2 flushed per step",
     }
+
+
+# ------------------------------------------------------------ n-sweep
+
+def run_sweep(args):
+    """The 2D n-sweep against the reference's own CUDA operators: for n in
+    64 .. 2048 (n x n image, n views, ceil(sqrt(2) n) cells of 1.5, DSO 2n,
+    DSD 3n), forward and backprojection timed separately, 50 runs after 3
+    warm-ups each (the reference benchmark's protocol, benchmark/bench.py:
+    51-75), CUDA events around every call on both sides, L2 flushed before
+    every call; relative L2 of our outputs against the reference's (the
+    backprojection only up to 1024 views, above which the reference's chunks
+    race)."""
+    import torch
+
+    import curadon_gb300 as cg
+    from curadon_gb300 import _build
+    from curadon_gb300.backend import raise_on_wait_timeouts
+
+    _build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ref, why = reference_ops()
+    runs, warm = 50, 3
+
+    def timed(fn):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(runs):
+            flush.zero_()
+            a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a_.record(stream)
+            fn()
+            b_.record(stream)
+            b_.synchronize()
+            ts.append(a_.elapsed_time(b_))
+        return sum(ts) / len(ts)
+
+    rows = []
+    for n in [int(v) for v in args.sweep_sizes.split(",")]:
+        wl = workload(f"fan{n}")
+        geom, vol, sino, vbp = make_problem(wl, dev)
+        row = {"n": n, "views": n, "det": wl["geom"]["det_shape"],
+               "algorithms": dict(zip(("forward", "backward"), geom.plan.algorithm))}
+        row["ms_forward"] = timed(lambda: cg.forward(vol, sino, geom))
+        row["ms_backward"] = timed(lambda: cg.backward(sino, vbp, geom))
+        raise_on_wait_timeouts()
+        if ref is not None:
+            h, nv = ref.plan2d(wl["geom"])
+            s_ref = torch.zeros_like(sino)
+            b_ref = torch.zeros_like(vol)
+            row["ref_ms_forward"] = timed(lambda: ref.forward2d(h, vol.data_ptr(),
+                                                                s_ref.data_ptr()))
+            row["ref_ms_backward"] = timed(lambda: ref.backward2d(h, b_ref.data_ptr(),
+                                                                  s_ref.data_ptr()))
+            cg.forward(vol, sino, geom)
+            row["forward_rel_l2"] = float((sino - s_ref).norm() / s_ref.norm())
+            if nv <= 1024:
+                b_ref.zero_()
+                ref.backward2d(h, b_ref.data_ptr(), s_ref.data_ptr())
+                b = torch.zeros_like(vol)
+                cg.backward(s_ref, b, geom)
+                row["backward_rel_l2"] = float((b - b_ref).norm() / b_ref.norm())
+            ref.destroy2d(h)
+            row["vs_ref_forward"] = row["ref_ms_forward"] / row["ms_forward"]
+            row["vs_ref_backward"] = row["ref_ms_backward"] / row["ms_backward"]
+        rows.append(row)
+        print(json.dumps(row), file=sys.stderr, flush=True)
+        del geom, vol, sino, vbp
+        torch.cuda.empty_cache()
+    return {"metric": "fwd/bwd proj ops/s (n-sweep)", "unit": "ms per call",
+            "protocol": f"{runs} runs after {warm} warm-ups per operator, CUDA events, L2 "
+                        "flushed per call", "reference": why or "oracle/_ref shim (sm_103a)",
+            "rows": rows}
 
 
 # ------------------------------------------------------------ serving
@@ -823,7 +1067,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.workload == "serve":
+    if args.workload == "sweep":
+        line = run_sweep(args) if rank == 0 else None
+    elif args.workload == "serve":
         line = run_serve(args) if rank == 0 else None
     elif args.workload == "batch":
         line = run_batch(args) if rank == 0 else None

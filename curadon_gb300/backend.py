@@ -18,6 +18,7 @@ of bounds instead).
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 import torch
@@ -25,7 +26,8 @@ import torch
 from ._lib import check, load
 
 __all__ = ["plan_2d", "plan_2d_vec", "plan_3d", "forward_2d", "backward_2d", "adjoint_2d",
-           "forward_3d", "backward_3d"]
+           "forward_3d", "backward_3d", "wait_timeouts", "raise_on_wait_timeouts",
+           "WaitTimeoutError"]
 
 
 def _u64(a):
@@ -222,11 +224,37 @@ def _check_2d(vol, sino, plan: plan_2d):
 
 
 def wait_timeouts() -> int:
-    """Bounded waits that gave up in this library's kernels on the current
-    device since the last call (``cg_wait_timeouts``); 0 when all is well."""
+    """Thread blocks of this library's kernels on the current device whose
+    bounded wait for their own bulk copies gave up since the last call
+    (``cg_wait_timeouts``, which reads and clears the count; it waits for the
+    device).  0 when all is well; otherwise the outputs of the launches in
+    between are not to be trusted."""
     n = C.c_ulonglong()
     check(load().cg_wait_timeouts(C.byref(n)))
     return n.value
+
+
+class WaitTimeoutError(RuntimeError):
+    """A kernel's bounded wait for its own bulk copies gave up: the results
+    computed since the previous check are not to be trusted."""
+
+
+def raise_on_wait_timeouts() -> None:
+    """Raises ``WaitTimeoutError`` when a bounded wait gave up since the last
+    check (synchronises with the device).  The operators call it after every
+    launch when the environment variable ``CURADON_GB300_CHECK_WAITS`` is 1."""
+    n = wait_timeouts()
+    if n:
+        raise WaitTimeoutError(f"{n} thread block(s) gave up waiting for their bulk copies; "
+                               "the results since the last check are not to be trusted")
+
+
+_CHECK_WAITS = os.environ.get("CURADON_GB300_CHECK_WAITS", "0") == "1"
+
+
+def _after_launch() -> None:
+    if _CHECK_WAITS:
+        raise_on_wait_timeouts()
 
 
 def forward_2d(volume, sinogram, plan: plan_2d):
@@ -235,6 +263,7 @@ def forward_2d(volume, sinogram, plan: plan_2d):
     check(plan._L.cg_forward_2d_ex(plan.handle, C.c_void_p(volume.data_ptr()),
                                    C.c_void_p(sinogram.data_ptr()), _bits(sinogram),
                                    _stream(volume)))
+    _after_launch()
 
 
 def backward_2d(volume, sinogram, plan: plan_2d):
@@ -243,6 +272,7 @@ def backward_2d(volume, sinogram, plan: plan_2d):
     check(plan._L.cg_backward_2d_ex(plan.handle, C.c_void_p(volume.data_ptr()),
                                     C.c_void_p(sinogram.data_ptr()), _bits(sinogram),
                                     _stream(volume)))
+    _after_launch()
 
 
 def adjoint_2d(volume, sinogram, plan: plan_2d):

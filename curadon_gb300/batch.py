@@ -12,21 +12,25 @@ default: one array copy per problem, then one launch) or the FP32 register
 march (``forward="registers"``); ``forward="auto"`` times both on the bound
 problems once and keeps the faster (the sinograms' contents are restored
 afterwards).  The backprojection is the staged one; results equal the
-single-problem operators with those algorithms bit for bit.  No
-counterpart in the reference, which runs one problem per call.
+single-problem operators with those algorithms bit for bit; ``adjoint()``
+adds the matched adjoint (the exact transpose of the register forward).
+``BatchProjector`` wraps a batch as a differentiable PyTorch function over
+flat buffers.  No counterpart in the reference, which runs one problem per
+call.
 """
 from __future__ import annotations
 
 import ctypes as C
 from typing import Sequence
 
+import numpy as np
 import torch
 
 from ._lib import check, load
 from .backend import _check_tensor, _stream
 from .geometry import FanGeometry
 
-__all__ = ["Batch2d"]
+__all__ = ["Batch2d", "BatchProjector"]
 
 
 class Batch2d:
@@ -119,3 +123,90 @@ class Batch2d:
     def backward(self):
         """volume_i += A_i^T sinogram_i for every problem."""
         check(self._L.cg_batch2d_backward(self._h, _stream(self._keep[1][0])))
+
+    def adjoint(self):
+        """volume_i += the matched adjoint of sinogram_i for every problem (the
+        exact transpose of the ``forward="registers"`` march; the first call
+        allocates the accumulators, so make it before a graph capture)."""
+        check(self._L.cg_batch2d_adjoint(self._h, _stream(self._keep[1][0])))
+
+
+class _BatchProject(torch.autograd.Function):
+    """s = A x over a whole batch, x and s flat (every problem's volume, then
+    every problem's sinogram, concatenated); the backward is the batched
+    drop-in backprojector or, for a matched projector, the batched adjoint."""
+
+    @staticmethod
+    def forward(ctx, x, proj):
+        proj.X.copy_(x)
+        proj._fwd.forward()
+        ctx.proj = proj
+        return proj.S.clone()
+
+    @staticmethod
+    def backward(ctx, grad):
+        p = ctx.proj
+        p.R.copy_(grad)
+        p.G.zero_()
+        if p.matched:
+            p._bwd.adjoint()
+        else:
+            p._bwd.backward()
+        return p.G.clone(), None
+
+
+class BatchProjector:
+    """The projection operator of a whole batch as a differentiable PyTorch
+    function.  ``BatchProjector(geoms, device)`` binds the problems to flat
+    buffers once; ``proj(x)`` takes every volume concatenated (float32, as
+    ``proj.split_volumes`` splits it) and returns every sinogram
+    concatenated, through ``torch.autograd``: its gradient is the batched
+    backprojection (the reference's gradient of the forward is its
+    backprojector, python/standalone/src/curadon/diffable.py:14-38) or, with
+    ``matched=True``, the batched matched adjoint, the exact transpose of the
+    register forward that ``matched`` selects.  Both directions are a few
+    launches for the whole batch, capturable in a CUDA graph."""
+
+    def __init__(self, geoms: Sequence[FanGeometry], device=None, forward: str = "texture",
+                 matched: bool = False):
+        dev = torch.device("cuda", 0) if device is None else torch.device(device)
+        self.geoms = list(geoms)
+        self.matched = bool(matched)
+        self.vol_shapes = [tuple(int(v) for v in g.vol_shape) for g in self.geoms]
+        self.sino_shapes = [tuple(g.sinogram_shape()) for g in self.geoms]
+        nv = [int(np.prod(s)) for s in self.vol_shapes]
+        ns = [int(np.prod(s)) for s in self.sino_shapes]
+        self.vol_offsets = np.cumsum([0] + nv)
+        self.sino_offsets = np.cumsum([0] + ns)
+        self.X = torch.zeros(int(self.vol_offsets[-1]), device=dev)
+        self.G = torch.zeros_like(self.X)
+        self.S = torch.zeros(int(self.sino_offsets[-1]), device=dev)
+        self.R = torch.zeros_like(self.S)
+        self._fwd = Batch2d(self.geoms, self.split_volumes(self.X), self.split_sinograms(self.S),
+                            forward="registers" if self.matched else forward)
+        self._bwd = Batch2d(self.geoms, self.split_volumes(self.G), self.split_sinograms(self.R))
+        self.device = dev
+
+    def split_volumes(self, flat: torch.Tensor):
+        o = self.vol_offsets
+        return [flat[o[i]:o[i + 1]].view(s) for i, s in enumerate(self.vol_shapes)]
+
+    def split_sinograms(self, flat: torch.Tensor):
+        o = self.sino_offsets
+        return [flat[o[i]:o[i + 1]].view(s) for i, s in enumerate(self.sino_shapes)]
+
+    def __call__(self, x: torch.Tensor) -> torch.Tensor:
+        if x.shape != self.X.shape or x.dtype != torch.float32 or x.device != self.device:
+            raise ValueError(f"x must be a float32 tensor of {tuple(self.X.shape)} elements on "
+                             f"{self.device}")
+        return _BatchProject.apply(x, self)
+
+    def adjoint(self, s: torch.Tensor) -> torch.Tensor:
+        """A^T s (no autograd) with this projector's backward operator."""
+        self.R.copy_(s)
+        self.G.zero_()
+        if self.matched:
+            self._bwd.adjoint()
+        else:
+            self._bwd.backward()
+        return self.G.clone()

@@ -24,13 +24,13 @@ namespace {
 // to (row, col), (row, col + 1), (row + 1, col), (row + 1, col + 1), so a
 // sample is one 16-byte atomic instead of two 8-byte ones.
 template <bool QUAD>
-__global__ void __launch_bounds__(256)
-    k_adj2d(void *__restrict__ accA, void *__restrict__ accB, const float *__restrict__ sino,
-            const float2 *__restrict__ tsrc, const float2 *__restrict__ tu0,
-            const float2 *__restrict__ tdu, int W, int H, int det, int nangles, float sx,
-            float sy, int pa, int pb) {
-    const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    const int view = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void adj2d_ray(void *__restrict__ accA, void *__restrict__ accB,
+                                          const float *__restrict__ sino,
+                                          const float2 *__restrict__ tsrc,
+                                          const float2 *__restrict__ tu0,
+                                          const float2 *__restrict__ tdu, int W, int H, int det,
+                                          int nangles, float sx, float sy, int pa, int pb, int u,
+                                          int view) {
     if (u >= det || view >= nangles) return;
     const float2 s = tsrc[view], o = tu0[view], du = tdu[view];
     const float fu = (float)u;
@@ -91,17 +91,75 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+template <bool QUAD>
+__global__ void __launch_bounds__(256)
+    k_adj2d(void *__restrict__ accA, void *__restrict__ accB, const float *__restrict__ sino,
+            const float2 *__restrict__ tsrc, const float2 *__restrict__ tu0,
+            const float2 *__restrict__ tdu, int W, int H, int det, int nangles, float sx,
+            float sy, int pa, int pb) {
+    adj2d_ray<QUAD>(accA, accB, sino, tsrc, tu0, tdu, W, H, det, nangles, sx, sy, pa, pb,
+                    blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
+}
+
 // vol[y][x] += the four quad entries covering (x, y) in each layout.
-__global__ void k_fold2d_quad(float *__restrict__ vol, const float4 *__restrict__ A,
-                              const float4 *__restrict__ B, int W, int H, int pa, int pb) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void fold2d_quad(float *__restrict__ vol, const float4 *__restrict__ A,
+                                            const float4 *__restrict__ B, int W, int H, int pa,
+                                            int pb, int x, int y) {
     if (x >= W || y >= H) return;
     const float4 *ra = A + (size_t)(y + kPad) * pa + (x + kPad);
     const float4 *rb = B + (size_t)(x + kPad) * pb + (y + kPad);
     const float sa = (ra[0].x + ra[-1].y) + (ra[-pa].z + ra[-pa - 1].w);
     const float sb = (rb[0].x + rb[-1].y) + (rb[-pb].z + rb[-pb - 1].w);
     vol[(size_t)y * W + x] += sa + sb;
+}
+
+__global__ void k_fold2d_quad(float *__restrict__ vol, const float4 *__restrict__ A,
+                              const float4 *__restrict__ B, int W, int H, int pa, int pb) {
+    fold2d_quad(vol, A, B, W, H, pa, pb, blockIdx.x * blockDim.x + threadIdx.x,
+                blockIdx.y * blockDim.y + threadIdx.y);
+}
+
+// The matched adjoint of a batch (quad accumulators), as three launches over
+// the batch's work list: zeroing every problem's accumulators, the scatter
+// (one ray per thread, 32 cells x 8 views per block) and the fold (one voxel
+// per thread, 32 x 8 per block).  Each problem's result equals its
+// single-problem matched adjoint up to the order of the atomic additions.
+__global__ void __launch_bounds__(256)
+    k_batch_adj2d_zero(const Prob2d *__restrict__ probs, const int *__restrict__ start,
+                       int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob2d &q = probs[i];
+    const long long na = (long long)q.pa * (q.H + 2 * kPad);
+    const long long nb = (long long)q.pb * (q.W + 2 * kPad);
+    const long long base = (long long)(blockIdx.x - start[i]) * 1024;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const long long e = base + k * 256 + threadIdx.x;
+        if (e < na) q.quadA[e] = z;
+        else if (e < na + nb) q.quadB[e - na] = z;
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    k_batch_adj2d(const Prob2d *__restrict__ probs, const int *__restrict__ start, int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob2d &q = probs[i];
+    const int local = blockIdx.x - start[i];
+    const int gx = (q.det + 31) / 32;
+    adj2d_ray<true>(q.quadA, q.quadB, q.sino, q.src, q.u0, q.du, q.W, q.H, q.det, q.nangles, q.sx,
+                    q.sy, q.pa, q.pb, (local % gx) * 32 + threadIdx.x,
+                    (local / gx) * 8 + threadIdx.y);
+}
+
+__global__ void __launch_bounds__(256)
+    k_batch_fold2d(const Prob2d *__restrict__ probs, const int *__restrict__ start, int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob2d &q = probs[i];
+    const int local = blockIdx.x - start[i];
+    const int gx = (q.W + 31) / 32;
+    fold2d_quad(q.vol, q.quadA, q.quadB, q.W, q.H, q.pa, q.pb, (local % gx) * 32 + threadIdx.x,
+                (local / gx) * 8 + threadIdx.y);
 }
 
 // vol[y][x] += A[y][x].x + A[y][x-1].y + B[x][y].x + B[x][y-1].y (padded).
@@ -268,19 +326,39 @@ __global__ void k_fold3d_quad(float *__restrict__ vol, const float4 *__restrict_
 
 }  // namespace
 
+size_t adj2d_quad_elems(const Plan2d &p, bool layoutA) {
+    return layoutA ? (size_t)p.pitchA() * (p.H + 2 * kPad) : (size_t)p.pitchB() * (p.W + 2 * kPad);
+}
+
+int ensure_adj2d_quads(Plan2d &p) {
+    if (p.d_quadA) return CG_OK;
+    CG_TRY_CUDA(cudaMalloc(&p.d_quadA, adj2d_quad_elems(p, true) * sizeof(float4)));
+    CG_TRY_CUDA(cudaMalloc(&p.d_quadB, adj2d_quad_elems(p, false) * sizeof(float4)));
+    return CG_OK;
+}
+
+int launch_batch2d_adjoint(const Prob2d *probs, const int *starts,
+                           const int totals[kBatchStages], int count, cudaStream_t s) {
+    const dim3 tile(32, 8);
+    k_batch_adj2d_zero<<<totals[4], 256, 0, s>>>(probs, starts + 4 * (count + 1), count);
+    CG_TRY_CUDA(cudaGetLastError());
+    k_batch_adj2d<<<totals[5], tile, 0, s>>>(probs, starts + 5 * (count + 1), count);
+    CG_TRY_CUDA(cudaGetLastError());
+    k_batch_fold2d<<<totals[6], tile, 0, s>>>(probs, starts + 6 * (count + 1), count);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
 int launch_adjoint2d(Plan2d &p, float *vol, const float *sino, cudaStream_t s) {
-    const size_t na = (size_t)p.pitchA() * (p.H + 2 * kPad);
-    const size_t nb = (size_t)p.pitchB() * (p.W + 2 * kPad);
+    const size_t na = adj2d_quad_elems(p, true);
+    const size_t nb = adj2d_quad_elems(p, false);
     dim3 block(p.fwd_bx, p.fwd_by);
     dim3 grid(ceil_div(p.det, p.fwd_bx), ceil_div(p.nangles, p.fwd_by));
     if (grid.y > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     const dim3 fgrid(ceil_div(p.W, 32), ceil_div(p.H, 8));
     // quad accumulators when both fit in 96 MB, where the L2 holds the atomics
     if (p.adj_quad > 0 || (p.adj_quad < 0 && (na + nb) * sizeof(float4) <= (96u << 20))) {
-        if (!p.d_quadA) {
-            CG_TRY_CUDA(cudaMalloc(&p.d_quadA, na * sizeof(float4)));
-            CG_TRY_CUDA(cudaMalloc(&p.d_quadB, nb * sizeof(float4)));
-        }
+        if (int rc = ensure_adj2d_quads(p)) return rc;
         CG_TRY_CUDA(cudaMemsetAsync(p.d_quadA, 0, na * sizeof(float4), s));
         CG_TRY_CUDA(cudaMemsetAsync(p.d_quadB, 0, nb * sizeof(float4), s));
         k_adj2d<true><<<grid, block, 0, s>>>(p.d_quadA, p.d_quadB, sino, p.d_src, p.d_u0, p.d_du,

@@ -13,7 +13,9 @@
 // problem's volume is copied into its plan's array, then one launch samples
 // all problems through their bindless texture handles) or, selected with
 // cg_batch2d_set_forward, the FP32 register march (algorithm 0); the batched
-// backprojection is the staged one (algorithm 2).  Each problem uses its own
+// backprojection is the staged one (algorithm 2); cg_batch2d_adjoint runs
+// the matched adjoint (the exact transpose of the register march) over the
+// same work list.  Each problem uses its own
 // plan's scratch, so a plan may appear in one batch only once, and a batch
 // must not overlap on the GPU with other calls on its plans.
 #include <memory>
@@ -30,8 +32,9 @@ struct cg_batch2d {
     std::vector<cg::Plan2d *> plans;
     std::vector<cg::Prob2d> probs;  // host copy (the texture forward's copies)
     cg::Prob2d *d_probs = nullptr;
-    int *d_starts = nullptr;  // 4 stages x (count + 1)
-    int totals[4] = {0, 0, 0, 0};
+    int *d_starts = nullptr;  // kBatchStages stages x (count + 1)
+    int totals[cg::kBatchStages] = {};
+    bool adjoint_ready = false;  // the plans' quad accumulators are bound
 };
 
 using namespace cg;
@@ -65,8 +68,8 @@ int cg_batch2d_create(cg_batch2d **batch, cg_plan2d *const *plans, float *const 
     CG_REQUIRE(guard.ok(), "cannot select the plans' device");
 
     std::vector<Prob2d> probs(count);
-    std::vector<int> starts(4 * (count + 1), 0);
-    long long totals[4] = {0, 0, 0, 0};
+    std::vector<int> starts(kBatchStages * (count + 1), 0);
+    long long totals[kBatchStages] = {};
     for (int i = 0; i < count; ++i) {
         const Plan2d &p = *plans[i];
         Prob2d &q = probs[i];
@@ -78,9 +81,10 @@ int cg_batch2d_create(cg_batch2d **batch, cg_plan2d *const *plans, float *const 
         q.sx = p.sx, q.sy = p.sy, q.ox = p.ox, q.oy = p.oy, q.ds = p.ds;
         if (int rc = ensure_vol_texture(*plans[i])) return rc;
         q.tex = p.tex_vol, q.arr = p.arr_vol;
-        int blocks[4];
+        q.quadA = p.d_quadA, q.quadB = p.d_quadB;
+        int blocks[kBatchStages];
         batch_blocks(p, blocks);
-        for (int st = 0; st < 4; ++st) {
+        for (int st = 0; st < kBatchStages; ++st) {
             starts[st * (count + 1) + i] = (int)totals[st];
             totals[st] += blocks[st];
             starts[st * (count + 1) + i + 1] = (int)totals[st];
@@ -94,7 +98,7 @@ int cg_batch2d_create(cg_batch2d **batch, cg_plan2d *const *plans, float *const 
     b->count = count;
     b->plans.assign(plans, plans + count);
     b->probs = probs;
-    for (int st = 0; st < 4; ++st) b->totals[st] = (int)totals[st];
+    for (int st = 0; st < kBatchStages; ++st) b->totals[st] = (int)totals[st];
     auto fail = [&](cudaError_t e) {
         free_batch(b.get());
         return set_error(e == cudaErrorMemoryAllocation ? CG_ERR_NOMEM : CG_ERR_CUDA,
@@ -150,6 +154,26 @@ int cg_batch2d_get_forward(const cg_batch2d *batch, int *algorithm) {
     CG_REQUIRE(batch && algorithm, "NULL argument");
     *algorithm = batch->fwd_algo;
     return CG_OK;
+}
+
+int cg_batch2d_adjoint(cg_batch2d *batch, void *stream) {
+    clear_error();
+    CG_REQUIRE(batch, "batch is NULL");
+    DeviceGuard guard(batch->device);
+    CG_REQUIRE(guard.ok(), "cannot select the batch's device");
+    if (!batch->adjoint_ready) {
+        // first call: every plan's quad accumulators, bound into the work list
+        for (int i = 0; i < batch->count; ++i) {
+            if (int rc = ensure_adj2d_quads(*batch->plans[i])) return rc;
+            batch->probs[i].quadA = batch->plans[i]->d_quadA;
+            batch->probs[i].quadB = batch->plans[i]->d_quadB;
+        }
+        CG_TRY_CUDA(cudaMemcpy(batch->d_probs, batch->probs.data(),
+                               sizeof(Prob2d) * batch->count, cudaMemcpyHostToDevice));
+        batch->adjoint_ready = true;
+    }
+    return launch_batch2d_adjoint(batch->d_probs, batch->d_starts, batch->totals, batch->count,
+                                  (cudaStream_t)stream);
 }
 
 int cg_batch2d_backward(cg_batch2d *batch, void *stream) {

@@ -160,7 +160,22 @@ struct Prob2d {
     float sx, sy, ox, oy, ds;
     cudaTextureObject_t tex;  // the plan's volume texture (texture forward)
     cudaArray_t arr;          // and its array
+    float4 *quadA, *quadB;    // matched adjoint: the plan's quad accumulators
 };
+
+// Problem of a batched launch's block b: the last i with start[i] <= b
+// (stage s of problem i owns the blocks [start[i], start[i + 1])).
+__device__ __forceinline__ int batch_problem(const int *__restrict__ start, int count, int b) {
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+// Batched stages: re-layout, forward, sinogram re-layout, backprojection,
+// and the matched adjoint's zeroing, scatter and fold.
+constexpr int kBatchStages = 7;
 
 struct Plan3d {
     int device = 0;
@@ -262,9 +277,15 @@ int add_into_half(void *vol, const float *add, long long n, cudaStream_t s);
 int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s);
 // batches (proj2d.cu): blocks of each stage of one problem, and the launch of
 // one direction over a batch whose starts hold 4 x (count + 1) block starts
-void batch_blocks(const Plan2d &p, int blocks[4]);
-int launch_batch2d(const Prob2d *probs, const int *starts, const int totals[4], int count,
-                   bool forward, cudaStream_t s);
+void batch_blocks(const Plan2d &p, int blocks[kBatchStages]);
+int launch_batch2d(const Prob2d *probs, const int *starts, const int totals[kBatchStages],
+                   int count, bool forward, cudaStream_t s);
+// the matched adjoint's padded accumulator sizes (float4 elements) and
+// their allocation (on first use)
+size_t adj2d_quad_elems(const Plan2d &p, bool layoutA);
+int ensure_adj2d_quads(Plan2d &p);
+int launch_batch2d_adjoint(const Prob2d *probs, const int *starts,
+                           const int totals[kBatchStages], int count, cudaStream_t s);
 int launch_backward2d(const Plan2d &p, float *vol, cudaStream_t s);
 
 int ensure_plan3d_scratch(Plan3d &p, bool fwd, bool bwd);

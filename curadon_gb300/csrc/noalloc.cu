@@ -93,7 +93,8 @@ extern "C" int cg_backward_2d_static(float *volume, const float *sinogram,
         return set_error(CG_ERR_INVALID,
                          "problem needs " + std::to_string(total) + " bytes of scratch; the "
                          "static scratch holds " + std::to_string(kStaticScratchBytes) +
-                         " (nangles x (det_count + 4) x 8 bytes plus 92 bytes per view)");
+                         " (a call needs at most 8 x nangles x (det_count + 4) + 84 x nangles "
+                         "+ 2040 bytes)");
 
     void *base = nullptr;
     int rc = static_scratch(&base);
@@ -118,6 +119,10 @@ extern "C" int cg_backward_2d_static(float *volume, const float *sinogram,
     p.d_bproj = reinterpret_cast<float4 *>(b + off_proj);
     p.d_sinoP = reinterpret_cast<float2 *>(b + off_sino);
     apply_algo_env(&p, nullptr);
+    // Only the register backprojector (0) and the staged one (2) run on this
+    // scratch alone; the texture-unit and split algorithms would allocate
+    // arrays, so an override selecting them falls back to the staged kernel.
+    if (p.algo_bwd != 0) p.algo_bwd = 2;
 
     cudaStream_t s = (cudaStream_t)stream;
     CG_TRY_CUDA(cudaMemcpyAsync(p.d_angles, angles, 4 * n, cudaMemcpyHostToDevice, s));

@@ -678,7 +678,16 @@ __global__ void __launch_bounds__(T * VS, MB)
                           lay + (size_t)(q + kPad) * pitch + c0, row_bytes, bar);
         }
     };
-    unsigned phases = 0;  // TMA: completed phases of each buffer's barrier, mod 2
+    // TMA bookkeeping, per thread: completed phases of each buffer's barrier
+    // (mod 2), buffers whose copies it has not yet seen complete, and whether
+    // one of its waits gave up.  A give-up stops the block at the next chunk
+    // boundary (every thread learns it from the same barrier), so no further
+    // copy is issued; before exit thread 0 waits, again bounded, for the
+    // copies still outstanding.  The block's outputs are then not to be
+    // trusted and the give-up is counted for cg_wait_timeouts.
+    unsigned phases = 0, pending = 0;
+    int gave_up = 0;
+    auto staged = [&](int ci) { return ci < kCs2MaxChunks && s_win[ci] >= 0; };
     if constexpr (TMA) {
         if (threadIdx.x == 0) {
             mbar_init(bar0, 1);
@@ -686,17 +695,24 @@ __global__ void __launch_bounds__(T * VS, MB)
             mbar_fence_init();
         }
         __syncthreads();
-        if (nch > 0) stage_tma(0, 0);
+        if (nch > 0) {
+            stage_tma(0, 0);
+            if (staged(0)) pending |= 1u;
+        }
     } else {
         if (nch > 0) stage(0, 0);
         asm volatile("cp.async.commit_group;\n" ::);
     }
     for (int ci = 0; ci < nch; ++ci) {
-        if constexpr (!TMA) asm volatile("cp.async.wait_group 0;\n" ::);
-        __syncthreads();
         if constexpr (TMA) {
-            if (ci + 1 < nch) stage_tma(ci + 1, (ci + 1) & 1);
+            if (__syncthreads_or(gave_up)) break;
+            if (ci + 1 < nch) {
+                stage_tma(ci + 1, (ci + 1) & 1);
+                if (staged(ci + 1)) pending |= 1u << ((ci + 1) & 1);
+            }
         } else {
+            asm volatile("cp.async.wait_group 0;\n" ::);
+            __syncthreads();
             if (ci + 1 < nch) stage(ci + 1, (ci + 1) & 1);
             asm volatile("cp.async.commit_group;\n" ::);
         }
@@ -704,10 +720,12 @@ __global__ void __launch_bounds__(T * VS, MB)
         const int win = ci < kCs2MaxChunks ? s_win[ci] : -1;
         if (TMA && win >= 0) {
             const int b = ci & 1;
-            if (!mbar_wait(bar0 + 8u * (unsigned)b, (phases >> b) & 1u, kWaitTries) &&
-                threadIdx.x == 0)
-                atomicAdd(&g_wait_timeouts, 1ull);
-            phases ^= 1u << b;
+            if (mbar_wait(bar0 + 8u * (unsigned)b, (phases >> b) & 1u, kWaitTries)) {
+                phases ^= 1u << b;
+                pending &= ~(1u << b);
+            } else {
+                gave_up = 1;
+            }
         }
         if (win >= 0) {
             const int c0 = (win >> 16) - kPad, wx = win & 0xffff;
@@ -764,6 +782,13 @@ __global__ void __launch_bounds__(T * VS, MB)
         }
     }
     if constexpr (!TMA) asm volatile("cp.async.wait_group 0;\n" ::);
+    if constexpr (TMA) {
+        if (__syncthreads_or(gave_up) && threadIdx.x == 0) {
+            atomicAdd(&g_wait_timeouts, 1ull);
+            for (int b = 0; b < 2; ++b)
+                if ((pending >> b) & 1u) mbar_wait(bar0 + 8u * (unsigned)b, (phases >> b) & 1u, kWaitTries);
+        }
+    }
 
 #pragma unroll
     for (int g = 0; g < GV; ++g) {
@@ -989,9 +1014,19 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
             mbar_fence_init();
         }
     }
+    // BULK: a wait that gives up stops the tile at the next group of views
+    // (every thread learns it from the same barrier), so no further copy is
+    // issued; before exit thread 0 waits, again bounded, for the copies it
+    // has not seen complete.  The tile's results are then not to be trusted
+    // and the give-up is counted for cg_wait_timeouts.
+    int gave_up = 0;
     for (int v0 = 0; v0 < nangles; v0 += kSmViews) {
         const int nv = min(kSmViews, nangles - v0);
-        __syncthreads();
+        if constexpr (BULK) {
+            if (__syncthreads_or(gave_up)) break;
+        } else {
+            __syncthreads();
+        }
         if (tid < nv) {
             const float4 a = proj[v0 + tid], b = proj[nangles + v0 + tid];
             sA[tid] = a, sB[tid] = b;
@@ -1060,9 +1095,8 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                 }
             }
             asm volatile("cp.async.wait_all;\n" ::);
-            if (!mbar_wait(bar, phase, kWaitTries) && tid == 0)
-                atomicAdd(&g_wait_timeouts, 1ull);
-            phase ^= 1u;
+            if (mbar_wait(bar, phase, kWaitTries)) phase ^= 1u;
+            else gave_up = 1;
         }
         for (int e = tid; !BULK && e < nv * kSmWin; e += 256) {
             const int j = e / kSmWin, i = e - j * kSmWin;
@@ -1157,6 +1191,12 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
             }
         }
     }
+    if constexpr (BULK) {
+        if (__syncthreads_or(gave_up) && tid == 0) {
+            atomicAdd(&g_wait_timeouts, 1ull);
+            if (gave_up) mbar_wait(bar, phase, kWaitTries);
+        }
+    }
     if (x < W) {
 #pragma unroll
         for (int r = 0; r < kSmRows; ++r) {
@@ -1187,16 +1227,8 @@ namespace {
 // A batch runs every stage of many 2D problems (any sizes, geometries) as
 // one launch over a work list: stage s of problem i owns the blocks
 // [start[s][i], start[s][i + 1]) of the launch, and each block finds its
-// problem by binary search over those starts, then runs the single-problem
-// tile or ray code on it.
-__device__ __forceinline__ int batch_problem(const int *__restrict__ start, int count, int b) {
-    int lo = 0, hi = count - 1;
-    while (lo < hi) {  // last i with start[i] <= b
-        const int mid = (lo + hi + 1) >> 1;
-        if (start[mid] <= b) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
+// problem by binary search over those starts (batch_problem), then runs the
+// single-problem tile or ray code on it.
 
 __global__ void __launch_bounds__(256)
     k_batch_relayout2d(const Prob2d *__restrict__ probs, const int *__restrict__ start, int count) {
@@ -1245,15 +1277,21 @@ __global__ void __launch_bounds__(256, 4)
 
 // Blocks of each batched stage for one problem (the launch shapes of the
 // single-problem kernels above).
-void batch_blocks(const Plan2d &p, int blocks[4]) {
+void batch_blocks(const Plan2d &p, int blocks[kBatchStages]) {
     blocks[0] = ceil_div(p.W + 2 * kPad, kTile) * ceil_div(p.H + 2 * kPad, kTile);
     blocks[1] = ceil_div(p.det, 32) * ceil_div(p.nangles, 8);
     blocks[2] = (int)ceil_div((long long)p.pitchS() * p.nangles, 256);
     blocks[3] = ceil_div(p.W, 32) * ceil_div(p.H, 8 * kSmRows);
+    // matched adjoint: 1024 float4 zeroed per block, one ray per thread in
+    // 32 x 8 blocks, one voxel per thread in 32 x 8 blocks
+    blocks[4] = (int)ceil_div((long long)(adj2d_quad_elems(p, true) + adj2d_quad_elems(p, false)),
+                              1024);
+    blocks[5] = ceil_div(p.det, 32) * ceil_div(p.nangles, 8);
+    blocks[6] = ceil_div(p.W, 32) * ceil_div(p.H, 8);
 }
 
-int launch_batch2d(const Prob2d *probs, const int *starts, const int totals[4], int count,
-                   bool forward, cudaStream_t s) {
+int launch_batch2d(const Prob2d *probs, const int *starts, const int totals[kBatchStages],
+                   int count, bool forward, cudaStream_t s) {
     const dim3 tile(32, 8);
     if (forward) {
         k_batch_relayout2d<<<totals[0], tile, 0, s>>>(probs, starts, count);

@@ -244,11 +244,14 @@ int cg_backward_3d(float *x, const uint64_t vol_shape[3], const float vol_spacin
  * cg_backward_2d on the same arguments (plan_2d's geometry without
  * det_offset, which the backprojection does not use), accumulating into
  * `volume`; all scratch lives in one 16 MiB device array that the library
- * holds on every GPU that loads it, so problems needing more --
- * nangles * (det_count + 4) * 8 bytes plus 92 bytes per view -- are rejected
- * with CG_ERR_INVALID.  The first call on a device looks the array up (make
- * it before any stream capture).  All calls share the array: calls that
- * overlap on the GPU race and must be ordered by the caller. */
+ * holds on every GPU that loads it.  A call needs at most
+ * 8 * nangles * (det_count + 4) + 84 * nangles + 2040 bytes of it; larger
+ * problems are rejected with CG_ERR_INVALID.  The first call on a device
+ * looks the array's device address up and keeps it for the life of the
+ * device's context (make that first call before any stream capture; after a
+ * cudaDeviceReset the kept address is stale, so do not call this again in
+ * that process).  All calls share the array: calls that overlap on the GPU
+ * race and must be ordered by the caller. */
 int cg_backward_2d_static(float *volume, const float *sinogram, const uint64_t vol_shape[2],
                           const float vol_spacing[2], const float vol_offset[2],
                           uint64_t det_count, float det_spacing, const float *DSO,
@@ -289,6 +292,14 @@ int cg_batch2d_destroy(cg_batch2d *batch);
 int cg_batch2d_forward(cg_batch2d *batch, void *stream);
 /* volume_i += A_i^T sinogram_i for every problem */
 int cg_batch2d_backward(cg_batch2d *batch, void *stream);
+/* volume_i += the matched adjoint (exact transpose of the register ray
+ * march, cg_adjoint_2d's operator) of sinogram_i for every problem, as three
+ * launches over the work list (zeroing, scatter, fold).  Pairs with the
+ * batched forward on algorithm 0 for gradients and solvers that need A^T.
+ * The first call allocates the plans' accumulators (make it before any
+ * stream capture).  No counterpart in the reference, whose gradient is its
+ * backprojector (python/standalone/src/curadon/diffable.py:14-38). */
+int cg_batch2d_adjoint(cg_batch2d *batch, void *stream);
 /* the batched forward's algorithm: 1 texture unit (default), 0 registers */
 int cg_batch2d_set_forward(cg_batch2d *batch, int algorithm);
 int cg_batch2d_get_forward(const cg_batch2d *batch, int *algorithm);

@@ -65,3 +65,19 @@ def ref_ops(cuda_device):
 
 def gpu_threads():
     return max(1, os.cpu_count() or 1)
+
+
+@pytest.fixture(autouse=True)
+def _no_wait_timeouts(request):
+    """After every GPU test: no bounded wait in this library's kernels gave up
+    (a give-up leaves that launch's results untrustworthy)."""
+    yield
+    if request.node.get_closest_marker("gpu") is None:
+        return
+    import torch
+
+    if not torch.cuda.is_available():
+        return
+    from curadon_gb300.backend import wait_timeouts
+
+    assert wait_timeouts() == 0, "a kernel's bounded wait for its bulk copies gave up"

@@ -65,3 +65,33 @@ def test_static_rejects_problems_beyond_its_scratch():
     rc = _call_static(L, 1 << 20, 1 << 20, g, 0)
     assert rc == _lib.CG_ERR_INVALID
     assert b"static scratch" in L.cg_last_error()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("algo", ["bwd2d=split4", "bwd2d=tex", "bwd2d=alu"])
+def test_static_backprojection_under_algorithm_override(cuda_device, monkeypatch, algo):
+    """An override naming a backprojector that would allocate (texture unit,
+    split) must not change the result: the entry point then runs the staged
+    kernel on its own scratch, and its sinogram copy matches the kernel."""
+    import torch
+
+    from curadon_gb300 import FanGeometry, backward_2d
+
+    L = _lib.load()
+    stream = torch.cuda.current_stream(cuda_device).cuda_stream
+    g = fan_config(192, 150)
+    geom = FanGeometry(**g)  # plan made before the override: the default kernels
+    rng = np.random.default_rng(11)
+    sino = torch.as_tensor(rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32),
+                           device=cuda_device)
+    expect = torch.zeros((192, 192), device=cuda_device)
+    backward_2d(expect, sino, geom.plan)
+    monkeypatch.setenv("CURADON_GB300_ALGO", algo)
+    for _ in range(2):
+        got = torch.zeros_like(expect)
+        rc = _call_static(L, got.data_ptr(), sino.data_ptr(), g, stream)
+        assert rc == _lib.CG_OK, L.cg_last_error()
+        torch.cuda.synchronize()
+        e = rel_l2(got.cpu(), expect.cpu())
+        print(f"{algo}: rel-L2 {e:.2e}")
+        assert e <= TOL
