@@ -39,11 +39,9 @@ import numpy as np  # noqa: E402
 # Main kernel of each operator by the plan's algorithm name.
 KERNELS = {
     ("fan", "forward", "texture"): "k_fwd2d_tex", ("fan", "forward", "chunked"): "k_fwd2d_cslab",
-    ("fan", "forward", "registers"): "k_fwd2d", ("fan", "forward", "hybrid"): "k_fwd2d_hyb",
-    ("fan", "forward", "slab"): "k_fwd2d_slab", ("fan", "backward", "shared"): "k_bwd2d_smem",
+    ("fan", "forward", "registers"): "k_fwd2d", ("fan", "backward", "shared"): "k_bwd2d_smem",
     ("fan", "backward", "registers"): "k_bwd2d", ("fan", "backward", "texture"): "k_bwd2d_tex",
-    ("cone", "forward", "texture"): "k_fwd3d_tex3", ("cone", "forward", "layered"): "k_fwd3d_tex2l",
-    ("cone", "forward", "registers"): "k_fwd3d", ("cone", "forward", "slab"): "k_fwd3d_slab",
+    ("cone", "forward", "texture"): "k_fwd3d_tex3", ("cone", "forward", "registers"): "k_fwd3d",
     ("cone", "forward", "quad"): "k_fwd3d_quad", ("cone", "forward", "mixed"): "k_fwd3d_quad",
     ("cone", "backward", "registers"): "k_bwd3d", ("cone", "backward", "axial"): "k_bwd3d_ax",
 }
@@ -63,6 +61,10 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--sweep-sizes", default="64,128,256,512,1024,2048",
                    help="image sizes of --workload sweep")
+    p.add_argument("--serve-requests", type=int, default=400,
+                   help="requests of --workload serve")
+    p.add_argument("--serve-rate", type=float, default=200.0,
+                   help="Poisson arrival rate of --workload serve (per second)")
     p.add_argument("--no-reference-gpu", action="store_true",
                    help="skip the reference's own CUDA operators beside ours (default run)")
     p.add_argument("--batch-forward", default="texture", choices=["texture", "registers"],
@@ -244,16 +246,14 @@ def kernels_per_step(wl, geom) -> int:
     fwd, bwd = geom.plan.algorithm
     nv = len(wl["geom"]["angles"])
     if wl["kind"] == "fan":
-        # forward: texture 1; split: re-layout + texture share + chunked rest;
-        # others: re-layout + kernel
-        f = {"texture": 1, "split": 3}.get(fwd, 2)
-        # backprojection: texture one per 2048 views; split: re-layout +
-        # texture rows + staged rows; others: re-layout + kernel
-        b = {"texture": -(-nv // 2048), "split": 3}.get(bwd, 2)
+        # forward: texture 1 (plus an array copy); others: re-layout + kernel
+        f = 1 if fwd == "texture" else 2
+        # backprojection: texture one per 2048 views; others: re-layout + kernel
+        b = -(-nv // 2048) if bwd == "texture" else 2
         return f + b
-    # forward: texture 1; layered: transpose + kernel; registers, slab, quad,
-    # mixed: two re-layouts + kernel
-    f = {"texture": 1, "layered": 2}.get(fwd, 3)
+    # forward: texture 1; registers: two re-layouts + kernel; quad, mixed: two
+    # re-layouts + kernel (plus the texture array copy)
+    f = 1 if fwd == "texture" else 3
     # backprojection: re-layout + one kernel (axial: one per 768 views)
     b = 1 + (-(-nv // 768) if bwd == "axial" else 1)
     return f + b
@@ -786,12 +786,13 @@ def run_sweep(args):
 
 # ------------------------------------------------------------ serving
 
-def serve_requests(n_req: int, dev, seed: int = 4000):
-    """A seeded request mix in the proportions of the served stream: 70 %
-    2D FBP (n log-uniform over 128..2048, n views), 25 % 2D SIRT-20 (n
-    128..512), 5 % 3D CGLS-30 (n 64..128, 2n views); sizes drawn from a
-    log-spaced set so geometries repeat as in a clinic.  Sinograms are
-    projections of seeded phantoms, in pinned host memory."""
+def serve_requests(n_req: int, dev, seed: int = 4000, kinds=("fbp", "sirt", "cgls")):
+    """A seeded request mix of the served stream: 70 % 2D FBP (n log-uniform
+    over 128..2048, n views), 25 % 2D SIRT-20 (n log-uniform over
+    128..1024), 5 % 3D CGLS-30 (128^3..256^3, 180..360 views, 1.5 n cells);
+    sizes drawn from log-spaced sets so geometries repeat as in a clinic's
+    protocols.  ``kinds`` keeps a sub-mix (the others are redrawn).
+    Sinograms are projections of seeded phantoms, in pinned host memory."""
     import torch
 
     from curadon_gb300 import ConeGeometry, FanGeometry, forward
@@ -800,26 +801,30 @@ def serve_requests(n_req: int, dev, seed: int = 4000):
 
     rng = np.random.default_rng(seed)
     fbp_sizes = [128, 181, 256, 362, 512, 724, 1024, 1448, 2048]
-    sirt_sizes = [128, 181, 256, 362, 512]
-    cone_sizes = [64, 96, 128]
+    sirt_sizes = [128, 181, 256, 362, 512, 724, 1024]
+    cone_sizes = [128, 160, 192, 224, 256]
+    cone_views = [180, 270, 360]
     geoms, reqs = {}, []
-    for _ in range(n_req):
+    while len(reqs) < n_req:
         u = rng.random()
         if u < 0.70:
-            kind, n = "fbp", int(rng.choice(fbp_sizes))
+            kind, n, nv = "fbp", int(rng.choice(fbp_sizes)), 0
         elif u < 0.95:
-            kind, n = "sirt", int(rng.choice(sirt_sizes))
+            kind, n, nv = "sirt", int(rng.choice(sirt_sizes)), 0
         else:
-            kind, n = "cgls", int(rng.choice(cone_sizes))
-        key = (kind == "cgls", n)
+            kind, n, nv = "cgls", int(rng.choice(cone_sizes)), int(rng.choice(cone_views))
+        seed_k = int(rng.integers(1 << 30))
+        if kind not in kinds:
+            continue
+        key = (kind == "cgls", n, nv)
         if key not in geoms:
             if kind == "cgls":
-                geoms[key] = ConeGeometry(**cone_config(n, 2 * n, int(1.5 * n)))
+                geoms[key] = ConeGeometry(**cone_config(n, nv, int(1.5 * n)))
             else:
                 geoms[key] = FanGeometry(**fan_config(n))
         g = geoms[key]
-        ph = (ellipsoids_3d(n, int(rng.integers(1 << 30)), device=dev) if kind == "cgls"
-              else ellipses_2d(n, int(rng.integers(1 << 30)), device=dev)).contiguous()
+        ph = (ellipsoids_3d(n, seed_k, device=dev) if kind == "cgls"
+              else ellipses_2d(n, seed_k, device=dev)).contiguous()
         y = torch.zeros(g.sinogram_shape(), device=dev)
         forward(ph, y, g)
         iters = {"fbp": 0, "sirt": 20, "cgls": 30}[kind]
@@ -828,46 +833,23 @@ def serve_requests(n_req: int, dev, seed: int = 4000):
     return reqs
 
 
-def run_serve(args):
-    """Served solves/s with Poisson arrivals against the plain loop (one
-    problem at a time, each solved and read back before the next)."""
+def _serve_pass(reqs, rate: float, seed: int = 7, batching: bool = True):
+    """Submits ``reqs`` with Poisson arrivals at ``rate`` per second to a new
+    server (after a warm-up pass of residency) and returns its stats."""
     import threading
 
-    import torch
-
-    from curadon_gb300 import _build
-    from curadon_gb300.fbp import fbp
     from curadon_gb300.serve import Server
-    from curadon_gb300.solvers import cgls, sirt
 
-    _build.build()
-    dev = torch.device("cuda", 0)
-    n_req = max(20, args.steps * 8)
-    reqs = serve_requests(n_req, dev)
-
-    def plain(r):
-        y = r.sinogram.to(dev)
-        x = (fbp(y, r.geom) if r.kind == "fbp" else
-             sirt(r.geom, y, r.iters) if r.kind == "sirt" else cgls(r.geom, y, r.iters))
-        return x.cpu()
-
-    for r in reqs[:min(len(reqs), 30)]:  # warm-up: plans and filters of the plain path
-        plain(r)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for r in reqs:
-        plain(r)
-    t_plain = time.perf_counter() - t0
-
-    srv = Server(device=0, slots=8)
-    for f in [srv.submit(r) for r in reqs[:min(len(reqs), 30)]]:  # warm-up: slot residency
+    srv = Server(device=0, slots=8, batching=batching)
+    for f in [srv.submit(r) for r in reqs]:  # warm-up: slot and class-batch residency
         f.result()
     srv.latencies.clear()
     srv.completed, srv.t_first, srv.t_last = 0, None, None
-    rate = 200.0
-    rng = np.random.default_rng(7)
+    rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
     futs = []
+    sampler = ClockSampler(0)
+    sampler.start()
 
     def client():
         t_start = time.perf_counter()
@@ -882,22 +864,86 @@ def run_serve(args):
     th.join()
     for f in futs:
         f.result()
+    batches = srv.batches_run
     srv.close()
     st = srv.stats()
-    plain_rate = len(reqs) / t_plain
+    st["clocks"] = sampler.stop()
+    st["batches"] = batches
+    st["arrival_span_s"] = float(arrivals[-1])
+    return st
+
+
+def run_serve(args):
+    """The served reconstruction stream: requests of the served mix at their
+    specified sizes with Poisson arrivals at 200/s, solves/s and p50 / p99
+    latency, against the plain loop (one request at a time, each solved and
+    read back before the next); again at an arrival rate below capacity
+    (latency without a growing queue); and the 2D part of the mix alone,
+    where coalescing applies."""
+    import torch
+
+    from curadon_gb300 import _build
+    from curadon_gb300.fbp import fbp
+    from curadon_gb300.solvers import cgls, sirt
+
+    _build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+
+    def plain_rate(reqs):
+        def plain(r):
+            y = r.sinogram.to(dev)
+            x = (fbp(y, r.geom) if r.kind == "fbp" else
+                 sirt(r.geom, y, r.iters) if r.kind == "sirt" else cgls(r.geom, y, r.iters))
+            return x.cpu()
+
+        for r in reqs:  # warm-up: plans and filters of the plain path
+            plain(r)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for r in reqs:
+            plain(r)
+        return len(reqs) / (time.perf_counter() - t0)
+
+    n_req = args.serve_requests
+    reqs = serve_requests(n_req, dev)
     kinds = {k: sum(r.kind == k for r in reqs) for k in ("fbp", "sirt", "cgls")}
+    plain_all = plain_rate(reqs)
+    served = _serve_pass(reqs, args.serve_rate)
+    sub_rate = max(1.0, 0.7 * served["solves_per_s"])
+    relaxed = _serve_pass(reqs, sub_rate, seed=8)
+    # the 2D part alone (FBP and SIRT, coalesced into class batches), at an
+    # arrival rate above its capacity so that solves/s measures the server
+    reqs2d = serve_requests(n_req, dev, seed=4001, kinds=("fbp", "sirt"))
+    plain_2d = plain_rate(reqs2d)
+    rate_2d = 10 * args.serve_rate
+    served_2d = _serve_pass(reqs2d, rate_2d)
+    unbatched_2d = _serve_pass(reqs2d, rate_2d, batching=False)
     return {
-        "metric": "served solves/s", "value": st["solves_per_s"], "unit": "solves/s",
-        "n_gpus": 1, "steps": len(reqs), "warmup": 30, "ms_per_step": 1e3 / st["solves_per_s"],
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "metric": "served solves/s", "value": served["solves_per_s"], "unit": "solves/s",
+        "n_gpus": 1, "steps": len(reqs), "warmup": len(reqs),
+        "ms_per_step": 1e3 / served["solves_per_s"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded phantoms, projected by the forward operator)",
         "config": {"workload": f"served stream of {len(reqs)} requests, Poisson arrivals at "
-                               f"{rate:.0f}/s: {kinds['fbp']} 2D FBP (n 128..2048), "
-                               f"{kinds['sirt']} 2D SIRT-20 (n 128..512), {kinds['cgls']} 3D "
-                               "CGLS-30 (n 64..128, 2n views), 8 slots",
+                               f"{args.serve_rate:.0f}/s: {kinds['fbp']} 2D FBP (n 128..2048), "
+                               f"{kinds['sirt']} 2D SIRT-20 (n 128..1024), {kinds['cgls']} 3D "
+                               "CGLS-30 (128^3..256^3, 180..360 views), 8 slots, 2D requests "
+                               "below 704^2 pixels coalesced into class batches of up to 16",
                    "parallelism": "one GPU, concurrent streams"},
-        "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
-        "plain_loop_solves_per_s": plain_rate, "speedup_vs_plain_loop": st["solves_per_s"] / plain_rate,
+        "p50_ms": served["p50_ms"], "p99_ms": served["p99_ms"], "clocks": served["clocks"],
+        "batches": served["batches"],
+        "plain_loop_solves_per_s": plain_all,
+        "speedup_vs_plain_loop": served["solves_per_s"] / plain_all,
+        "below_capacity": {"rate_per_s": sub_rate, "solves_per_s": relaxed["solves_per_s"],
+                           "p50_ms": relaxed["p50_ms"], "p99_ms": relaxed["p99_ms"]},
+        "mix_2d_only": {"requests": len(reqs2d), "rate_per_s": rate_2d,
+                        "solves_per_s": served_2d["solves_per_s"],
+                        "p50_ms": served_2d["p50_ms"], "p99_ms": served_2d["p99_ms"],
+                        "batches": served_2d["batches"],
+                        "plain_loop_solves_per_s": plain_2d,
+                        "speedup_vs_plain_loop": served_2d["solves_per_s"] / plain_2d,
+                        "without_coalescing_solves_per_s": unbatched_2d["solves_per_s"]},
     }
 
 
@@ -933,106 +979,98 @@ def batch_problems(dev, count: int = 64):
 
 
 def run_batch(args):
-    """Gradient descent x <- x - a A^T (A x - y) on the batched workload: one
-    iteration over all problems is a batched forward (one array copy per
-    problem and one texture launch) and a batched backprojection (two
-    launches) with two elementwise ops on flat buffers, captured once in a
-    CUDA graph and replayed; against the plain loop (the single-problem
-    operators, problem by problem).  The value counts operator calls (two
-    per problem and iteration) per second."""
+    """The batched, differentiable workload: 10 unrolled gradient-descent steps
+    x <- x - a grad 1/2 ||A x - y||^2 over all 64 problems, each step through
+    torch.autograd on the batched projector (one forward and one gradient for
+    the whole batch, a few launches each), one step captured in a CUDA graph
+    and replayed.  ``value`` counts operator calls (two per problem and step)
+    per second.  Beside it: the same steps as a plain loop of single-problem
+    calls through the same autograd functions (one problem per launch), and
+    the reference's own CUDA operators in the same plain loop (its geometry
+    holds no per-view jitter, so it runs the unjittered circular problems of
+    the same sizes: the same work).  ``matched`` repeats the batched steps
+    with the exact gradient (register forward, batched matched adjoint)."""
     import torch
 
-    from curadon_gb300 import _build, backward, forward
-    from curadon_gb300.batch import Batch2d
+    from curadon_gb300 import TorchForward, _build
+    from curadon_gb300.batch import BatchProjector
 
     _build.build()
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     probs = batch_problems(dev)
     count = len(probs)
-    nv = [n * n for _, n, _ in probs]
-    ns = [int(np.prod(y.shape)) for _, _, y in probs]
-    X, G = torch.zeros(sum(nv), device=dev), torch.zeros(sum(nv), device=dev)
-    S, R = torch.zeros(sum(ns), device=dev), torch.zeros(sum(ns), device=dev)
-    Y = torch.cat([y.reshape(-1) for _, _, y in probs])
-    A = torch.empty(sum(nv), device=dev)
-
-    def views(flat, sizes, shapes):
-        offs = np.cumsum([0] + sizes)
-        return [flat[offs[i]:offs[i + 1]].view(shapes[i]) for i in range(len(sizes))]
-
-    vshapes = [(n, n) for _, n, _ in probs]
-    sshapes = [tuple(y.shape) for _, _, y in probs]
-    xs, gs = views(X, nv, vshapes), views(G, nv, vshapes)
-    ss, rs = views(S, ns, sshapes), views(R, ns, sshapes)
     geoms = [g for g, _, _ in probs]
-    bf = Batch2d(geoms, xs, ss, forward=args.batch_forward)  # s_i = A_i x_i
-    bb = Batch2d(geoms, gs, rs)  # g_i += A_i^T r_i
-    # step sizes 1 / ||A_i^T A_i|| by power iteration (set-up, untimed)
-    X.uniform_(0.0, 1.0)
-    for _ in range(8):
-        bf.forward()
-        R.copy_(S)
-        G.zero_()
-        bb.backward()
-        for x, g in zip(xs, gs):
-            x.copy_(g / g.norm().clamp_min(1e-20))
-    bf.forward()
-    for a, s_ in zip(views(A, nv, vshapes), ss):
-        a.fill_(1.0 / float(s_.norm() ** 2))
-    X.zero_()
-
-    def iteration():
-        bf.forward()
-        torch.sub(S, Y, out=R)
-        G.zero_()
-        bb.backward()
-        X.addcmul_(A, G, value=-1.0)
-
-    for _ in range(max(3, args.warmup)):
-        iteration()
-    torch.cuda.synchronize()
-    graph = torch.cuda.CUDAGraph()
-    cap = torch.cuda.Stream()
-    cap.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(cap), torch.cuda.graph(graph, stream=cap):
-        iteration()
-    torch.cuda.current_stream().wait_stream(cap)
-    X.zero_()
     iters = 10
     steps = max(1, args.steps // 10)  # a step = the 10 unrolled iterations
-    for _ in range(max(3, args.warmup)):
-        graph.replay()
-    torch.cuda.synchronize()
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(steps)]
-    for k in range(steps):
-        X.zero_()
-        ev[k][0].record()
-        for _ in range(iters):
-            graph.replay()
-        ev[k][1].record()
-    torch.cuda.synchronize()
-    batch_ms = sum(a.elapsed_time(b) for a, b in ev)
-    # the cost the iterations drive down (a check that the solver works)
-    bf.forward()
-    residual = float(torch.linalg.vector_norm(S - Y) / torch.linalg.vector_norm(Y))
 
-    # plain loop: the single-problem operators problem by problem
-    yv = views(Y, ns, sshapes)
-    av = views(A, nv, vshapes)
+    def batched(matched: bool):
+        proj = BatchProjector(geoms, dev, forward=args.batch_forward, matched=matched)
+        Y = torch.cat([y.reshape(-1) for _, _, y in probs])
+        # step sizes 1 / ||A_i^T A_i|| by power iteration (set-up, untimed)
+        v = torch.rand_like(proj.X)
+        for _ in range(8):
+            with torch.no_grad():
+                w = proj.adjoint(proj(v))
+            v = torch.cat([(t / t.norm().clamp_min(1e-20)).reshape(-1)
+                           for t in proj.split_volumes(w)])
+        with torch.no_grad():
+            av = proj(v)
+        A = torch.cat([torch.full((int(np.prod(sh)),), 1.0 / float(a_.norm() ** 2), device=dev)
+                       for sh, a_ in zip(proj.vol_shapes, proj.split_sinograms(av))])
+        x = torch.zeros_like(proj.X)
+
+        def iteration():
+            xr = x.detach().requires_grad_(True)
+            r = proj(xr) - Y
+            (g,) = torch.autograd.grad(0.5 * (r * r).sum(), xr)
+            x.sub_(A * g)
+
+        for _ in range(max(3, args.warmup)):
+            iteration()
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        cap = torch.cuda.Stream()
+        cap.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(cap), torch.cuda.graph(graph, stream=cap):
+            iteration()
+        torch.cuda.current_stream().wait_stream(cap)
+        for _ in range(max(3, args.warmup)):
+            graph.replay()
+        torch.cuda.synchronize()
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(steps)]
+        for k in range(steps):
+            x.zero_()
+            ev[k][0].record()
+            for _ in range(iters):
+                graph.replay()
+            ev[k][1].record()
+        torch.cuda.synchronize()
+        ms = sum(a_.elapsed_time(b_) for a_, b_ in ev) / steps
+        with torch.no_grad():
+            res = float(torch.linalg.vector_norm(proj(x) - Y) / torch.linalg.vector_norm(Y))
+        return ms, res, proj, A
+
+    batch_ms, residual, proj, A = batched(False)
+    matched_ms, matched_res, _, _ = batched(True)
+
+    # plain loop: the same autograd steps problem by problem (single-problem calls)
+    ys = [y for _, _, y in probs]
+    av = proj.split_volumes(A)
+    xs = [torch.zeros(tuple(int(v) for v in g.vol_shape), device=dev) for g in geoms]
 
     def plain_iteration():
         for i, g in enumerate(geoms):
-            forward(xs[i], ss[i], g)
-            torch.sub(ss[i], yv[i], out=rs[i])
-            gs[i].zero_()
-            backward(rs[i], gs[i], g)
-            xs[i].addcmul_(av[i], gs[i], value=-1.0)
+            xr = xs[i].detach().requires_grad_(True)
+            r = TorchForward.apply(xr, g) - ys[i]
+            (gr,) = torch.autograd.grad(0.5 * (r * r).sum(), xr)
+            xs[i].sub_(av[i] * gr)
 
     for _ in range(3):
         plain_iteration()
     torch.cuda.synchronize()
-    X.zero_()
+    for t in xs:
+        t.zero_()
     a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a_ev.record()
     for _ in range(iters):
@@ -1041,25 +1079,70 @@ def run_batch(args):
     torch.cuda.synchronize()
     plain_ms = a_ev.elapsed_time(b_ev)
 
-    ops = 2 * count * iters * steps
+    # the reference's operators in the same plain loop (circular problems of the same sizes)
+    ref, why = reference_ops()
+    ref_ms = None
+    if ref is not None:
+        from curadon_gb300.phantom import fan_config
+
+        handles, rx, rs, rg = [], [], [], []
+        for g, n, y in probs:
+            h, _ = ref.plan2d(fan_config(n, int(y.shape[0])))
+            handles.append(h)
+            rx.append(torch.zeros((n, n), device=dev))
+            rs.append(torch.zeros_like(y))
+            rg.append(torch.zeros((n, n), device=dev))
+
+        def ref_iteration():
+            for i in range(count):
+                ref.forward2d(handles[i], rx[i].data_ptr(), rs[i].data_ptr())
+                torch.sub(rs[i], ys[i], out=rs[i])
+                rg[i].zero_()
+                ref.backward2d(handles[i], rg[i].data_ptr(), rs[i].data_ptr())
+                rx[i].sub_(av[i] * rg[i])
+
+        ref_iteration()
+        torch.cuda.synchronize()
+        a_ev.record()
+        for _ in range(iters):
+            ref_iteration()
+        b_ev.record()
+        torch.cuda.synchronize()
+        ref_ms = a_ev.elapsed_time(b_ev)
+        for h in handles:
+            ref.destroy2d(h)
+
+    ops = 2 * count * iters
     value = ops / (batch_ms / 1e3)
-    plain_value = 2 * count * iters / (plain_ms / 1e3)
+    plain_value = ops / (plain_ms / 1e3)
     kinds = sorted({n for _, n, _ in probs})
-    return {
+    line = {
         "metric": "fwd/bwd proj ops/s", "value": value, "unit": "ops/s", "n_gpus": 1,
         "steps": steps, "warmup": max(3, args.warmup),
-        "ms_per_step": batch_ms / steps, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": batch_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded ellipse phantoms, jittered vector geometries, Poisson noise)",
-        "config": {"workload": f"batched gradient descent: {count} 2D fan-beam problems, n in "
-                               f"{kinds}, 180..720 views, per-view jitter sigma 0.5 px in "
-                               "vector form, y = Ax + Poisson noise (I0 1e4); a step = 10 "
-                               "iterations x - a A^T(Ax - y) over all problems",
+        "config": {"workload": f"batched differentiable gradient descent: {count} 2D fan-beam "
+                               f"problems, n in {kinds}, 180..720 views, per-view jitter sigma "
+                               "0.5 px in vector form, y = Ax + Poisson noise (I0 1e4); a step = "
+                               "10 unrolled iterations x - a grad 1/2||Ax - y||^2 through "
+                               "torch.autograd over all problems, one iteration graph-captured",
                    "l2": "the working set (0.3-1 GB) exceeds L2", "parallelism": "one GPU"},
-        "gpu_launches": (2 + (1 if bf.forward_algorithm == "texture" else 2)) * iters * steps,
-        "plain_loop_ops_per_s": plain_value, "speedup_vs_plain_loop": value / plain_value,
+        "gpu_launches": (2 + (1 if proj._fwd.forward_algorithm == "texture" else 2)) * iters * steps,
+        "gradient": "drop-in (the backprojector, as the reference's autograd function)",
         "relative_residual_after_10": residual,
+        "plain_loop_ops_per_s": plain_value, "speedup_vs_plain_loop": value / plain_value,
+        "matched": {"ops_per_s": ops / (matched_ms / 1e3), "ms_per_step": matched_ms,
+                    "speedup_vs_plain_loop": (ops / (matched_ms / 1e3)) / plain_value,
+                    "relative_residual_after_10": matched_res,
+                    "gradient": "exact (register forward, batched matched adjoint)"},
     }
+    if ref_ms is not None:
+        line["reference_plain_loop_ops_per_s"] = ops / (ref_ms / 1e3)
+        line["speedup_vs_reference_plain_loop"] = value / (ops / (ref_ms / 1e3))
+    else:
+        line["reference_plain_loop"] = {"unavailable": why}
+    return line
 
 
 def main():

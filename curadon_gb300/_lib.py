@@ -66,6 +66,7 @@ SIGNATURES = [
     ("cg_batch2d_forward", C.c_int, [C.c_void_p, C.c_void_p]),
     ("cg_batch2d_backward", C.c_int, [C.c_void_p, C.c_void_p]),
     ("cg_batch2d_adjoint", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("cg_batch2d_set_active", C.c_int, [C.c_void_p, C.c_int]),
     ("cg_batch2d_set_forward", C.c_int, [C.c_void_p, C.c_int]),
     ("cg_batch2d_get_forward", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
 ]

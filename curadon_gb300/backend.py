@@ -2,7 +2,7 @@
 
 Same names, argument order and meaning as the reference's bindings
 (python/standalone/src/bind.cpp:58-66, plan.cu:34-58, forward.cu:138-143,
-backward.cu:279-284).  Tensors are torch CUDA tensors, C-contiguous; 2D
+backward.cu:135-140).  Tensors are torch CUDA tensors, C-contiguous; 2D
 volumes and sinograms are float32 or float16 (the volume's as the plan's
 vol_prec), 3D ones float32.  Work is enqueued on torch's current stream of
 the tensors' device.
@@ -44,18 +44,23 @@ def _stream(t: torch.Tensor) -> C.c_void_p:
     return C.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
 
 
-FORWARD_2D = ("registers", "texture", "hybrid", "slab", "chunked", "split")
-BACKWARD_2D = ("registers", "texture", "shared", "split")
-FORWARD_3D = ("registers", "texture", "layered", "slab", "quad", "mixed")
-BACKWARD_3D = ("registers", "axial")
+# algorithm names and the C ABI's codes (cg_plan2d/3d_set_algorithm)
+FORWARD_2D = {"registers": 0, "texture": 1, "chunked": 4}
+BACKWARD_2D = {"registers": 0, "texture": 1, "shared": 2}
+FORWARD_3D = {"registers": 0, "texture": 1, "quad": 4, "mixed": 5}
+BACKWARD_3D = {"registers": 0, "axial": 1}
 
 
 def _algo_index(name, names, what):
     if name is None:
         return -1
     if name not in names:
-        raise ValueError(f"{what} algorithm must be one of {names}, got {name!r}")
-    return names.index(name)
+        raise ValueError(f"{what} algorithm must be one of {tuple(names)}, got {name!r}")
+    return names[name]
+
+
+def _algo_name(code, names):
+    return next(k for k, v in names.items() if v == code)
 
 
 def _check_tensor(t, name: str, ndim: int | None = None, half: bool = False):
@@ -146,7 +151,7 @@ class plan_2d:
         """(forward, backward) algorithm names of this plan."""
         f, b = C.c_int(), C.c_int()
         check(self._L.cg_plan2d_get_algorithm(self._h, C.byref(f), C.byref(b)))
-        return FORWARD_2D[f.value], BACKWARD_2D[b.value]
+        return _algo_name(f.value, FORWARD_2D), _algo_name(b.value, BACKWARD_2D)
 
     def set_algorithm(self, forward=None, backward=None):
         """Selects the algorithms (names from FORWARD_2D / BACKWARD_2D)."""
@@ -323,7 +328,7 @@ class plan_3d:
     def algorithm(self):
         f, b = C.c_int(), C.c_int()
         check(self._L.cg_plan3d_get_algorithm(self._h, C.byref(f), C.byref(b)))
-        return FORWARD_3D[f.value], BACKWARD_3D[b.value]
+        return _algo_name(f.value, FORWARD_3D), _algo_name(b.value, BACKWARD_3D)
 
     def set_algorithm(self, forward=None, backward=None):
         check(self._L.cg_plan3d_set_algorithm(
@@ -395,6 +400,7 @@ def forward_3d(x, vol_shape, vol_spacing, vol_offset, sinogram, psi, theta, phi,
 
 def backward_3d(x, vol_shape, vol_spacing, vol_offset, sinogram, phi, theta, psi, sino_shape,
                 det_spacing, det_offset, det_rotation, DSO, DSD, COR):
-    """Per-call 3D backprojection (backward.cu:282-284), accumulating into x."""
+    """Per-call 3D backprojection (backward.cu:20-72, bound at :135-140),
+    accumulating into x."""
     _call_3d("cg_backward_3d", x, vol_shape, vol_spacing, vol_offset, sinogram, phi, theta, psi,
              sino_shape, det_spacing, det_offset, det_rotation, DSO, DSD, COR)

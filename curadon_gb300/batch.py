@@ -124,6 +124,11 @@ class Batch2d:
         """volume_i += A_i^T sinogram_i for every problem."""
         check(self._L.cg_batch2d_backward(self._h, _stream(self._keep[1][0])))
 
+    def set_active(self, active: int):
+        """Later calls run problems [0, active) only (a resident batch serving
+        however many requests are waiting)."""
+        check(self._L.cg_batch2d_set_active(self._h, int(active)))
+
     def adjoint(self):
         """volume_i += the matched adjoint of sinogram_i for every problem (the
         exact transpose of the ``forward="registers"`` march; the first call

@@ -188,7 +188,11 @@ __global__ void k_fold2d(float *__restrict__ vol, const float2 *__restrict__ A,
 // and, when the next sample's lower slice is the same element (the ray
 // advanced one slice within the same row and column), added to it, so the
 // two go out as one atomic.
-template <bool QUAD, bool BAND = false, bool MERGE = false>
+// AGG (quads, with MERGE): warp-aggregated atomics -- the lanes of a warp
+// whose lower-slice element coincides at a step (found with
+// __match_any_sync) pass their contributions through shared memory to the
+// lowest such lane, which sums them in lane order and issues one atomic.
+template <bool QUAD, bool BAND = false, bool MERGE = false, bool AGG = false>
 __global__ void __launch_bounds__(256)
     k_adj3d(void *__restrict__ A, void *__restrict__ B, const float *__restrict__ sino,
             const float4 *__restrict__ torg, const float4 *__restrict__ tdu,
@@ -272,7 +276,31 @@ __global__ void __launch_bounds__(256)
             } else if (held_at != ~(size_t)0) {
                 atomicAdd(q + held_at, held);
             }
-            atomicAdd(q + i00, lower);
+            if constexpr (AGG) {
+                __shared__ float4 s_agg[8][32];
+                const unsigned active = __activemask();
+                const int lane = (int)(threadIdx.x + threadIdx.y * blockDim.x) & 31;
+                const int wslot = (int)(threadIdx.x + threadIdx.y * blockDim.x) >> 5;
+                const unsigned peers = __match_any_sync(active, (unsigned)i00);
+                const int leader = __ffs(peers) - 1;
+                // lanes that share their element with another lane; only
+                // they take part in the exchange and its two warp barriers
+                const unsigned shared = __ballot_sync(active, peers != (1u << lane));
+                if (peers != (1u << lane)) {
+                    if (lane != leader) s_agg[wslot][lane] = lower;
+                    __syncwarp(shared);
+                    if (lane == leader) {
+                        for (unsigned rest = peers & ~(1u << lane); rest; rest &= rest - 1) {
+                            const float4 o = s_agg[wslot][__ffs(rest) - 1];
+                            lower.x += o.x, lower.y += o.y, lower.z += o.z, lower.w += o.w;
+                        }
+                    }
+                    __syncwarp(shared);
+                }
+                if (lane == leader) atomicAdd(q + i00, lower);
+            } else {
+                atomicAdd(q + i00, lower);
+            }
             held = upper, held_at = i00 + (size_t)pa * pb;
         } else if constexpr (QUAD) {
             float4 *q = static_cast<float4 *>(L) + i00;
@@ -404,8 +432,10 @@ int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s) {
         }
         CG_TRY_CUDA(cudaMemsetAsync(p.d_quadA, 0, elems * sizeof(float4), s));
         CG_TRY_CUDA(cudaMemsetAsync(p.d_quadB, 0, elems * sizeof(float4), s));
-        auto kq = p.adj_merge ? (band ? k_adj3d<true, true, true> : k_adj3d<true, false, true>)
-                              : (band ? k_adj3d<true, true> : k_adj3d<true, false>);
+        auto kq = p.adj_agg   ? (band ? k_adj3d<true, true, true, true>
+                                      : k_adj3d<true, false, true, true>)
+                  : p.adj_merge ? (band ? k_adj3d<true, true, true> : k_adj3d<true, false, true>)
+                                : (band ? k_adj3d<true, true> : k_adj3d<true, false>);
         kq<<<grid, dim3(32, 8), 0, s>>>(p.d_quadA, p.d_quadB, sino, p.d_forg, p.d_fdu, p.d_fdv,
                                         p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V, p.nangles, utiles,
                                         p.exact_t);

@@ -34,7 +34,14 @@ struct cg_batch2d {
     cg::Prob2d *d_probs = nullptr;
     int *d_starts = nullptr;  // kBatchStages stages x (count + 1)
     int totals[cg::kBatchStages] = {};
+    std::vector<int> starts;  // host copy of d_starts
+    int active = 0;           // problems [0, active) run (cg_batch2d_set_active)
     bool adjoint_ready = false;  // the plans' quad accumulators are bound
+
+    // blocks of each stage for the active problems
+    void active_totals(int out[cg::kBatchStages]) const {
+        for (int st = 0; st < cg::kBatchStages; ++st) out[st] = starts[st * (count + 1) + active];
+    }
 };
 
 using namespace cg;
@@ -96,6 +103,8 @@ int cg_batch2d_create(cg_batch2d **batch, cg_plan2d *const *plans, float *const 
     std::unique_ptr<cg_batch2d> b(new cg_batch2d());
     b->device = plans[0]->device;
     b->count = count;
+    b->active = count;
+    b->starts = starts;
     b->plans.assign(plans, plans + count);
     b->probs = probs;
     for (int st = 0; st < kBatchStages; ++st) b->totals[st] = (int)totals[st];
@@ -133,12 +142,22 @@ int cg_batch2d_forward(cg_batch2d *batch, void *stream) {
     CG_REQUIRE(batch, "batch is NULL");
     DeviceGuard guard(batch->device);
     CG_REQUIRE(guard.ok(), "cannot select the batch's device");
+    int totals[kBatchStages];
+    batch->active_totals(totals);
     if (batch->fwd_algo == 1)
-        return launch_batch2d_fwd_tex(batch->d_probs, batch->probs,
-                                      batch->d_starts + (batch->count + 1), batch->totals[1],
+        return launch_batch2d_fwd_tex(batch->d_probs, batch->probs, batch->active,
+                                      batch->d_starts + (batch->count + 1), totals[1],
                                       (cudaStream_t)stream);
-    return launch_batch2d(batch->d_probs, batch->d_starts, batch->totals, batch->count, true,
+    return launch_batch2d(batch->d_probs, batch->d_starts, totals, batch->count, true,
                           (cudaStream_t)stream);
+}
+
+int cg_batch2d_set_active(cg_batch2d *batch, int active) {
+    clear_error();
+    CG_REQUIRE(batch, "batch is NULL");
+    CG_REQUIRE(active > 0 && active <= batch->count, "active count must be in [1, count]");
+    batch->active = active;
+    return CG_OK;
 }
 
 int cg_batch2d_set_forward(cg_batch2d *batch, int algorithm) {
@@ -172,7 +191,9 @@ int cg_batch2d_adjoint(cg_batch2d *batch, void *stream) {
                                sizeof(Prob2d) * batch->count, cudaMemcpyHostToDevice));
         batch->adjoint_ready = true;
     }
-    return launch_batch2d_adjoint(batch->d_probs, batch->d_starts, batch->totals, batch->count,
+    int totals[kBatchStages];
+    batch->active_totals(totals);
+    return launch_batch2d_adjoint(batch->d_probs, batch->d_starts, totals, batch->count,
                                   (cudaStream_t)stream);
 }
 
@@ -181,7 +202,9 @@ int cg_batch2d_backward(cg_batch2d *batch, void *stream) {
     CG_REQUIRE(batch, "batch is NULL");
     DeviceGuard guard(batch->device);
     CG_REQUIRE(guard.ok(), "cannot select the batch's device");
-    return launch_batch2d(batch->d_probs, batch->d_starts, batch->totals, batch->count, false,
+    int totals[kBatchStages];
+    batch->active_totals(totals);
+    return launch_batch2d(batch->d_probs, batch->d_starts, totals, batch->count, false,
                           (cudaStream_t)stream);
 }
 

@@ -36,9 +36,6 @@ void free_plan2d(Plan2d *p) {
     if (p->tex_sino) cudaDestroyTextureObject(p->tex_sino);
     if (p->arr_vol) cudaFreeArray(p->arr_vol);
     if (p->arr_sino) cudaFreeArray(p->arr_sino);
-    if (p->aux) cudaStreamDestroy(p->aux);
-    if (p->ev_fork) cudaEventDestroy(p->ev_fork);
-    if (p->ev_join) cudaEventDestroy(p->ev_join);
     void *ptrs[] = {p->d_angles, p->d_DSO,   p->d_DSD,   p->d_src,   p->d_u0,    p->d_du,
                     p->d_bmeta,  p->d_bproj, p->d_layA,  p->d_layB,  p->d_sinoP, p->d_vol32,
                     p->d_sino32, p->d_quadA, p->d_quadB};
@@ -48,11 +45,8 @@ void free_plan2d(Plan2d *p) {
 
 void free_plan3d(Plan3d *p) {
     if (!p) return;
-    for (cudaTextureObject_t t : {p->tex3, p->texA, p->texB})
-        if (t) cudaDestroyTextureObject(t);
-    for (cudaArray_t a : {p->arr3, p->arrA, p->arrB})
-        if (a) cudaFreeArray(a);
-    if (p->d_volT) cudaFree(p->d_volT);
+    if (p->tex3) cudaDestroyTextureObject(p->tex3);
+    if (p->arr3) cudaFreeArray(p->arr3);
     void *ptrs[] = {p->d_forg, p->d_fdu, p->d_fdv, p->d_fsrc, p->d_borg, p->d_bdx,
                     p->d_bdy,  p->d_bdz, p->d_volA, p->d_volB, p->d_sinoP, p->d_quadA,
                     p->d_quadB, p->d_sinoQ, p->d_volQA, p->d_volQB};
@@ -61,11 +55,10 @@ void free_plan3d(Plan3d *p) {
 }
 
 // Compiled kernel shapes of the chunked 2D forward (launch_forward2d_cslab)
-// and variants of the staged 2D backprojector (launch_backward2d_smem).
-constexpr int kFwdChunkShapes[] = {4,   104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438, 439,
-                                   440, 441, 442, 443, 444, 447, 448, 449, 450, 451, 453, 463, 473,
-                                   474, 484};
-constexpr int kBwdStagedVariants[] = {3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38, 48, 68};
+// and variants of the staged 2D backprojector (launch_backward2d_smem): the
+// defaults and the autotuner's other candidates.
+constexpr int kFwdChunkShapes[] = {443, 474, 484};
+constexpr int kBwdStagedVariants[] = {27, 48, 68};
 
 template <size_t N>
 bool listed(const int (&list)[N], int v) {
@@ -76,19 +69,18 @@ bool listed(const int (&list)[N], int v) {
 
 // Overrides of a new plan's algorithms for measurement and testing, read
 // from CURADON_GB300_ALGO: comma-separated key=value tokens, e.g.
-// "fwd2d=tex,bwd2d_minb=4".  Keys: fwd2d = alu | tex | slab | cslab |
-// cslab<shape> | hyb<1..7> | split<0..16>; bwd2d = alu | tex | smem |
-// split<0..16>; bwd2d_minb = 3 | 4 | 5 | 14 | 24 | 25 | 26 | 27 | 28 | 37 | 38 |
-// 48 | 68 (staged backprojector shapes; 37 / 38: 27 / 28 on absolute-position
-// pairs; 48: 38 with 8 x 4-pixel warps; 68: 48 with rows by bulk copies); adj2d = pair | quad; fwd3d = alu | tex3 | tex2l | slab | quad |
-// mixed; fwd3d_tex = 0..8 (texture warps of 8 in forward 5);
-// fwd3d_block = BXxBYxBZ;
-// bwd3d = scalar | pk | pkmagic | quad (backward 0) | ax8m5 | ax8 | ax16 |
-// ax16m4 (backward 1); adj3d = pair | quad; adj3d_order = band | view;
-// adj3d_merge = 0 | 1; t3d = step | exact (running-sum or drift-free sample
-// parameters of the 3D ray marches).
-// Unknown tokens are
-// ignored; without the variable every plan starts at the measured defaults.
+// "fwd2d=tex,bwd2d_minb=48".  Keys: fwd2d = alu | tex | cslab |
+// cslab<443 | 474 | 484>; bwd2d = alu | tex | smem; bwd2d_minb = 27 | 48 | 68
+// (staged backprojector variants); adj2d = pair | quad; fwd3d = alu | tex3 |
+// quad | mixed; fwd3d_tex = 0..8 (texture warps of 8 in the mixed forward);
+// fwd3d_block = BXxBYxBZ; bwd3d = quad | pair (general kernel on row-pair
+// quads or on 8-byte pairs, its fallback where quads do not fit) | ax8m5
+// (axial runs);
+// adj3d = pair | quad; adj3d_order = band | view; adj3d_merge = 0 | 1;
+// adj3d_agg = 0 | 1 (warp-aggregated atomics on the merged quads);
+// t3d = step | exact (running-sum or drift-free sample parameters of the 3D
+// ray marches).  Unknown tokens are ignored; without the variable every plan
+// starts at the measured defaults.
 void apply_algo_env(Plan2d *p2, Plan3d *p3) {
     const char *env = std::getenv("CURADON_GB300_ALGO");
     if (!env) return;
@@ -108,38 +100,17 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
     for (const auto &[key, val] : kv) {
         if (p2 && key == "fwd2d") {
             if (val == "alu") p2->algo_fwd = 0;
-            for (int k = 0; k <= 16; ++k)
-                if (val == "split" + std::to_string(k)) p2->algo_fwd = 5, p2->split_sixteenths = k;
             if (val == "tex") p2->algo_fwd = 1;
-            if (val == "slab") p2->algo_fwd = 3;
             if (val.rfind("cslab", 0) == 0) {
                 p2->algo_fwd = 4;
-                // chunk shapes: 4 (rows x 512-pair rows, 256-cell bundles), 104 / 108
-                // (4 / 8 rows, 128-cell bundles), 204 / 304 / 308 (packed sums),
-                // 404 / 408 (packed sums and pair reuse), 414 / 418 / 428 (the
-                // same with 2 threads per cell, each on 2 of the 4 views), 438
-                // (8 views per bundle, 2 threads per cell on 4 each), 448 (16
-                // views per 64-cell bundle, 4 threads per cell on 4 each), 439
-                // (438 at <= 64 registers), 441 (439 with half-warps of 8 cells x
-                // 2 view groups), 442 / 443 (441 with 12 / 16-row chunks), 444 (443
-                // with 192-pair windows at <= 64 registers), 447 (8
-                // views per 64-cell bundle, 4 threads per cell on 2 each), 451 / 453
-                // (441 / 443 with interleaved view groups), 463 / 473 (443 / 453
-                // reading absolute-position pairs), 474 (473 without pair reuse),
-                // 484 (474 staged by bulk copies on mbarriers)
                 for (int k : kFwdChunkShapes)
                     if (val == "cslab" + std::to_string(k)) p2->fwd_chunk_rows = k;
             }
-            for (int k = 1; k < 8; ++k)
-                if (val == "hyb" + std::to_string(k)) p2->algo_fwd = 2, p2->tex_eighths = k;
         }
         if (p2 && key == "bwd2d") {
             if (val == "alu") p2->algo_bwd = 0;
             if (val == "tex") p2->algo_bwd = 1;
             if (val == "smem") p2->algo_bwd = 2;
-            for (int k = 0; k <= 16; ++k)
-                if (val == "split" + std::to_string(k) && !p2->vec && p2->nangles <= 2048)
-                    p2->algo_bwd = 3, p2->bwd_split_sixteenths = k;
         }
         if (p2 && key == "adj2d") {
             if (val == "pair") p2->adj_quad = 0;
@@ -151,8 +122,6 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
         if (p3 && key == "fwd3d") {
             if (val == "alu") p3->algo_fwd = 0;
             if (val == "tex3") p3->algo_fwd = 1;
-            if (val == "tex2l") p3->algo_fwd = 2;
-            if (val == "slab") p3->algo_fwd = 3;
             if (val == "quad") p3->algo_fwd = 4;
             if (val == "mixed") p3->algo_fwd = 5;
         }
@@ -160,17 +129,15 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
             for (int k = 0; k <= 8; ++k)
                 if (val == std::to_string(k)) p3->fwd_tex_warps = k;
         if (p3 && key == "bwd3d") {
-            static const char *general[] = {"scalar", "pk", "pkmagic", "quad"};
-            static const char *runs[] = {"ax8m5", "ax8", "ax16", "ax16m4"};
-            for (int i = 0; i < 4; ++i) {
-                if (val == general[i]) p3->algo_bwd = 0, p3->bwd_packed = i;
-                if (val == runs[i]) p3->algo_bwd = 1, p3->bwd_axial = i;
-            }
+            if (val == "quad") p3->algo_bwd = 0, p3->bwd_packed = 3;
+            if (val == "pair") p3->algo_bwd = 0, p3->bwd_packed = 2;
+            if (val == "ax8m5") p3->algo_bwd = 1;
         }
         if (p3 && key == "t3d") {
             if (val == "step") p3->exact_t = false;
             if (val == "exact") p3->exact_t = true;
         }
+        if (p3 && key == "adj3d_agg") p3->adj_agg = val == "1";
         if (p3 && key == "adj3d_merge") {
             if (val == "0") p3->adj_merge = false;
             if (val == "1") p3->adj_merge = true;
@@ -659,12 +626,12 @@ int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by) {
 int cg_plan2d_set_algorithm(cg_plan2d *plan, int forward, int backward) {
     clear_error();
     CG_REQUIRE(plan, "plan is NULL");
-    CG_REQUIRE(forward >= -1 && forward <= 5, "2D forward algorithm must be -1..5");
-    CG_REQUIRE(backward >= -1 && backward <= 3, "2D backward algorithm must be -1..3");
+    CG_REQUIRE(forward == -1 || forward == 0 || forward == 1 || forward == 4,
+               "2D forward algorithm must be 0 (registers), 1 (texture) or 4 (chunked)");
+    CG_REQUIRE(backward >= -1 && backward <= 2,
+               "2D backward algorithm must be 0 (registers), 1 (texture) or 2 (staged)");
     CG_REQUIRE(!plan->vec || backward == -1 || backward == 2,
                "vector-geometry plans backproject with the staged algorithm (2)");
-    CG_REQUIRE(backward != 3 || plan->nangles <= 2048,
-               "the split backprojection takes at most 2048 views");
     if (forward >= 0) plan->algo_fwd = forward;
     if (backward >= 0) plan->algo_bwd = backward;
     return CG_OK;
@@ -709,83 +676,18 @@ int cg_plan2d_tables(const cg_plan2d *plan, float *sources, float *u_origins, fl
 
 namespace {
 
-int ensure_aux_stream(cg_plan2d *plan);
-
-// Forward algorithm 5: the first share of the views through the texture unit
-// on the plan's internal stream, the rest by the chunked forward on the
-// caller's stream, the two kernels resident side by side (the chunked
-// forward's blocks are bounded by shared memory, the texture forward's use
-// none).  The internal stream forks from and joins back into the caller's
-// stream through events, so the call stays stream-ordered and capturable.
-int forward2d_split(cg_plan2d *plan, const float *volume, float *sinogram, cudaStream_t s) {
-    int rc = load_vol_texture(*plan, volume, s);
-    if (rc) return rc;
-    if ((rc = ensure_aux_stream(plan))) return rc;
-    const int vt = (int)((long long)plan->nangles * plan->split_sixteenths / 16);
-    CG_TRY_CUDA(cudaEventRecord(plan->ev_fork, s));
-    CG_TRY_CUDA(cudaStreamWaitEvent(plan->aux, plan->ev_fork, 0));
-    rc = launch_forward2d_tex_views(*plan, sinogram, 0, vt, plan->aux);
-    if (!rc) rc = launch_forward2d_cslab(*plan, sinogram, s, plan->fwd_chunk_rows, vt);
-    // join even after an error so the caller's stream (or capture) is whole
-    const cudaError_t e1 = cudaEventRecord(plan->ev_join, plan->aux);
-    const cudaError_t e2 = cudaStreamWaitEvent(s, plan->ev_join, 0);
-    if (rc) return rc;
-    CG_TRY_CUDA(e1);
-    CG_TRY_CUDA(e2);
-    return CG_OK;
-}
-
 int forward2d_f32(cg_plan2d *plan, const float *volume, float *sinogram, cudaStream_t s) {
     if (plan->algo_fwd == 1) return launch_forward2d_tex(*plan, volume, sinogram, s);
-    if (plan->algo_fwd == 2) return launch_forward2d_hyb(*plan, volume, sinogram, s);
     int rc = launch_relayout2d(*plan, volume, s);
     if (rc) return rc;
-    if (plan->algo_fwd == 3 && slab_supported(*plan))
-        return launch_forward2d_slab(*plan, sinogram, s);
     if (plan->algo_fwd == 4) return launch_forward2d_cslab(*plan, sinogram, s, plan->fwd_chunk_rows);
-    if (plan->algo_fwd == 5) return forward2d_split(plan, volume, sinogram, s);
     return launch_forward2d(*plan, sinogram, s);
-}
-
-// Backward algorithm 3: the last share of the pixel rows through the
-// texture unit on the plan's internal stream, the first rows by the staged
-// backprojector on the caller's stream, side by side (the staged kernel is
-// bound by instruction issue, the texture one by the texture unit); the rows
-// are disjoint, so the two add into the volume independently.
-int ensure_aux_stream(cg_plan2d *plan) {
-    if (!plan->aux) {
-        CG_TRY_CUDA(cudaStreamCreateWithFlags(&plan->aux, cudaStreamNonBlocking));
-        CG_TRY_CUDA(cudaEventCreateWithFlags(&plan->ev_fork, cudaEventDisableTiming));
-        CG_TRY_CUDA(cudaEventCreateWithFlags(&plan->ev_join, cudaEventDisableTiming));
-    }
-    return CG_OK;
-}
-
-int backward2d_split(cg_plan2d *plan, float *volume, cudaStream_t s) {
-    constexpr int kTile = 64;  // pixel rows of one staged tile
-    const int ys = (int)((long long)plan->H * (16 - plan->bwd_split_sixteenths) / 16) / kTile * kTile;
-    int rc = ensure_aux_stream(plan);
-    if (rc) return rc;
-    CG_TRY_CUDA(cudaEventRecord(plan->ev_fork, s));
-    CG_TRY_CUDA(cudaStreamWaitEvent(plan->aux, plan->ev_fork, 0));
-    rc = launch_backward2d_tex_rows(*plan, volume, ys, plan->aux);
-    if (!rc) rc = launch_backward2d_smem(*plan, volume, s, ys);
-    const cudaError_t e1 = cudaEventRecord(plan->ev_join, plan->aux);
-    const cudaError_t e2 = cudaStreamWaitEvent(s, plan->ev_join, 0);
-    if (rc) return rc;
-    CG_TRY_CUDA(e1);
-    CG_TRY_CUDA(e2);
-    return CG_OK;
 }
 
 int backward2d_f32(cg_plan2d *plan, float *volume, const float *sinogram, cudaStream_t s) {
     if (plan->algo_bwd == 1) return launch_backward2d_tex(*plan, volume, sinogram, s);
     int rc = launch_relayout_sino2d(*plan, sinogram, s);
     if (rc) return rc;
-    if (plan->algo_bwd == 3) {
-        if ((rc = load_sino_texture(*plan, sinogram, s))) return rc;
-        return backward2d_split(plan, volume, s);
-    }
     if (plan->algo_bwd == 2) return launch_backward2d_smem(*plan, volume, s);
     return launch_backward2d(*plan, volume, s);
 }
@@ -874,7 +776,8 @@ int cg_plan3d_create(cg_plan3d **plan, int device, const uint64_t vol_shape[3],
 int cg_plan3d_set_algorithm(cg_plan3d *plan, int forward, int backward) {
     clear_error();
     CG_REQUIRE(plan, "plan is NULL");
-    CG_REQUIRE(forward >= -1 && forward <= 5, "3D forward algorithm must be -1..5");
+    CG_REQUIRE(forward == -1 || forward == 0 || forward == 1 || forward == 4 || forward == 5,
+               "3D forward algorithm must be 0 (registers), 1 (texture), 4 (quad) or 5 (mixed)");
     CG_REQUIRE(backward >= -1 && backward <= 1, "3D backward algorithm must be -1..1");
     if (forward >= 0) plan->algo_fwd = forward;
     if (backward >= 0) plan->algo_bwd = backward;
@@ -905,7 +808,6 @@ int cg_forward_3d_plan(cg_plan3d *plan, const float *volume, float *sinogram, vo
     CG_REQUIRE(volume && sinogram, "volume and sinogram must be device pointers");
     DeviceGuard guard(plan->device);
     CG_REQUIRE(guard.ok(), "cannot select the plan's device");
-    if (plan->algo_fwd == 3) return launch_forward3d_slab(*plan, volume, sinogram, (cudaStream_t)stream);
     if (plan->algo_fwd >= 4) return launch_forward3d_quad(*plan, volume, sinogram, (cudaStream_t)stream);
     if (plan->algo_fwd != 0) return launch_forward3d_tex(*plan, volume, sinogram, (cudaStream_t)stream);
     int rc = ensure_plan3d_scratch(*plan, true, false);
@@ -953,9 +855,7 @@ int cg_forward_3d(const float *x, const uint64_t vol_shape[3], const float vol_s
     rc = make_plan3d(&p, dev, vol_shape, vol_spacing, vol_offset, phi, theta, psi, nangles,
                      det_shape, det_spacing, det_offset, det_rotation, DSO, DSD, COR);
     if (rc) return rc;
-    if (p->algo_fwd == 3) {
-        rc = launch_forward3d_slab(*p, x, sinogram, (cudaStream_t)stream);
-    } else if (p->algo_fwd >= 4) {
+    if (p->algo_fwd >= 4) {
         rc = launch_forward3d_quad(*p, x, sinogram, (cudaStream_t)stream);
     } else if (p->algo_fwd != 0) {
         rc = launch_forward3d_tex(*p, x, sinogram, (cudaStream_t)stream);

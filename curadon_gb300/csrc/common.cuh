@@ -104,43 +104,22 @@ struct Plan2d {
     cudaTextureObject_t tex_vol = 0, tex_sino = 0;
 
     // algorithm per operator: forward 0 = registers, 1 = texture unit,
-    // 2 = texture + registers, 3 = shared-memory row slabs, 4 = chunked
-    // shared-memory slabs, 5 = chunked slabs beside the texture unit on a
-    // share of the views;
-    // backprojection 0 = registers, 1 = texture unit, 2 = shared-memory rows.
-    // Defaults: the fastest measured on GB300 (2D n-sweep); the forward
-    // becomes chunked for volumes of 704^2 pixels and more (cg_plan2d_create).
+    // 4 = chunked shared-memory slabs; backprojection 0 = registers,
+    // 1 = texture unit, 2 = staged shared-memory windows.  Defaults: the
+    // fastest measured on GB300 (2D n-sweep); the forward becomes chunked for
+    // volumes of 704^2 pixels and more (cg_plan2d_create).
     int algo_fwd = 1, algo_bwd = 2;
-    int tex_eighths = 4;              // hybrid forward: share of warps on the texture unit
-    // split forward (algorithm 5): sixteenths of the views projected by the
-    // texture unit on an internal stream beside the chunked forward's rest
-    int split_sixteenths = 4;
-    // split backprojection (algorithm 3): sixteenths of the pixel rows
-    // backprojected by the texture unit beside the staged kernel's rest
-    int bwd_split_sixteenths = 3;
-    cudaStream_t aux = nullptr;       // internal stream, created on first use
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    // chunked forward: chunk shape; 484 = 16-row chunks staged by bulk
-    // copies of the tensor memory access unit on mbarriers, bundles of 8
-    // views x 128 cells, two threads per cell on 4 interleaved views each,
-    // each half-warp on 8 cells x 2 adjacent views, packed sums,
-    // absolute-position pairs, both pairs loaded per sample, 3 blocks/SM
-    // (-5.6 % at n=2048 against 474, the same staged by per-lane cp.async;
-    // 474 is -2 % against 473, which takes the lower pair from the previous
-    // sample where the column did not move, and -18 % against 443, 473 with
-    // view groups 4 views apart and (v, d) pairs)
+    // chunked forward's kernel shape: 484 (default: 16-row chunks staged by
+    // bulk copies on mbarriers, bundles of 8 views x 128 cells, two threads
+    // per cell on 4 interleaved views, packed sums, absolute-position pairs),
+    // 474 (the same staged by per-lane cp.async) or 443 ((v, d) pairs, pair
+    // reuse, view groups four views apart); the autotuner's candidates
     int fwd_chunk_rows = 484;
-    // staged backprojector variant: 68 = 4 blocks/SM, packed FP32 pairs of
-    // rows, floor taken by FP32 adds, window rows by bulk copies of the tensor
-    // memory access unit (pair-wise cp.async where a window reaches past the
-    // row), view loop unrolled 4 times, absolute-position sinogram pairs,
-    // warps on 8 x 4 pixels (default, measured fastest: -5 % against 48, the
-    // same staged pair by pair with cp.async; 48 is -2 % against 38, the same
-    // with warps on 32 x 1 pixels; 38 is -6.5 % against 27, the same unrolled
-    // twice on (t, d) pairs); 37 = 38 unrolled twice; 24 = 27 with register
-    // copies; 25 / 26 = 24
-    // with the view loop unrolled 4 / 1 times; 28 = 27 unrolled 4 times; 14 =
-    // 24 with the conversion unit's floor; 3, 4, 5 = scalar at 3..5 blocks/SM
+    // staged backprojector's variant: 68 (default: packed FP32 row pairs,
+    // floor by FP32 adds, window rows by bulk copies, absolute-position
+    // pairs, 8 x 4-pixel warps), 48 (the same staged pair by pair with
+    // cp.async) or 27 ((t, d) pairs, 32 x 1-pixel warps); the autotuner's
+    // candidates
     int bwd_min_blocks = 68;
 
     // row pitches of layA / layB in pairs, even so every row starts on 16 bytes
@@ -209,34 +188,28 @@ struct Plan3d {
     // merge consecutive samples' shared quad element into one atomic
     // (-11 % at 128^3, -10 % at 256^3)
     bool adj_merge = true;
+    // merged quads plus warp-aggregated atomics (lanes whose lower-slice
+    // element coincides combine before one atomic)
+    bool adj_agg = false;
     // ray-march sample parameters t_k = tmin + k h by one FMA instead of the
     // reference's running sum t += h, whose rounding accumulates along long
     // rays (on from 512 voxels along an axis: against the FP64 oracle the
     // running sum leaves rays of a 512^3 volume up to 2.5e-3 off, relative)
     bool exact_t = false;
 
-    // texture-unit variants (allocated on first use)
-    cudaArray_t arr3 = nullptr, arrA = nullptr, arrB = nullptr;
-    cudaTextureObject_t tex3 = 0, texA = 0, texB = 0;
-    float *d_volT = nullptr;          // x<->z transposed volume for arrB
+    // texture-unit forward (allocated on first use)
+    cudaArray_t arr3 = nullptr;
+    cudaTextureObject_t tex3 = 0;
 
-    // forward 0 = registers, 1 = tex3D, 2 = layered bilinear + lerp,
-    // 3 = shared-memory slabs, 4 = quads (FP32 trilinear, two 16-byte loads
-    // per sample), 5 = quads with some warps on the texture unit; backward 0 = general voxel runs along z,
-    // 1 = runs along y when every view maps y onto the detector's v axis
-    // (`axial`; otherwise 0 runs);
-    // defaults: the fastest measured on GB300 (256^3 and 512^3 workloads)
+    // forward 0 = registers, 1 = tex3D, 4 = quads (FP32 trilinear, two
+    // 16-byte loads per sample), 5 = quads with some warps on the texture
+    // unit; backward 0 = general voxel runs along z, 1 = runs along y when
+    // every view maps y onto the detector's v axis (`axial`; otherwise 0
+    // runs).  Defaults: the fastest measured on GB300 (256^3 and 512^3)
     int algo_fwd = 5, algo_bwd = 1;
-    // backward 0: 3 = two voxels per packed FP32 instruction with the floor
-    // by FP32 adds, each bilinear sample one 16-byte load of a row-pair quad
-    // (default; -9 % at 256^3 and 512^3 against 2), 2 = the same reading two
-    // 8-byte pairs, 1 = packed with the conversion unit's floor, 0 = one
-    // voxel at a time
+    // backward 0: 3 = each bilinear sample one 16-byte load of a row-pair
+    // quad (default), 2 = two 8-byte pairs (where the quads do not fit)
     int bwd_packed = 3;
-    // backward 1: 0 = runs of 8 voxels at <= 48 registers (default; -27 % at
-    // 256^3 and -29 % at 512^3 against backward 0), 1 = runs of 8 at <= 64,
-    // 2 / 3 = runs of 16 at <= 80 / 64
-    int bwd_axial = 0;
     // forward 5: warps of each 8 that sample through the texture unit (4 for
     // volumes of 300^3 voxels and more, set at plan creation)
     int fwd_tex_warps = 3;
@@ -290,18 +263,13 @@ int launch_backward2d(const Plan2d &p, float *vol, cudaStream_t s);
 
 int ensure_plan3d_scratch(Plan3d &p, bool fwd, bool bwd);
 int launch_forward3d(const Plan3d &p, const float *vol, float *sino, cudaStream_t s);
-int launch_forward3d_slab(Plan3d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_forward3d_quad(Plan3d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s);
 
 int launch_adjoint2d(Plan2d &p, float *vol, const float *sino, cudaStream_t s);
 int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s);
 
-int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s, int rows = -1);
-int load_sino_texture(Plan2d &p, const float *sino, cudaStream_t s);
-int launch_backward2d_tex_rows(const Plan2d &p, float *vol, int y0, cudaStream_t s);
-bool slab_supported(const Plan2d &p);
-int launch_forward2d_slab(const Plan2d &p, float *sino, cudaStream_t s);
+int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s);
 // rows: chunk shape (4, 8: rows of 256-cell bundles; 104, 108: 4 or 8 rows
 // of 128-cell bundles)
 int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int rows, int v0 = 0,
@@ -310,15 +278,13 @@ int launch_forward2d_tex_views(const Plan2d &p, float *sino, int v0, int nv, cud
 // Copies the volume into the plan's 2D texture array.
 int load_vol_texture(Plan2d &p, const float *vol, cudaStream_t s);
 int ensure_vol_texture(Plan2d &p);
-int launch_batch2d_fwd_tex(const Prob2d *d_probs, const std::vector<Prob2d> &probs,
+// the first `active` problems of a batch (the work list's blocks [0, total))
+int launch_batch2d_fwd_tex(const Prob2d *d_probs, const std::vector<Prob2d> &probs, int active,
                            const int *starts, int total, cudaStream_t s);
 int launch_forward2d_tex(Plan2d &p, const float *vol, float *sino, cudaStream_t s);
-int launch_forward2d_hyb(Plan2d &p, const float *vol, float *sino, cudaStream_t s);
 int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t s);
+// texture forward (tex3D, the reference's trilinear sampling)
 int launch_forward3d_tex(Plan3d &p, const float *vol, float *sino, cudaStream_t s);
-// texture forward, trilinear (tex3D) or layered bilinear + FP32 lerp
-int launch_forward3d_texture(Plan3d &p, const float *vol, float *sino, cudaStream_t s,
-                             bool trilinear);
 int upload_volume_texture3(Plan3d &p, const float *vol, cudaStream_t s);
 
 // Reads CURADON_GB300_ALGO ("fwd2d=tex,bwd2d=smem,fwd3d=tex2l,...") over the

@@ -229,14 +229,11 @@ __global__ void __launch_bounds__(256)
               blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
 }
 
-// ------------------------------------------------------------ forward, slab
+// ------------------------------------------------------------ forward, shared ray set-up
 
-constexpr int kSlabThreads = 1024;
-constexpr int kSlabRing = 3;  // staged rows: r, r+1 in use, r+2 in flight
-
-// Ray set-up shared by the slab kernel's two passes: the reference's FP32
-// sequence (forward_2d.hpp:52-68, intersection.h:31-46).  Returns false for a
-// ray that misses the box.
+// Ray set-up of the chunked forward: the reference's FP32 sequence
+// (forward_2d.hpp:52-68, intersection.h:31-46).  Returns false for a ray that
+// misses the box.
 struct FanRay {
     float p, vp, q, fq, nrm;
     int n, sq;
@@ -276,140 +273,6 @@ __device__ __forceinline__ bool fan_ray(const float2 s, const float2 o, const fl
     return true;
 }
 
-// Row-synchronous forward projection.  Block = (group of G views) x (ray
-// class: y-stepping rays on layA when blockIdx.y == 0, x-stepping rays on
-// layB when 1); thread t owns the rays of cells t, t + 1024, ... of each view
-// of the group, RPV per view.  The block walks the rows of its layout in
-// order; each padded row of pairs is copied into a 3-slot shared-memory ring
-// with 16-byte cp.async (one row ahead of use), and every ray active on row r
-// takes its sample from rows r and r + 1 there: two conflict-free 8-byte
-// shared loads and two FMAs.  A ray's row range is the reference's
-// rint(max|rd|) unit steps from its entry row; rays stepping towards smaller
-// rows are visited in the opposite order (same samples, summed backwards).
-// Rays that miss the box are written as 0 by the class-0 block.
-template <int RPV, int G>
-__global__ void __launch_bounds__(kSlabThreads, 1)
-    k_fwd2d_slab(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
-                 float *__restrict__ sino, const float2 *__restrict__ tsrc,
-                 const float2 *__restrict__ tu0, const float2 *__restrict__ tdu, int W, int H,
-                 int det, int nangles, float sx, float sy, int pa, int pb) {
-    extern __shared__ __align__(16) float2 ring[];  // kSlabRing x pitch
-    __shared__ int s_rmin, s_rmax;
-    constexpr int R = RPV * G;
-    const bool cls_y = blockIdx.y == 0;
-    const float2 *lay = cls_y ? layA : layB;
-    const int pitch = cls_y ? pa : pb;
-    const int qmax = cls_y ? H : W;   // rows of the layout run over [-kPad, qmax + 1]
-    const unsigned pcap = (unsigned)((cls_y ? W : H) + kPad);
-    const int v0 = blockIdx.x * G;
-
-    if (threadIdx.x == 0) s_rmin = INT_MAX, s_rmax = INT_MIN;
-    __syncthreads();
-
-    float p[R], V[R], alo[R], ahi[R];
-    int rlo[R], len[R];
-    int my_min = INT_MAX, my_max = INT_MIN;
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-        const int view = v0 + i / RPV, u = threadIdx.x + (i % RPV) * kSlabThreads;
-        alo[i] = ahi[i] = 0.f;
-        len[i] = 0;
-        rlo[i] = 0;
-        p[i] = V[i] = 0.f;
-        if (view >= nangles || u >= det) continue;
-        FanRay r;
-        if (!fan_ray(tsrc[view], tu0[view], tdu[view], u, W, H, sx, sy, r)) continue;
-        if (r.ymajor != cls_y) continue;
-        const int iq = (int)fminf(fmaxf(floorf(r.q), -(float)kPad), (float)qmax);
-        const int n = min(r.n, r.sq > 0 ? qmax - iq + 1 : iq + kPad + 1);
-        if (n <= 0) continue;
-        const int lo = r.sq > 0 ? iq : iq - (n - 1);
-        V[i] = r.sq > 0 ? r.vp : -r.vp;
-        // position at row `lo`: the entry point for forward-stepping rays,
-        // the last sample for backward-stepping ones
-        p[i] = r.sq > 0 ? r.p : fmaf((float)(n - 1), r.vp, r.p);
-        rlo[i] = lo;
-        len[i] = n;
-        my_min = min(my_min, lo);
-        my_max = max(my_max, lo + n - 1);
-    }
-    if (my_min <= my_max) {
-        atomicMin(&s_rmin, my_min);
-        atomicMax(&s_rmax, my_max);
-    }
-    __syncthreads();
-    const int rmin = s_rmin, rmax = s_rmax;
-
-    if (rmin <= rmax) {
-        // rows rmin .. rmax + 1 are read; row index q lives at padded q + kPad
-        const int chunks = pitch / 2;  // 16-byte chunks per row
-        auto stage = [&](int row) {
-            if (row > qmax + 1) return;
-            const float4 *src =
-                reinterpret_cast<const float4 *>(lay + (size_t)(row + kPad) * pitch);
-            float4 *dst = reinterpret_cast<float4 *>(ring + ((row - rmin) % kSlabRing) * pitch);
-            for (int c = threadIdx.x; c < chunks; c += kSlabThreads) {
-                const unsigned sa = (unsigned)__cvta_generic_to_shared(dst + c);
-                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa),
-                             "l"(src + c));
-            }
-        };
-        stage(rmin);
-        stage(rmin + 1);
-        asm volatile("cp.async.commit_group;\n" ::);
-        for (int r = rmin; r <= rmax; ++r) {
-            asm volatile("cp.async.wait_group 0;\n" ::);
-            __syncthreads();
-            stage(r + 2);
-            asm volatile("cp.async.commit_group;\n" ::);
-            const float2 *rowlo = ring + ((r - rmin) % kSlabRing) * pitch;
-            const float2 *rowhi = ring + ((r + 1 - rmin) % kSlabRing) * pitch;
-#pragma unroll
-            for (int i = 0; i < R; ++i) {
-                if ((unsigned)(r - rlo[i]) < (unsigned)len[i]) {
-                    const float pf = floorf(p[i]);
-                    const float fp = p[i] - pf;
-                    const unsigned ip = min((unsigned)((int)pf + kPad), pcap);
-                    const float2 lo = rowlo[ip], hi = rowhi[ip];
-                    alo[i] += fmaf(fp, lo.y, lo.x);
-                    ahi[i] += fmaf(fp, hi.y, hi.x);
-                    p[i] += V[i];
-                }
-            }
-        }
-        asm volatile("cp.async.wait_group 0;\n" ::);
-    }
-
-#pragma unroll
-    for (int i = 0; i < R; ++i) {
-        const int view = v0 + i / RPV, u = threadIdx.x + (i % RPV) * kSlabThreads;
-        if (view >= nangles || u >= det) continue;
-        FanRay r;
-        float out;
-        if (!fan_ray(tsrc[view], tu0[view], tdu[view], u, W, H, sx, sy, r)) {
-            if (!cls_y) continue;
-            out = 0.f;
-        } else {
-            if (r.ymajor != cls_y) continue;
-            out = fmaf(r.fq, ahi[i] - alo[i], alo[i]) * r.nrm;
-        }
-        sino[(size_t)view * det + u] = out;
-    }
-}
-
-template <int RPV, int G>
-int launch_slab(const Plan2d &p, float *sino, cudaStream_t s) {
-    const int pitch = max(p.pitchA(), p.pitchB());
-    const size_t smem = sizeof(float2) * (size_t)kSlabRing * pitch;
-    if (int rc = ensure_smem_attr((const void *)k_fwd2d_slab<RPV, G>, (int)smem)) return rc;
-    dim3 grid(ceil_div(p.nangles, G), 2);
-    k_fwd2d_slab<RPV, G><<<grid, kSlabThreads, smem, s>>>(
-        p.d_layA, p.d_layB, sino, p.d_src, p.d_u0, p.d_du, p.W, p.H, p.det, p.nangles, p.sx,
-        p.sy, p.pitchA(), p.pitchB());
-    CG_TRY_CUDA(cudaGetLastError());
-    return CG_OK;
-}
-
 }  // namespace
 
 __device__ unsigned long long g_wait_timeouts = 0;
@@ -423,34 +286,11 @@ int take_wait_timeouts(unsigned long long *count) {
 
 // True for the chunked forward's shapes that read the absolute-position
 // layouts (relayout2d_tile<true>).
-bool cslab_abs(int rows) {
-    return rows == 463 || rows == 473 || rows == 474 || rows == 484;
-}
+bool cslab_abs(int rows) { return rows == 474 || rows == 484; }
 
-// True for the staged backprojector's shapes that read the absolute-position
-// sinogram pairs (relayout_sino2d_elem<true>).
-bool bwd_abs(int min_blocks) {
-    return min_blocks == 37 || min_blocks == 38 || min_blocks == 48 || min_blocks == 68;
-}
-
-// True when the slab forward supports the plan's sizes.
-bool slab_supported(const Plan2d &p) {
-    const size_t smem = sizeof(float2) * kSlabRing * (size_t)std::max(p.pitchA(), p.pitchB());
-    return p.det <= 6 * kSlabThreads && smem <= 200 * 1024;
-}
-
-int launch_forward2d_slab(const Plan2d &p, float *sino, cudaStream_t s) {
-    const int rpv = ceil_div(p.det, kSlabThreads);
-    switch (rpv) {
-        case 1: return launch_slab<1, 4>(p, sino, s);
-        case 2: return launch_slab<2, 3>(p, sino, s);
-        case 3: return launch_slab<3, 2>(p, sino, s);
-        case 4: return launch_slab<4, 1>(p, sino, s);
-        case 5: return launch_slab<5, 1>(p, sino, s);
-        case 6: return launch_slab<6, 1>(p, sino, s);
-        default: return set_error(CG_ERR_INVALID, "detector too wide for the slab forward");
-    }
-}
+// True for the staged backprojector's variants that read the
+// absolute-position sinogram pairs (relayout_sino2d_elem<true>).
+bool bwd_abs(int min_blocks) { return min_blocks == 48 || min_blocks == 68; }
 
 namespace {
 
@@ -815,13 +655,7 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
     // views [v0, v0 + nv): the kernel sees offset tables and sinogram rows
     if (nv < 0) nv = p.nangles - v0;
     if (nv <= 0) return CG_OK;
-    const int ng = rows == 438 || rows == 439 || rows == 440 || rows == 441 || rows == 442 ||
-                           rows == 443 || rows == 444 || rows == 447 || rows == 451 ||
-                           rows == 453 || rows == 463 || rows == 473 || rows == 474 ||
-                           rows == 484
-                       ? 8
-                   : rows == 448 || rows == 449 || rows == 450   ? 16
-                                                                 : kCs2G;  // views per bundle
+    const int ng = 8;  // views per bundle of the compiled shapes
     const int groups = ceil_div(nv, ng);
     if (groups > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     if (std::max(p.pitchA(), p.pitchB()) >= 32768)
@@ -836,35 +670,14 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
         CG_TRY_CUDA(cudaGetLastError());
         return CG_OK;
     };
+    // the default (484) and the autotuner's other candidates (474: the same
+    // staged by per-lane cp.async; 443: (v, d) pairs, pair reuse, view groups
+    // four views apart); the measured history of the shapes is in the design
+    // notes
     switch (rows) {
-        case 4: return go(k_fwd2d_cslab<4, 512, 256, false>, 4, 512, 256);
-        case 104: return go(k_fwd2d_cslab<4, 256, 128, false>, 4, 256, 128);
-        case 108: return go(k_fwd2d_cslab<8, 256, 128, false>, 8, 256, 128);
-        case 204: return go(k_fwd2d_cslab<4, 512, 256, true>, 4, 512, 256);
-        case 304: return go(k_fwd2d_cslab<4, 256, 128, true>, 4, 256, 128);
-        case 308: return go(k_fwd2d_cslab<8, 256, 128, true>, 8, 256, 128);
-        case 408: return go(k_fwd2d_cslab<8, 256, 128, true, true>, 8, 256, 128);
-        case 418: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2>, 8, 256, 128, 2);
-        case 414: return go(k_fwd2d_cslab<4, 256, 128, true, true, 2>, 4, 256, 128, 2);
-        case 428: return go(k_fwd2d_cslab<8, 512, 256, true, true, 2>, 8, 512, 256, 2);
-        case 438: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8>, 8, 256, 128, 2);
-        case 448: return go(k_fwd2d_cslab<8, 256, 64, true, true, 4, 16>, 8, 256, 64, 4);
-        case 439: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 4>, 8, 256, 128, 2);
-        case 447: return go(k_fwd2d_cslab<8, 256, 64, true, true, 4, 8>, 8, 256, 64, 4);
-        case 440: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 5>, 8, 256, 128, 2);
-        case 441: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 4, 1>, 8, 256, 128, 2);
-        case 442: return go(k_fwd2d_cslab<12, 256, 128, true, true, 2, 8, 4, 1>, 12, 256, 128, 2);
         case 443: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 1>, 16, 256, 128, 2);
-        case 453: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 2>, 16, 256, 128, 2);
-        case 463: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 1, true>, 16, 256, 128, 2);
-        case 473: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 2, true>, 16, 256, 128, 2);
         case 474: return go(k_fwd2d_cslab<16, 256, 128, true, false, 2, 8, 3, 2, true>, 16, 256, 128, 2);
         case 484: return go(k_fwd2d_cslab<16, 256, 128, true, false, 2, 8, 3, 2, true, true>, 16, 256, 128, 2);
-        case 451: return go(k_fwd2d_cslab<8, 256, 128, true, true, 2, 8, 4, 2>, 8, 256, 128, 2);
-        case 444: return go(k_fwd2d_cslab<16, 192, 128, true, true, 2, 8, 4, 1>, 16, 192, 128, 2);
-        case 449: return go(k_fwd2d_cslab<8, 256, 64, true, true, 4, 16, 3>, 8, 256, 64, 4);
-        case 450: return go(k_fwd2d_cslab<8, 256, 128, true, true, 4, 16, 2>, 8, 256, 128, 4);
-        case 404: return go(k_fwd2d_cslab<4, 256, 128, true, true>, 4, 256, 128);
         default: return set_error(CG_ERR_INVALID, "unknown chunk shape");
     }
 }
@@ -963,8 +776,11 @@ constexpr int kSmWin = 128;   // pairs of one view's row staged for a tile
 // by a lane of warp 0 and completed on an mbarrier; rows whose window
 // reaches past the padded sinogram row are copied pair by pair with the
 // index clamp as before.
+// R: pixels per thread (rows 8 apart), so tiles of 32 x 8R pixels; every
+// pixel's sum runs over the views in the same order whatever R, so results
+// do not depend on it.
 template <bool PK, bool MAGIC = false, int VU = 2, bool CPA = false, bool ABS = false,
-          bool MAPQ = false, bool BULK = false>
+          bool MAPQ = false, bool BULK = false, int R = kSmRows>
 __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                                                 const float2 *__restrict__ S,
                                                 const float4 *__restrict__ proj, int W, int H,
@@ -980,7 +796,7 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
     const unsigned bar = (unsigned)__cvta_generic_to_shared(&s_bar);
     unsigned phase = 0;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int xt = bx * 32, yt = by * (8 * kSmRows);
+    const int xt = bx * 32, yt = by * (8 * R);
     const int x = xt + (MAPQ ? (int)((threadIdx.y & 3) * 8 + (threadIdx.x & 7)) : (int)threadIdx.x);
     const int y0 = yt + (MAPQ ? (int)((threadIdx.y >> 2) * 4 + (threadIdx.x >> 3)) : (int)threadIdx.y);
     const float ex = (float)W / 2.0f, ey = (float)H / 2.0f;
@@ -992,9 +808,9 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
     const float X = ((float)x - ex) * sx + ox + 0.5f;
     // rows r and r + 1 of the thread's column as one pair (the packed loop's
     // operands and accumulators)
-    float2 Y2[kSmRows / 2], acc2[kSmRows / 2];
+    float2 Y2[R / 2], acc2[R / 2];
 #pragma unroll
-    for (int i = 0; i < kSmRows / 2; ++i) {
+    for (int i = 0; i < R / 2; ++i) {
         Y2[i] = make_float2(((float)(y0 + 16 * i) - ey) * sy + oy + 0.5f,
                             ((float)(y0 + 16 * i + 8) - ey) * sy + oy + 0.5f);
         acc2[i] = make_float2(0.f, 0.f);
@@ -1034,7 +850,7 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 const float cX = ((float)(xt + (c & 1) * 31) - ex) * sx + ox + 0.5f;
-                const float cY = ((float)(yt + (c >> 1) * (8 * kSmRows - 1)) - ey) * sy + oy + 0.5f;
+                const float cY = ((float)(yt + (c >> 1) * (8 * R - 1)) - ey) * sy + oy + 0.5f;
                 const float den = fmaf(a.y, cY, fmaf(a.x, cX, a.z));
                 const float yi = fmaf(b.y, cY, fmaf(b.x, cX, b.z));
                 const float ub = fmaf(__fdividef(1.0f, den), yi, edm);
@@ -1128,7 +944,7 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                     const float2 A2 = make_float2(A, A), B2 = make_float2(B, B);
                     const float2 e2 = make_float2(edq, edq);
 #pragma unroll
-                    for (int r = 0; r < kSmRows; r += 2) {
+                    for (int r = 0; r < R; r += 2) {
                         const float2 Yr = Y2[r >> 1];
                         const float2 den = __ffma2_rn(ay, Yr, A2);
                         const float2 yi = __ffma2_rn(by, Yr, B2);
@@ -1160,7 +976,7 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
                     }
                 } else {
 #pragma unroll
-                    for (int r = 0; r < kSmRows; ++r) {
+                    for (int r = 0; r < R; ++r) {
                         const float den = fmaf(a.y, Yv(r), A);
                         const float yi = fmaf(b.y, Yv(r), B);
                         const float w = rcp_approx(den);
@@ -1176,7 +992,7 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
             } else {
                 const float2 *row = S + (size_t)(v0 + j) * pitch;
 #pragma unroll
-                for (int r = 0; r < kSmRows; ++r) {
+                for (int r = 0; r < R; ++r) {
                     const float den = fmaf(a.y, Yv(r), A);
                     const float yi = fmaf(b.y, Yv(r), B);
                     const float w = rcp_approx(den);
@@ -1199,7 +1015,7 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
     }
     if (x < W) {
 #pragma unroll
-        for (int r = 0; r < kSmRows; ++r) {
+        for (int r = 0; r < R; ++r) {
             const int y = y0 + 8 * r;
             const float a = (r & 1) ? acc2[r >> 1].y : acc2[r >> 1].x;
             if (y < H) vol[(size_t)y * W + x] += a * inv;
@@ -1209,13 +1025,14 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
 
 // MINB: resident blocks per SM the register allocation must allow
 template <int MINB, bool PK, bool MAGIC = false, int VU = 2, bool CPA = false, bool ABS = false,
-          bool MAPQ = false, bool BULK = false>
+          bool MAPQ = false, bool BULK = false, int R = kSmRows>
 __global__ void __launch_bounds__(256, MINB)
     k_bwd2d_smem(float *__restrict__ vol, const float2 *__restrict__ S,
                  const float4 *__restrict__ proj, int W, int H, int det, int nangles, float sx,
                  float sy, float ox, float oy, float ds) {
-    bwd2d_smem_tile<PK, MAGIC, VU, CPA, ABS, MAPQ, BULK>(vol, S, proj, W, H, det, nangles, sx,
-                                                         sy, ox, oy, ds, blockIdx.x, blockIdx.y);
+    bwd2d_smem_tile<PK, MAGIC, VU, CPA, ABS, MAPQ, BULK, R>(vol, S, proj, W, H, det, nangles,
+                                                            sx, sy, ox, oy, ds, blockIdx.x,
+                                                            blockIdx.y);
 }
 
 }  // namespace
@@ -1349,30 +1166,46 @@ int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s) {
     return CG_OK;
 }
 
-int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s, int rows) {
-    // pixel rows [0, rows): whole tiles of 8 * kSmRows rows, or all of H
-    if (rows < 0) rows = p.H;
-    if (rows <= 0) return CG_OK;
-    dim3 grid(ceil_div(p.W, 32), ceil_div(rows, 8 * kSmRows));
+// Streaming multiprocessors of the current device (looked up once per device).
+static int sm_count() {
+    static int counts[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!counts[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+            n = 152;
+        counts[dev] = n;
+    }
+    return counts[dev];
+}
+
+int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s) {
+    // tiles of 32 x 64 pixels; an image whose tiles would not give every SM
+    // two blocks takes 32 x 16-pixel tiles (two pixels per thread) instead,
+    // four times the blocks, the same sums
+    const bool small = (long long)ceil_div(p.W, 32) * ceil_div(p.H, 8 * kSmRows) < 2LL * sm_count();
+    const dim3 grid(ceil_div(p.W, 32), ceil_div(p.H, 8 * (small ? 2 : kSmRows)));
     auto go = [&](auto kernel) {
         kernel<<<grid, dim3(32, 8), 0, s>>>(vol, p.d_sinoP, p.d_bproj, p.W, p.H, p.det,
                                             p.nangles, p.sx, p.sy, p.ox, p.oy, p.ds);
     };
+    // the default (68) and the autotuner's other candidates (48: the same
+    // staged pair by pair with cp.async; 27: (t, d) pairs, 32 x 1-pixel warps,
+    // view loop unrolled twice)
     switch (p.bwd_min_blocks) {
-        case 3: go(k_bwd2d_smem<3, false>); break;
-        case 4: go(k_bwd2d_smem<4, false>); break;
-        case 5: go(k_bwd2d_smem<5, false>); break;
-        case 14: go(k_bwd2d_smem<4, true>); break;
-        case 25: go(k_bwd2d_smem<4, true, true, 4>); break;
-        case 26: go(k_bwd2d_smem<4, true, true, 1>); break;
-        case 27: go(k_bwd2d_smem<4, true, true, 2, true>); break;
-        case 37: go(k_bwd2d_smem<4, true, true, 2, true, true>); break;
-        case 38: go(k_bwd2d_smem<4, true, true, 4, true, true>); break;
-        case 48: go(k_bwd2d_smem<4, true, true, 4, true, true, true>); break;
-        case 68: go(k_bwd2d_smem<4, true, true, 4, true, true, true, true>); break;
-        case 28: go(k_bwd2d_smem<4, true, true, 4, true>); break;
-        case 24: go(k_bwd2d_smem<4, true, true>); break;
-        default: go(k_bwd2d_smem<4, true, true, 4, true, true, true, true>); break;
+        case 27:
+            small ? go(k_bwd2d_smem<4, true, true, 2, true, false, false, false, 2>)
+                  : go(k_bwd2d_smem<4, true, true, 2, true>);
+            break;
+        case 48:
+            small ? go(k_bwd2d_smem<4, true, true, 4, true, true, true, false, 2>)
+                  : go(k_bwd2d_smem<4, true, true, 4, true, true, true>);
+            break;
+        default:
+            small ? go(k_bwd2d_smem<4, true, true, 4, true, true, true, true, 2>)
+                  : go(k_bwd2d_smem<4, true, true, 4, true, true, true, true>);
+            break;
     }
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;

@@ -124,6 +124,7 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+
 __global__ void k_relayout_sino3d(const float *__restrict__ sino, int U, int V, int nangles,
                                   float2 *__restrict__ S) {
     const int PU = U + 2 * kP3, PV = V + 2 * kP3;
@@ -273,13 +274,7 @@ __global__ void __launch_bounds__(256)
     sino[((size_t)view * V + iv) * U + iu] = acc;
 }
 
-// ------------------------------------------------------------ forward, slab
-
-constexpr int kS3Threads = 256;
-constexpr int kS3BU = 32, kS3BV = 8;  // detector cells per block
-constexpr int kS3G = 4;               // views per block
-constexpr int kS3K = 4;               // slices of marching per chunk
-constexpr int kS3MaxPairs = 5120;     // staged pairs per chunk (40 KB)
+// ------------------------------------------------------------ forward, quads
 
 // Ray set-up of forward_3d.hpp:56-81 (intersection.h:12-28) in the
 // reference's FP32 operations.
@@ -400,231 +395,6 @@ __global__ void __launch_bounds__(256)
         t = march_next(t, k, r.tmin, r.h, exact_t);
     }
     sino[((size_t)view * V + iv) * U + iu] = acc;
-}
-
-// Chunked slab forward.  Block = kS3G views x (32 x 8 detector cells) x ray
-// class (blockIdx.z & 1: 0 = rays stepping along z read volA, whose slices
-// are z planes; 1 = rays stepping along x read volB, slices x planes).  The
-// block marches its slice axis c in chunks of kS3K slices, in the direction
-// its rays advance.  For a chunk [kl, kl + kS3K) every sample of every ray
-// with c in that range is taken from shared memory: the window of pairs the
-// bundle can touch there is bounded by the bundle's 4 x kS3G corner rays
-// (each view's cells form a rectangle and the map from cell to the ray's
-// crossing of a c-plane is projective, so its extremes are at the corners;
-// the slope along a is clamped to [-1, 1], which every ray of the class
-// obeys) at the chunk's two bounding planes, plus one texel of margin; that
-// window of kS3K + 1 slices is copied in with 8-byte cp.async.  Each sample
-// is then four 8-byte shared loads (pairs along the contiguous axis a, rows
-// b, b+1, slices c, c+1) and seven FMA-lerps.  Samples are the reference's
-// float t-loop in order, so each ray's sum is accumulated in the same order.
-// A chunk whose window exceeds kS3MaxPairs (or a bundle with a view whose
-// corner rays do not all advance one way along c) samples the same layout
-// from global memory.
-__global__ void __launch_bounds__(kS3Threads, 3)
-    k_fwd3d_slab(const float2 *__restrict__ A, const float2 *__restrict__ B,
-                 float *__restrict__ sino, const float4 *__restrict__ torg,
-                 const float4 *__restrict__ tdu, const float4 *__restrict__ tdv,
-                 const float4 *__restrict__ tsrc, int X, int Y, int Z, int U, int V, int P) {
-    extern __shared__ __align__(16) float2 win[];  // kS3MaxPairs
-    __shared__ float s_cor[4 * kS3G][4];          // per corner: alpha_a, beta_a, alpha_b, beta_b
-    __shared__ int s_cor_ok, s_kmin, s_kmax, s_rpos, s_rneg;
-    __shared__ int s_wa0, s_wb0, s_Wa, s_Hb, s_use;
-
-    const int cls = blockIdx.z & 1;  // 1: c = x (volB)
-    const int g0 = (blockIdx.z >> 1) * kS3G;
-    const int ub0 = blockIdx.x * kS3BU, vb0 = blockIdx.y * kS3BV;
-    const int iu = ub0 + (threadIdx.x & (kS3BU - 1)), iv = vb0 + (threadIdx.x >> 5);
-    const float2 *L = cls ? B : A;
-    const int Na = cls ? Z : X, Nc = cls ? X : Z;
-    const int PA = Na + 2 * kP3, PB = Y + 2 * kP3;
-    const size_t slab_pairs = (size_t)PA * PB;
-
-    if (threadIdx.x == 0) {
-        s_cor_ok = 1, s_kmin = INT_MAX, s_kmax = INT_MIN;
-        s_rpos = 0, s_rneg = 0;
-    }
-    __syncthreads();
-
-    // ---- corner rays of the bundle (warp 0, one lane per corner)
-    if (threadIdx.x < 4 * kS3G) {
-        const int gi = threadIdx.x >> 2, c = threadIdx.x & 3;
-        const int view = min(g0 + gi, P - 1);
-        const int cu = (c & 1) ? min(ub0 + kS3BU - 1, U - 1) : ub0;
-        const int cv = (c & 2) ? min(vb0 + kS3BV - 1, V - 1) : vb0;
-        const Ray3 r = setup_ray3(torg[view], tdu[view], tdv[view], tsrc[view], cu, cv, X, Y, Z);
-        const float sa = cls ? r.sz : r.sx, da = cls ? r.dz : r.dx;
-        const float sc = cls ? r.sx : r.sz, dc = cls ? r.dx : r.dz;
-        // rays of this class have |da / dc| <= 1; per view the slopes are
-        // bounded by the corners' when dc keeps one sign over its cells
-        const unsigned pos = __ballot_sync(0xffffu, dc > 0.f) >> (threadIdx.x & ~3u) & 0xfu;
-        if (pos != 0u && pos != 0xfu) atomicAnd(&s_cor_ok, 0);
-        const float ba = fminf(fmaxf(da / dc, -1.f), 1.f), bb = r.dy / dc;
-        s_cor[threadIdx.x][0] = sa - sc * ba;
-        s_cor[threadIdx.x][1] = ba;
-        s_cor[threadIdx.x][2] = r.sy - sc * bb;
-        s_cor[threadIdx.x][3] = bb;
-    }
-
-    // ---- this thread's rays
-    float sa[kS3G], sb[kS3G], sc[kS3G], da[kS3G], db[kS3G], dc[kS3G];
-    float t[kS3G], tmax[kS3G], h[kS3G], acc[kS3G];
-    int left[kS3G];
-    int kmin = INT_MAX, kmax = INT_MIN;
-#pragma unroll
-    for (int g = 0; g < kS3G; ++g) {
-        left[g] = 0;
-        acc[g] = 0.f;
-        sa[g] = sb[g] = sc[g] = da[g] = db[g] = dc[g] = t[g] = tmax[g] = h[g] = 0.f;
-        const int view = g0 + g;
-        if (view >= P || iu >= U || iv >= V) continue;
-        const Ray3 r = setup_ray3(torg[view], tdu[view], tdv[view], tsrc[view], iu, iv, X, Y, Z);
-        if (!r.hit) continue;
-        const bool xmajor = fabsf(r.dx) > fabsf(r.dz);
-        if ((int)xmajor != cls) continue;
-        sa[g] = xmajor ? r.sz : r.sx, da[g] = xmajor ? r.dz : r.dx;
-        sc[g] = xmajor ? r.sx : r.sz, dc[g] = xmajor ? r.dx : r.dz;
-        sb[g] = r.sy, db[g] = r.dy;
-        t[g] = r.tmin, tmax[g] = r.tmax, h[g] = r.h;
-        left[g] = r.nsteps + 2;  // the float loop runs nsteps or nsteps + 1 times
-        const float c0 = fmaf(dc[g], r.tmin, sc[g]), c1 = fmaf(dc[g], r.tmax, sc[g]);
-        kmin = min(kmin, (int)floorf(fminf(c0, c1)));
-        kmax = max(kmax, (int)floorf(fmaxf(c0, c1)));
-        if (dc[g] > 0.f) s_rpos = 1; else s_rneg = 1;  // benign race: flags only
-    }
-    if (kmin <= kmax) {
-        atomicMin(&s_kmin, kmin);
-        atomicMax(&s_kmax, kmax);
-    }
-    __syncthreads();
-    const bool ok = s_cor_ok;
-    const int kall0 = max(s_kmin, -kP3), kall1 = min(s_kmax, Nc + 1);
-    const bool pass_pos = s_rpos, pass_neg = s_rneg;
-
-    // one pass per direction of advance along c (normally only one occurs)
-    for (int pass = 0; pass < 2; ++pass) {
-    const int dir = pass == 0 ? 1 : -1;
-    if ((dir > 0 && !pass_pos) || (dir < 0 && !pass_neg)) continue;
-    for (int step = 0; kall0 <= kall1; ++step) {
-        // chunk [kl, kl + kS3K) walked in the rays' direction
-        int kl;
-        if (dir > 0) {
-            kl = kall0 + step * kS3K;
-            if (kl > kall1) break;
-        } else {
-            const int kh = kall1 - step * kS3K;
-            if (kh < kall0) break;
-            kl = kh - kS3K + 1;
-        }
-        const float cl = (float)kl, ch = (float)(kl + kS3K);
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            // lane = corner (16) x bounding plane (2)
-            const int cidx = threadIdx.x >> 1;
-            const float cpl = (threadIdx.x & 1) ? ch : cl;
-            const float a = fmaf(s_cor[cidx][1], cpl, s_cor[cidx][0]);
-            const float b = fmaf(s_cor[cidx][3], cpl, s_cor[cidx][2]);
-            float amin = a, amax = a, bmin = b, bmax = b;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                amin = fminf(amin, __shfl_xor_sync(0xffffffffu, amin, o));
-                amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-                bmin = fminf(bmin, __shfl_xor_sync(0xffffffffu, bmin, o));
-                bmax = fmaxf(bmax, __shfl_xor_sync(0xffffffffu, bmax, o));
-            }
-            if (threadIdx.x == 0) {
-                int use = ok && amin > -1e6f && amax < 1e6f && bmin > -1e6f && bmax < 1e6f;
-                int wa0 = 0, wa1 = 0, wb0 = 0, wb1 = 0;
-                if (use) {
-                    // the layout holds pairs a in [-2, Na + 1] and rows b in
-                    // [-2, Y + 1]; samples on the far faces (a or b = N + 1)
-                    // read the zero padding there
-                    wa0 = max((int)floorf(amin) - 1, -kP3);
-                    wa1 = min((int)floorf(amax) + 1, Na + 1);
-                    wb0 = max((int)floorf(bmin) - 1, -kP3);
-                    wb1 = min((int)floorf(bmax) + 2, Y + 1);
-                    const long long pairs =
-                        (long long)(wa1 - wa0 + 1) * (wb1 - wb0 + 1) * (kS3K + 1);
-                    use = wa1 >= wa0 && wb1 >= wb0 && pairs <= kS3MaxPairs;
-                }
-                s_use = use, s_wa0 = wa0, s_wb0 = wb0;
-                s_Wa = wa1 - wa0 + 1, s_Hb = wb1 - wb0 + 1;
-            }
-        }
-        __syncthreads();
-        const int use = s_use;
-        const int wa0 = s_wa0, wb0 = s_wb0, Wa = s_Wa, Hb = s_Hb;
-        const int plane = Wa * Hb;
-        if (use) {
-            // one warp per staged row (slice, b), lanes along the row
-            const int rows = Hb * (kS3K + 1);
-            for (int row = threadIdx.x >> 5; row < rows; row += kS3Threads / 32) {
-                const int sl = row / Hb, rb = row - sl * Hb;
-                const int cc = min(max(kl + sl, -kP3), Nc + 1);
-                const float2 *src =
-                    L + ((size_t)(cc + kP3) * PB + (wb0 + rb + kP3)) * PA + (wa0 + kP3);
-                float2 *dst = win + row * Wa;
-                for (int ca = threadIdx.x & 31; ca < Wa; ca += 32) {
-                    const unsigned d = (unsigned)__cvta_generic_to_shared(dst + ca);
-                    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d),
-                                 "l"(src + ca));
-                }
-            }
-            asm volatile("cp.async.commit_group;\n" ::);
-            asm volatile("cp.async.wait_group 0;\n" ::);
-        }
-        __syncthreads();
-        const unsigned amaxw = (unsigned)(Wa - 1), bmaxw = (unsigned)(Hb - 2);
-#pragma unroll
-        for (int g = 0; g < kS3G; ++g) {
-            if ((dc[g] > 0.f) != (dir > 0)) continue;
-            while (left[g] > 0 && t[g] <= tmax[g]) {
-                const float pc = fmaf(dc[g], t[g], sc[g]);
-                if (pc >= ch || pc < cl) break;
-                const float pa = fmaf(da[g], t[g], sa[g]);
-                const float pb = fmaf(db[g], t[g], sb[g]);
-                const int ia = __float2int_rd(pa), ib = __float2int_rd(pb);
-                const int ic = __float2int_rd(pc);
-                const float wa = pa - (float)ia, wb = pb - (float)ib, wc = pc - (float)ic;
-                float2 q00, q10, q01, q11;
-                if (use) {
-                    // inside the window by construction; the clamps only guard
-                    // the far faces (zero padding) and rounding
-                    const unsigned wa_ = min((unsigned)(ia - wa0), amaxw);
-                    const unsigned wb_ = min((unsigned)(ib - wb0), bmaxw);
-                    const unsigned i0 = ((unsigned)(ic - kl) * Hb + wb_) * Wa + wa_;
-                    q00 = win[i0];
-                    q10 = win[i0 + Wa];
-                    q01 = win[i0 + plane];
-                    q11 = win[i0 + plane + Wa];
-                } else {
-                    const unsigned ca = min((unsigned)(ia + kP3), (unsigned)(Na + kP3));
-                    const unsigned cb = min((unsigned)(ib + kP3), (unsigned)(Y + kP3));
-                    const unsigned cs = min((unsigned)(ic + kP3), (unsigned)(Nc + kP3));
-                    const float2 *q = L + ((size_t)cs * PB + cb) * PA + ca;
-                    q00 = __ldg(q);
-                    q10 = __ldg(q + PA);
-                    q01 = __ldg(q + slab_pairs);
-                    q11 = __ldg(q + slab_pairs + PA);
-                }
-                const float l00 = fmaf(wa, q00.y, q00.x), l10 = fmaf(wa, q10.y, q10.x);
-                const float l01 = fmaf(wa, q01.y, q01.x), l11 = fmaf(wa, q11.y, q11.x);
-                const float m0 = fmaf(wb, l10 - l00, l00), m1 = fmaf(wb, l11 - l01, l01);
-                acc[g] += fmaf(wc, m1 - m0, m0);
-                t[g] += h[g];
-                --left[g];
-            }
-        }
-    }
-    }
-
-#pragma unroll
-    for (int g = 0; g < kS3G; ++g) {
-        const int view = g0 + g;
-        if (view >= P || iu >= U || iv >= V) continue;
-        const Ray3 r = setup_ray3(torg[view], tdu[view], tdv[view], tsrc[view], iu, iv, X, Y, Z);
-        if (!r.hit || (int)(fabsf(r.dx) > fabsf(r.dz)) != cls) continue;
-        sino[((size_t)view * V + iv) * U + iu] = acc[g];
-    }
 }
 
 // ------------------------------------------------------------ backward
@@ -952,7 +722,7 @@ int launch_forward3d(const Plan3d &p, const float *vol, float *sino, cudaStream_
 int launch_forward3d_quad(Plan3d &p, const float *vol, float *sino, cudaStream_t s) {
     const size_t n = (size_t)(p.X + kQP) * (p.Y + kQP) * (p.Z + kQP);
     // the kernel's offsets are 32-bit: larger volumes take the texture unit
-    if (n >= (1ull << 32)) return launch_forward3d_texture(p, vol, sino, s, true);
+    if (n >= (1ull << 32)) return launch_forward3d_tex(p, vol, sino, s);
     if (!p.d_volQA) {
         int rc = CG_OK;
         if (!try_malloc_or_oom((void **)&p.d_volQA, n * sizeof(float4), &rc) ||
@@ -969,7 +739,7 @@ int launch_forward3d_quad(Plan3d &p, const float *vol, float *sino, cudaStream_t
                 return launch_forward3d(p, vol, sino, s);
             }
             p.algo_fwd = 1;
-            return launch_forward3d_texture(p, vol, sino, s, true);
+            return launch_forward3d_tex(p, vol, sino, s);
         }
     }
     k_relayout3d_qa<<<ceil_div((long long)n, 256), 256, 0, s>>>(vol, p.X, p.Y, p.Z, p.d_volQA);
@@ -995,29 +765,6 @@ int launch_forward3d_quad(Plan3d &p, const float *vol, float *sino, cudaStream_t
     return CG_OK;
 }
 
-int launch_forward3d_slab(Plan3d &p, const float *vol, float *sino, cudaStream_t s) {
-    int rc = ensure_plan3d_scratch(p, true, false);
-    if (rc) return rc;
-    {
-        const long long n = (long long)p.volA_elems;
-        k_relayout3d_A<<<ceil_div(n, 256), 256, 0, s>>>(vol, p.X, p.Y, p.Z, p.d_volA);
-        CG_TRY_CUDA(cudaGetLastError());
-        dim3 g(ceil_div(p.X + 2 * kP3, 32), ceil_div(p.Z + 2 * kP3, 32), p.Y + 2 * kP3);
-        k_relayout3d_B<<<g, dim3(32, 8), 0, s>>>(vol, p.X, p.Y, p.Z, p.d_volB);
-        CG_TRY_CUDA(cudaGetLastError());
-    }
-    const size_t smem = sizeof(float2) * kS3MaxPairs;
-    const long long groups = ceil_div(p.nangles, kS3G);
-    if (2 * groups > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
-    dim3 grid(ceil_div(p.U, kS3BU), ceil_div(p.V, kS3BV), (unsigned)(2 * groups));
-    if (int rc = ensure_smem_attr((const void *)k_fwd3d_slab, (int)smem)) return rc;
-    k_fwd3d_slab<<<grid, kS3Threads, smem, s>>>(p.d_volA, p.d_volB, sino, p.d_forg, p.d_fdu,
-                                                p.d_fdv, p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V,
-                                                p.nangles);
-    CG_TRY_CUDA(cudaGetLastError());
-    return CG_OK;
-}
-
 int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream_t s) {
     const float zplane = p.DSO - p.DSD;
     const float hu = (float)(p.U / 2), hv = (float)(p.V / 2);
@@ -1026,15 +773,13 @@ int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream
         k_relayout_sino3d_qd<<<ceil_div(n, 256), 256, 0, s>>>(sino, p.U, p.V, p.nangles,
                                                               p.d_sinoQ);
         CG_TRY_CUDA(cudaGetLastError());
-        const int run = p.bwd_axial == 2 || p.bwd_axial == 3 ? 16 : 8;
+        constexpr int run = 8;
         const int tiles_x = ceil_div(p.X, 32), tiles_y = ceil_div(p.Y, run),
                   tiles_z = ceil_div(p.Z, 8);
         const int bricks = ceil_div(tiles_x, 2) * ceil_div(tiles_y, 8) * ceil_div(tiles_z, 8);
         const size_t plane = (size_t)(p.U + 2 * kP3) * (p.V + 2 * kP3);
-        auto kernel = p.bwd_axial == 0   ? k_bwd3d_ax<8, 5>
-                      : p.bwd_axial == 1 ? k_bwd3d_ax<8, 4>
-                      : p.bwd_axial == 2 ? k_bwd3d_ax<16, 3>
-                                         : k_bwd3d_ax<16, 4>;
+        // runs of 8 voxels at <= 48 registers (5 blocks per SM)
+        auto kernel = k_bwd3d_ax<run, 5>;
         // the view tables travel as a kernel parameter, kAxViews per launch
         AxViewParams tab{};
         for (int c0 = 0; c0 < p.nangles; c0 += kAxViews) {
@@ -1067,10 +812,8 @@ int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream
     }
     const int tiles_x = ceil_div(p.X, 32), tiles_y = ceil_div(p.Y, 8), tiles_z = ceil_div(p.Z, kBZ);
     const int bricks = ceil_div(tiles_x, 2) * ceil_div(tiles_y, 8) * ceil_div(tiles_z, 8);
-    auto kernel = quad                ? k_bwd3d<true, true, true>
-                  : p.bwd_packed == 2 ? k_bwd3d<true, true>
-                  : p.bwd_packed      ? k_bwd3d<true, false>
-                                      : k_bwd3d<false, false>;
+    // row-pair quads (default), or 8-byte pairs where the quads did not fit
+    auto kernel = quad ? k_bwd3d<true, true, true> : k_bwd3d<true, true>;
     kernel<<<bricks * 128, dim3(32, 8), 0, s>>>(
         vol, quad ? (const void *)p.d_sinoQ : (const void *)p.d_sinoP, p.d_borg, p.d_bdx,
         p.d_bdy, p.d_bdz, p.bsrc[0], p.bsrc[1], p.bsrc[2], zplane, hu, hv, p.X, p.Y, p.Z, p.U, p.V, p.nangles, tiles_x, tiles_y, tiles_z);

@@ -10,9 +10,6 @@
 //  k_fwd2d_tex    2D forward, tex2D on a 2D array refreshed per call
 //  k_bwd2d_tex    2D backprojection, tex1DLayered on the sinogram rows
 //  k_fwd3d_tex3   3D forward, tex3D (trilinear in the texture unit)
-//  k_fwd3d_tex2l  3D forward, two bilinear fetches from 2D layered arrays
-//                 (one array layered along z, one along x) and the lerp
-//                 across layers in FP32 registers
 #include <algorithm>
 #include <cfloat>
 #include <cstring>
@@ -135,91 +132,6 @@ __global__ void __launch_bounds__(256)
     fwd2d_tex_ray(q.tex, q.sino, q.src, q.u0, q.du, q.W, q.H, q.det, q.sx, q.sy, u, view);
 }
 
-// Warps whose (block, warp) index falls in the first `tex_eighths` of every
-// eight march through the texture unit, the others gather pair-packed texels
-// and filter in registers, so both the texture pipeline and the load/ALU
-// pipelines carry samples at once.  Ray set-up is shared.
-__global__ void __launch_bounds__(256)
-    k_fwd2d_hyb(cudaTextureObject_t tex, const float2 *__restrict__ layA,
-                const float2 *__restrict__ layB, float *__restrict__ sino,
-                const float2 *__restrict__ tsrc, const float2 *__restrict__ tu0,
-                const float2 *__restrict__ tdu, int W, int H, int det, int nangles, float sx,
-                float sy, int tex_eighths, int pa, int pb) {
-    const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    const int view = blockIdx.y * blockDim.y + threadIdx.y;
-    if (u >= det || view >= nangles) return;
-    const int warp = (threadIdx.y * blockDim.x + threadIdx.x) >> 5;
-    const bool use_tex = ((blockIdx.x + blockIdx.y * 3 + warp) & 7) < tex_eighths;
-    const float2 s = tsrc[view], o = tu0[view], du = tdu[view];
-    const float fu = (float)u;
-    const float dx = fmaf(du.x, fu, o.x);
-    const float dy = fmaf(du.y, fu, o.y);
-    float tmin = FLT_MIN, tmax = FLT_MAX;
-    {
-        const float t1 = __fdividef(-1.f - s.x, dx), t2 = __fdividef((float)W - s.x, dx);
-        tmin = fminf(fmaxf(t1, tmin), fmaxf(t2, tmin));
-        tmax = fmaxf(fminf(t1, tmax), fminf(t2, tmax));
-    }
-    {
-        const float t1 = __fdividef(-1.f - s.y, dy), t2 = __fdividef((float)H - s.y, dy);
-        tmin = fminf(fmaxf(t1, tmin), fmaxf(t2, tmin));
-        tmax = fmaxf(fminf(t1, tmax), fminf(t2, tmax));
-    }
-    float *out = sino + (size_t)view * det + u;
-    if ((double)tmin > (double)tmax - 1e-6) {
-        *out = 0.f;
-        return;
-    }
-    const float rox = fmaf(dx, tmin, s.x), roy = fmaf(dy, tmin, s.y);
-    const float tl = tmax - tmin;
-    const float rdx = dx * tl, rdy = dy * tl;
-    const float m = fmaxf(fabsf(rdx), fabsf(rdy));
-    int n = __float2int_rn(m);
-    const float vx = rdx / m, vy = rdy / m;
-    float acc;
-    if (use_tex) {
-        float x = rox, y = roy;
-        acc = 0.f;
-#pragma unroll 4
-        for (int j = 0; j < n; ++j) {
-            acc += tex2D<float>(tex, x, y);
-            x += vx;
-            y += vy;
-        }
-    } else {
-        const bool ymajor = fabsf(rdy) >= fabsf(rdx);
-        float p = (ymajor ? rox : roy) - 0.5f;
-        const float vp = ymajor ? vx : vy;
-        const float q = (ymajor ? roy : rox) - 0.5f;
-        const int sq = ((ymajor ? vy : vx) > 0.f) ? 1 : -1;
-        const float2 *lay = ymajor ? layA : layB;
-        const int pitch = ymajor ? pa : pb;
-        const float pmax = (float)(ymajor ? W : H);
-        const int qmax = ymajor ? H : W;
-        const float qf = floorf(q);
-        const float fq = q - qf;
-        const int iq = (int)fminf(fmaxf(qf, -(float)kPad), (float)qmax);
-        n = min(n, sq > 0 ? qmax - iq + 1 : iq + kPad + 1);
-        const float2 *row = lay + (size_t)(iq + kPad) * pitch + kPad;
-        const long long rstep = (long long)sq * pitch;
-        float acc_lo = 0.f, acc_hi = 0.f;
-#pragma unroll 4
-        for (int j = 0; j < n; ++j) {
-            const float pf = fminf(fmaxf(floorf(p), -(float)kPad), pmax);
-            const float fp = p - pf;
-            const int ip = (int)pf;
-            const float2 lo = __ldg(row + ip);
-            const float2 hi = __ldg(row + pitch + ip);
-            acc_lo += fmaf(fp, lo.y, lo.x);
-            acc_hi += fmaf(fp, hi.y, hi.x);
-            p += vp;
-            row += rstep;
-        }
-        acc = fmaf(fq, acc_hi - acc_lo, acc_lo);
-    }
-    *out = acc * hypotf(vx * sx, vy * sy);
-}
-
 // ------------------------------------------------------------ 2D backward
 
 constexpr int kTexBwdRows = 4;
@@ -337,56 +249,6 @@ __global__ void __launch_bounds__(256)
     sino[((size_t)view * V + iv) * U + iu] = acc;
 }
 
-// texA: layers z, texels (x, y);  texB: layers x, texels (z, y).
-__global__ void __launch_bounds__(256)
-    k_fwd3d_tex2l(cudaTextureObject_t texA, cudaTextureObject_t texB, float *__restrict__ sino,
-                  const float4 *__restrict__ torg, const float4 *__restrict__ tdu,
-                  const float4 *__restrict__ tdv, const float4 *__restrict__ tsrc, int X, int Y,
-                  int Z, int U, int V, int P) {
-    const int iu = blockIdx.x * blockDim.x + threadIdx.x;
-    const int iv = blockIdx.y * blockDim.y + threadIdx.y;
-    const int view = blockIdx.z * blockDim.z + threadIdx.z;
-    if (iu >= U || iv >= V || view >= P) return;
-    const RaySeg r = ray3d(torg[view], tdu[view], tdv[view], tsrc[view], iu, iv, X, Y, Z);
-    if (!r.hit) return;
-    // layered along the ray's dominant horizontal axis
-    const bool xmajor = fabsf(r.dx) > fabsf(r.dz);
-    const cudaTextureObject_t tex = xmajor ? texB : texA;
-    const float sa = xmajor ? r.sz : r.sx, da = xmajor ? r.dz : r.dx;
-    const float sc = xmajor ? r.sx : r.sz, dc = xmajor ? r.dx : r.dz;
-    const int nc = xmajor ? X : Z;
-    float acc = 0.f, t = r.tmin;
-    for (int k = 0; k <= r.nsteps + 1; ++k) {
-        if (!(t <= r.tmax)) break;
-        const float a = fmaf(da, t, sa) + 0.5f, b = fmaf(r.dy, t, r.sy) + 0.5f;
-        const float c = fmaf(dc, t, sc);
-        const float cf = floorf(c);
-        const float wc = c - cf;
-        const int ic = (int)cf;
-        const float v0 = (ic >= 0 && ic < nc) ? tex2DLayered<float>(tex, a, b, ic) : 0.f;
-        const float v1 = (ic + 1 >= 0 && ic + 1 < nc) ? tex2DLayered<float>(tex, a, b, ic + 1) : 0.f;
-        acc += fmaf(wc, v1 - v0, v0);
-        t += r.h;
-    }
-    sino[((size_t)view * V + iv) * U + iu] = acc;
-}
-
-// vol[z][y][x] -> out[x][y][z]
-__global__ void __launch_bounds__(256)
-    k_transpose_xz(const float *__restrict__ vol, float *__restrict__ out, int X, int Y, int Z) {
-    __shared__ float tile[32][33];
-    const int x0 = blockIdx.x * 32, z0 = blockIdx.y * 32, y = blockIdx.z;
-    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
-        const int z = z0 + j, x = x0 + threadIdx.x;
-        if (z < Z && x < X) tile[j][threadIdx.x] = vol[((size_t)z * Y + y) * X + x];
-    }
-    __syncthreads();
-    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
-        const int x = x0 + i, z = z0 + threadIdx.x;
-        if (x < X && z < Z) out[((size_t)x * Y + y) * Z + z] = tile[threadIdx.x][i];
-    }
-}
-
 }  // namespace
 
 // ------------------------------------------------------------ launchers
@@ -432,12 +294,14 @@ int ensure_vol_texture(Plan2d &p) {
 
 // Batched texture forward: each problem's volume into its plan's array, then
 // one launch over the work list (stage-1 starts: 32 x 8 cell-view tiles).
-int launch_batch2d_fwd_tex(const Prob2d *d_probs, const std::vector<Prob2d> &probs,
+int launch_batch2d_fwd_tex(const Prob2d *d_probs, const std::vector<Prob2d> &probs, int active,
                            const int *starts, int total, cudaStream_t s) {
-    for (const Prob2d &q : probs)
+    for (int i = 0; i < active; ++i) {
+        const Prob2d &q = probs[i];
         CG_TRY_CUDA(cudaMemcpy2DToArrayAsync(q.arr, 0, 0, q.vol, sizeof(float) * q.W,
                                              sizeof(float) * q.W, q.H, cudaMemcpyDeviceToDevice,
                                              s));
+    }
     k_batch_fwd2d_tex<<<total, dim3(32, 8), 0, s>>>(d_probs, starts, (int)probs.size());
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
@@ -451,21 +315,6 @@ int load_vol_texture(Plan2d &p, const float *vol, cudaStream_t s) {
     }
     CG_TRY_CUDA(cudaMemcpy2DToArrayAsync(p.arr_vol, 0, 0, vol, sizeof(float) * p.W,
                                          sizeof(float) * p.W, p.H, cudaMemcpyDeviceToDevice, s));
-    return CG_OK;
-}
-
-int launch_forward2d_hyb(Plan2d &p, const float *vol, float *sino, cudaStream_t s) {
-    int rc = load_vol_texture(p, vol, s);
-    if (rc) return rc;
-    rc = launch_relayout2d(p, vol, s);
-    if (rc) return rc;
-    dim3 block(p.fwd_bx, p.fwd_by);
-    dim3 grid(ceil_div(p.det, p.fwd_bx), ceil_div(p.nangles, p.fwd_by));
-    if (grid.y > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
-    k_fwd2d_hyb<<<grid, block, 0, s>>>(p.tex_vol, p.d_layA, p.d_layB, sino, p.d_src, p.d_u0,
-                                       p.d_du, p.W, p.H, p.det, p.nangles, p.sx, p.sy,
-                                       p.tex_eighths, p.pitchA(), p.pitchB());
-    CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }
 
@@ -489,26 +338,6 @@ int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t
     return CG_OK;
 }
 
-int load_sino_texture(Plan2d &p, const float *sino, cudaStream_t s) {
-    if (p.nangles > 2048) return set_error(CG_ERR_INVALID, "more views than one layered texture");
-    if (!p.arr_sino) {
-        int rc = alloc_array(&p.arr_sino, p.det, 0, p.nangles, cudaArrayLayered);
-        if (rc) return rc;
-        if ((rc = make_texture(p.arr_sino, &p.tex_sino))) return rc;
-    }
-    return copy_to_array(p.arr_sino, sino, p.det, 1, p.nangles, s);
-}
-
-// Pixel rows [y0, H) through the texture unit (the sinogram texture loaded).
-int launch_backward2d_tex_rows(const Plan2d &p, float *vol, int y0, cudaStream_t s) {
-    if (y0 >= p.H) return CG_OK;
-    dim3 grid(ceil_div(p.W, 32), ceil_div(p.H - y0, 32));
-    k_bwd2d_tex<<<grid, dim3(32, 8), 0, s>>>(vol, p.tex_sino, p.d_bmeta, p.W, p.H, p.det, 0,
-                                             p.nangles, p.sx, p.sy, p.ox, p.oy, p.ds, y0);
-    CG_TRY_CUDA(cudaGetLastError());
-    return CG_OK;
-}
-
 int upload_volume_texture3(Plan3d &p, const float *vol, cudaStream_t s) {
     if (!p.arr3) {
         int rc = alloc_array(&p.arr3, p.X, p.Y, p.Z, cudaArrayDefault);
@@ -519,43 +348,13 @@ int upload_volume_texture3(Plan3d &p, const float *vol, cudaStream_t s) {
 }
 
 int launch_forward3d_tex(Plan3d &p, const float *vol, float *sino, cudaStream_t s) {
-    return launch_forward3d_texture(p, vol, sino, s, p.algo_fwd == 1);
-}
-
-int launch_forward3d_texture(Plan3d &p, const float *vol, float *sino, cudaStream_t s,
-                             bool trilinear) {
     const dim3 block(p.fwd_bx, p.fwd_by, p.fwd_bz);
     const dim3 grid(ceil_div(p.U, p.fwd_bx), ceil_div(p.V, p.fwd_by), ceil_div(p.nangles, p.fwd_bz));
     if (grid.z > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
-    if (trilinear) {
-        if (!p.arr3) {
-            int rc = alloc_array(&p.arr3, p.X, p.Y, p.Z, cudaArrayDefault);
-            if (rc) return rc;
-            if ((rc = make_texture(p.arr3, &p.tex3))) return rc;
-        }
-        int rc = copy_to_array(p.arr3, vol, p.X, p.Y, p.Z, s);
-        if (rc) return rc;
-        k_fwd3d_tex3<<<grid, block, 0, s>>>(p.tex3, sino, p.d_forg, p.d_fdu, p.d_fdv, p.d_fsrc,
-                                            p.X, p.Y, p.Z, p.U, p.V, p.nangles, p.exact_t);
-        CG_TRY_CUDA(cudaGetLastError());
-        return CG_OK;
-    }
-    if (!p.arrA) {
-        int rc = alloc_array(&p.arrA, p.X, p.Y, p.Z, cudaArrayLayered);
-        if (rc) return rc;
-        if ((rc = make_texture(p.arrA, &p.texA))) return rc;
-        if ((rc = alloc_array(&p.arrB, p.Z, p.Y, p.X, cudaArrayLayered))) return rc;
-        if ((rc = make_texture(p.arrB, &p.texB))) return rc;
-        CG_TRY_CUDA(cudaMalloc(&p.d_volT, sizeof(float) * (size_t)p.X * p.Y * p.Z));
-    }
-    int rc = copy_to_array(p.arrA, vol, p.X, p.Y, p.Z, s);
+    int rc = upload_volume_texture3(p, vol, s);
     if (rc) return rc;
-    k_transpose_xz<<<dim3(ceil_div(p.X, 32), ceil_div(p.Z, 32), p.Y), dim3(32, 8), 0, s>>>(
-        vol, p.d_volT, p.X, p.Y, p.Z);
-    CG_TRY_CUDA(cudaGetLastError());
-    if ((rc = copy_to_array(p.arrB, p.d_volT, p.Z, p.Y, p.X, s))) return rc;
-    k_fwd3d_tex2l<<<grid, block, 0, s>>>(p.texA, p.texB, sino, p.d_forg, p.d_fdu, p.d_fdv,
-                                         p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V, p.nangles);
+    k_fwd3d_tex3<<<grid, block, 0, s>>>(p.tex3, sino, p.d_forg, p.d_fdu, p.d_fdv, p.d_fsrc, p.X,
+                                        p.Y, p.Z, p.U, p.V, p.nangles, p.exact_t);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }

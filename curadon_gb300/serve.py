@@ -12,6 +12,15 @@ slot has private scratch and the kernels are deterministic (CGLS's matched
 adjoint accumulates with atomics, so its results agree to rounding, within
 relative L2 1e-3).
 
+2D FBP and SIRT requests below 704^2 pixels are coalesced: requests of one
+geometry and kind that wait together run as one batch on a resident
+``Batch2d`` of that geometry class (up to ``batch_slots`` problems, one
+filter launch and one batched backprojection for FBP; for SIRT each
+iteration is one batched forward, one batched backprojection and three
+elementwise launches over all of them, captured once per batch size as a
+CUDA graph and replayed).  Batched results equal the single-request path bit
+for bit (the same kernels per problem).
+
 Latencies (submission to result on the host) and throughput are kept for
 ``stats()`` (p50 / p99 latency, solves per second).
 """
@@ -116,6 +125,100 @@ class _Slot:
         return r
 
 
+# 2D requests below this many pixels are coalesced into class batches (the
+# texture-unit forward's range, where single launches leave SMs idle)
+BATCH_PIXELS = 704 * 704
+
+
+def _batchable(req: Request) -> bool:
+    g = req.geom
+    return (req.kind in ("fbp", "sirt") and isinstance(g, FanGeometry)
+            and int(g.vol_shape[0]) * int(g.vol_shape[1]) < BATCH_PIXELS)
+
+
+def _class_key(req: Request) -> tuple:
+    return (req.kind, req.iters if req.kind == "sirt" else 0, req.filter_name,
+            _geom_key(req.geom))
+
+
+class _ClassBatch:
+    """``capacity`` resident problems of one 2D geometry and one kind: a
+    private plan per problem, stacked device buffers and bound batches.
+    ``run(ys, stream)`` solves len(ys) <= capacity requests at once."""
+
+    def __init__(self, req: Request, device: torch.device, capacity: int, lam: float = 1.0):
+        from .batch import Batch2d
+        from .fbp import _device_kernel
+
+        self.kind, self.iters, self.filter_name = req.kind, int(req.iters), req.filter_name
+        self.device, self.capacity = device, int(capacity)
+        self.busy = False
+        K = self.capacity
+        g0 = req.geom
+        self.geoms = [_clone_geom(g0, device.index or 0) for _ in range(K)]
+        H, W = (int(v) for v in g0.vol_shape)
+        V, D = g0.sinogram_shape()
+        self.nangles = V
+        self.Y = torch.zeros((K, V, D), device=device)
+        self.S = torch.zeros_like(self.Y)
+        self.X = torch.zeros((K, H, W), device=device)
+        if self.kind == "fbp":
+            self.h = _device_kernel(D, self.filter_name, 1.0, device)
+            self.bb = Batch2d(self.geoms, list(self.X), list(self.S))
+        else:
+            self.BP = torch.zeros_like(self.X)
+            self.bf = Batch2d(self.geoms, list(self.X), list(self.S), forward="texture")
+            self.bb = Batch2d(self.geoms, list(self.BP), list(self.S))
+            # SIRT row / column normalisations, the same for every problem
+            solver = SirtSolver(self.geoms[0], device, lam=lam)
+            self.R, self.C = solver.R, solver.C
+            self.graphs: Dict[int, torch.cuda.CUDAGraph] = {}
+        self.bytes = 4 * (self.Y.numel() * 2 + self.X.numel() * (1 if self.kind == "fbp" else 2))
+
+    def _sirt_iteration(self, m: int):
+        X, S, BP = self.X[:m], self.S[:m], self.BP[:m]
+        self.bf.forward()
+        torch.sub(self.Y[:m], S, out=S)
+        S.mul_(self.R)
+        BP.zero_()
+        self.bb.backward()
+        X.addcmul_(self.C, BP)
+        X.clamp_(min=0.0)
+
+    def run(self, ys: List[torch.Tensor], stream) -> torch.Tensor:
+        """Enqueues the solves of ``ys`` (host or device sinograms) on the
+        current stream; returns the stacked device results (a view)."""
+        from .fbp import filter_sinogram
+
+        m = len(ys)
+        for i, y in enumerate(ys):
+            self.Y[i].copy_(y, non_blocking=True)
+        if self.kind == "fbp":
+            filter_sinogram(self.Y[:m], self.filter_name, 1.0, np.pi / (2 * self.nangles),
+                            out=self.S[:m])
+            self.X[:m].zero_()
+            self.bb.set_active(m)
+            self.bb.backward()
+            return self.X[:m]
+        self.bf.set_active(m)
+        self.bb.set_active(m)
+        self.X[:m].zero_()
+        g = self.graphs.get(m)
+        if g is None:
+            # one iteration captured on this stream without a device-wide
+            # synchronisation (other requests keep running meanwhile)
+            g = torch.cuda.CUDAGraph()
+            g.capture_begin(capture_error_mode="thread_local")
+            try:
+                self._sirt_iteration(m)
+            finally:
+                g.capture_end()
+            self.graphs[m] = g
+        for _ in range(self.iters):
+            g.replay()
+        return self.X[:m]
+
+
 def _execute(slot: _Slot, req: Request) -> torch.Tensor:
     """Enqueues the request on the slot's stream; returns the device result."""
     g, solver = slot.resource(req.kind, req.geom)
@@ -138,9 +241,15 @@ def solve_alone(req: Request, device=0) -> torch.Tensor:
 
 class Server:
     def __init__(self, device: int = 0, slots: int = 8, hbm_budget: float = 150e9,
-                 max_resident: int = 16):
+                 max_resident: int = 16, batching: bool = True, batch_slots: int = 16,
+                 max_class_batches: int = 32):
         self.device = torch.device("cuda", device)
         torch.cuda.init()
+        self.batching = bool(batching)
+        self.batch_slots = int(batch_slots)
+        self.max_class_batches = int(max_class_batches)
+        self._classes: "collections.OrderedDict[tuple, _ClassBatch]" = collections.OrderedDict()
+        self.batches_run = 0
         self.slots = [_Slot(self.device, max_resident) for _ in range(slots)]
         self.free = list(range(slots))
         self.budget = float(hbm_budget)
@@ -183,19 +292,54 @@ class Server:
 
     # ---------------------------------------------------------- GPU thread
     def _next(self):
-        """The next request that fits a free slot and the memory budget, or
-        None; the queue is served in arrival order."""
+        """The next work that fits a free slot and the memory budget, or None:
+        the oldest waiting request, with -- when it is a batchable 2D request
+        whose class batch is idle -- every later waiting request of its class,
+        up to the batch's size and the budget.  Returns (items, need, class
+        key or None) with items a list of (request, future)."""
         with self._cv:
             if not self._pending or not self.free:
                 return None
-            req, fut = self._pending[0]
-            need = request_bytes(req)
-            if self._inflight and self.inflight_bytes + need > self.budget:
-                return None
-            if self._inflight and torch.cuda.mem_get_info(self.device)[0] < need:
-                return None
-            self._pending.popleft()
-            return req, fut, need
+            for idx, (req, fut) in enumerate(self._pending):
+                key = _class_key(req) if self.batching and _batchable(req) else None
+                cb = self._classes.get(key) if key is not None else None
+                if cb is not None and cb.busy:
+                    continue  # its class batch is in flight; later requests may go
+                need = request_bytes(req)
+                if self._inflight and self.inflight_bytes + need > self.budget:
+                    return None
+                if self._inflight and torch.cuda.mem_get_info(self.device)[0] < need:
+                    return None
+                items = [(req, fut)]
+                taken = [idx]
+                if key is not None:
+                    for j in range(idx + 1, len(self._pending)):
+                        if len(items) >= self.batch_slots:
+                            break
+                        r2, f2 = self._pending[j]
+                        if _batchable(r2) and _class_key(r2) == key:
+                            n2 = request_bytes(r2)
+                            if self.inflight_bytes + need + n2 > self.budget:
+                                break
+                            items.append((r2, f2))
+                            taken.append(j)
+                            need += n2
+                for j in reversed(taken):
+                    del self._pending[j]
+                return items, need, key
+            return None
+
+    def _class_batch(self, key, req: Request) -> _ClassBatch:
+        cb = self._classes.get(key)
+        if cb is None:
+            cb = _ClassBatch(req, self.device, self.batch_slots)
+            self._classes[key] = cb
+            while len(self._classes) > self.max_class_batches:
+                old_key = next(k for k, v in self._classes.items() if not v.busy)
+                del self._classes[old_key]
+        else:
+            self._classes.move_to_end(key)
+        return cb
 
     def _admit(self) -> bool:
         progressed = False
@@ -203,22 +347,36 @@ class Server:
             nxt = self._next()
             if nxt is None:
                 break
-            req, fut, need = nxt
+            items, need, key = nxt
             k = self.free.pop()
             slot = self.slots[k]
+            cb = None
             try:
                 with torch.cuda.stream(slot.stream):
-                    out = _execute(slot, req)
-                    host = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
-                    host.copy_(out, non_blocking=True)
+                    if key is None:
+                        outs = [_execute(slot, items[0][0])]
+                    else:
+                        cb = self._class_batch(key, items[0][0])
+                        cb.busy = True
+                        stacked = cb.run([r.sinogram for r, _ in items], slot.stream)
+                        outs = list(stacked)
+                        self.batches_run += 1
+                    hosts = []
+                    for out in outs:
+                        host = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
+                        host.copy_(out, non_blocking=True)
+                        hosts.append(host)
                     ev = torch.cuda.Event()
                     ev.record(slot.stream)
-            except Exception as e:  # a bad request fails alone
+            except Exception as e:  # a bad request fails alone (with its batch)
                 self.free.append(k)
-                fut.set_exception(e)
+                if cb is not None:
+                    cb.busy = False
+                for _, fut in items:
+                    fut.set_exception(e)
                 continue
             self.inflight_bytes += need
-            self._inflight.append((req, fut, k, ev, host, need))
+            self._inflight.append((items, k, ev, hosts, need, cb))
             progressed = True
         return progressed
 
@@ -226,17 +384,20 @@ class Server:
         progressed = False
         still = []
         for item in self._inflight:
-            req, fut, k, ev, host, need = item
+            items, k, ev, hosts, need, cb = item
             if ev.query():
                 now = time.perf_counter()
                 self.free.append(k)
                 self.inflight_bytes -= need
-                self.latencies.append(now - req.t_submit)
-                self.completed += 1
-                if self.t_first is None:
-                    self.t_first = req.t_submit
+                if cb is not None:
+                    cb.busy = False
+                for (req, fut), host in zip(items, hosts):
+                    self.latencies.append(now - req.t_submit)
+                    self.completed += 1
+                    if self.t_first is None or req.t_submit < self.t_first:
+                        self.t_first = req.t_submit
+                    fut.set_result(host)
                 self.t_last = now
-                fut.set_result(host)
                 progressed = True
             else:
                 still.append(item)

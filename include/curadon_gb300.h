@@ -144,8 +144,8 @@ int cg_plan2d_tables(const cg_plan2d *plan, float *sources, float *u_origins, fl
 int cg_forward_2d(cg_plan2d *plan, const float *volume, float *sinogram, void *stream);
 
 /* 2D voxel-driven backprojection, accumulating into `volume`.  Replaces
- * `backward_2d(volume, sinogram, plan)` (backward.cu:233-280 ->
- * bp::backproject_2d, backward_2d.hpp:302-306) for a float32 sinogram. */
+ * `backward_2d(volume, sinogram, plan)` (backward.cu:89-133 ->
+ * bp::backproject_2d, backward_2d.hpp:162-166) for a float32 sinogram. */
 int cg_backward_2d(cg_plan2d *plan, float *volume, const float *sinogram, void *stream);
 
 /* The same two operators with the sinogram's element type given: sino_bits
@@ -210,7 +210,7 @@ int cg_plan3d_get_algorithm(const cg_plan3d *plan, int *forward, int *backward);
 int cg_forward_3d_plan(cg_plan3d *plan, const float *volume, float *sinogram, void *stream);
 
 /* 3D voxel-driven backprojection with a plan, accumulating
- * (bp::backproject_3d, backward_3d.hpp:457-529). */
+ * (bp::backproject_3d, backward_3d.hpp:181-253). */
 int cg_backward_3d_plan(cg_plan3d *plan, float *volume, const float *sinogram, void *stream);
 
 /* Matched adjoint of cg_forward_3d_plan, accumulating into `volume`; rays
@@ -300,6 +300,11 @@ int cg_batch2d_backward(cg_batch2d *batch, void *stream);
  * stream capture).  No counterpart in the reference, whose gradient is its
  * backprojector (python/standalone/src/curadon/diffable.py:14-38). */
 int cg_batch2d_adjoint(cg_batch2d *batch, void *stream);
+/* Later forward / backward / adjoint calls run only problems [0, active)
+ * of the batch (1 <= active <= count; all of them after creation): a
+ * resident batch of `count` slots serves however many requests are waiting
+ * without being rebuilt. */
+int cg_batch2d_set_active(cg_batch2d *batch, int active);
 /* the batched forward's algorithm: 1 texture unit (default), 0 registers */
 int cg_batch2d_set_forward(cg_batch2d *batch, int algorithm);
 int cg_batch2d_get_forward(const cg_batch2d *batch, int *algorithm);

@@ -5,8 +5,9 @@ nanobind extension that cannot be built here (nanobind is not installed).
 ``ref_shim.cu`` repeats that extension's marshaling over the library and is
 compiled with nvcc for sm_103a against the reference headers:
 
-* where the reference tree exists (``CURADON_REF_ROOT``, default
-  ``/root/reference``), the headers are used where they lie, and they are also
+* where the reference tree exists (``CURADON_REF_ROOT``; unset, a checkout
+  named ``reference`` beside this repository), the headers are used where
+  they lie, and they are also
   staged, unmodified, into the git-ignored ``oracle/_ref/include`` -- the
   install step of a header-only library -- so that a machine without the
   reference tree can still compile the shim;
@@ -31,7 +32,8 @@ SHIM = ORACLE_DIR / "ref_shim.cu"
 
 
 def reference_include() -> Path | None:
-    root = Path(os.environ.get("CURADON_REF_ROOT", "/root/reference"))
+    env = os.environ.get("CURADON_REF_ROOT")
+    root = Path(env) if env else ORACLE_DIR.parent.parent / "reference"
     inc = root / "include"
     if (inc / "curadon" / "forward.hpp").exists():
         return inc

@@ -9,10 +9,10 @@
 // does before it calls the library (python/standalone/src/):
 //   ref_plan2d_create  <- plan.cu:34-56   (axis swap, thrust vectors)
 //   ref_forward2d      <- forward.cu:77-90 (spans {W,H}, {det, nangles})
-//   ref_backward2d     <- backward.cu:218-231
+//   ref_backward2d     <- backward.cu:75-87
 //   ref_forward2d_t / ref_backward2d_t  <- the f16 instantiations of both
 //   ref_forward3d      <- forward.cu:23-75 (axis swaps, psi/phi naming swap)
-//   ref_backward3d     <- backward.cu:164-216
+//   ref_backward3d     <- backward.cu:20-72
 #include <cstdint>
 #include <vector>
 

@@ -93,9 +93,9 @@ def test_matched_gradient_finite_differences(cuda_device):
     assert abs(fd - an) / abs(fd) < 1e-3
 
 
-@pytest.mark.parametrize("algo", ["registers", "slab", "chunked"])
+@pytest.mark.parametrize("algo", ["registers", "chunked"])
 def test_dot_product_2d_per_forward_algorithm(cuda_device, algo):
-    """The FP32-weight forwards (registers, slab, chunked) share the adjoint."""
+    """The FP32-weight forwards (registers, chunked) share the adjoint."""
     g = fan_config(200, 150)
     geom = FanGeometry(**g)
     geom.exact_plan.set_algorithm(forward=algo)
@@ -105,9 +105,9 @@ def test_dot_product_2d_per_forward_algorithm(cuda_device, algo):
     assert dot_test(geom, x, y, cuda_device) < 1e-5
 
 
-@pytest.mark.parametrize("algo", ["registers", "slab", "quad"])
+@pytest.mark.parametrize("algo", ["registers", "quad"])
 def test_dot_product_3d_per_forward_algorithm(cuda_device, algo):
-    """The FP32-weight 3D forwards (registers, slab, quad) share the adjoint."""
+    """The FP32-weight 3D forwards (registers, quad) share the adjoint."""
     g = cone_config(40, 36, 64)
     geom = ConeGeometry(**g)
     geom.exact_plan.set_algorithm(forward=algo)
@@ -147,10 +147,12 @@ def test_adjoint_accumulates(cuda_device):
 
 @pytest.mark.parametrize("variant", ["adj3d_merge=1", "adj3d_order=band",
                                      "adj3d_order=band,adj3d_merge=1",
-                                     "adj3d=pair,adj3d_order=band", "adj3d=pair"])
+                                     "adj3d=pair,adj3d_order=band", "adj3d=pair",
+                                     "adj3d_agg=1", "adj3d_agg=1,adj3d_order=band"])
 def test_dot_product_3d_scatter_variants(cuda_device, monkeypatch, variant):
     """Every shape of the 3D scatter (accumulators, block order, merged slice
-    atomics; CURADON_GB300_ALGO) is the transpose of the quad forward."""
+    atomics, warp-aggregated atomics; CURADON_GB300_ALGO) is the transpose of
+    the quad forward."""
     g = cone_config(40, 36, 64)
     monkeypatch.setenv("CURADON_GB300_ALGO", variant)
     geom = ConeGeometry(**g)

@@ -216,7 +216,7 @@ def test_batch_unrolled_gradient_descent_graph_equals_eager(cuda_device):
     for _ in range(6):
         with torch.no_grad():
             w = proj.adjoint(proj(v))
-        v = torch.cat([t / t.norm() for t in proj.split_volumes(w)])
+        v = torch.cat([(t / t.norm()).reshape(-1) for t in proj.split_volumes(w)])
     with torch.no_grad():
         av = proj(v)
     steps = torch.cat([torch.full((int(np.prod(s)),), 1.0 / float(a.norm() ** 2), device=cuda_device)

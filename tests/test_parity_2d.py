@@ -95,10 +95,6 @@ def test_backward_algorithms(cuda_device, algo, n, nangles):
     the layered texture's 2048 views."""
     g = fan_config(n, nangles)
     geom = make(g, cuda_device)
-    if algo == "split" and nangles > 2048:
-        with pytest.raises(ValueError, match="2048"):
-            geom.plan.set_algorithm(backward=algo)
-        return
     geom.plan.set_algorithm(backward=algo)
     rng = np.random.default_rng(n + nangles)
     sino = rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32)
@@ -251,74 +247,11 @@ def test_algorithm_override_variable(cuda_device):
     assert "('registers', 'texture')" in out.stdout, out.stdout
 
 
-@pytest.mark.parametrize("k", [0, 3, 16])
-def test_split_forward_shares_and_graph(cuda_device, monkeypatch, k):
-    """The split forward (k sixteenths of the views on the texture unit, on an
-    internal stream forked from the caller's) equals the oracle for every
-    share and is capturable in a CUDA graph: a replay equals a direct call."""
-    n, nangles = 160, 90
-    g = fan_config(n, nangles)
-    monkeypatch.setenv("CURADON_GB300_ALGO", f"fwd2d=split{k}")
-    geom = FanGeometry(**g, device=cuda_device.index or 0)
-    assert geom.plan.algorithm[0] == "split"
-    monkeypatch.delenv("CURADON_GB300_ALGO")
-    v = ellipses_2d(n, 3, device=cuda_device).contiguous()
-    s = torch.zeros(geom.sinogram_shape(), device=cuda_device)
-    forward(v, s, geom)
-    torch.cuda.synchronize()
-    so = oracle.fwd2d(g, v.cpu().numpy())
-    assert rel_l2(s.cpu().numpy(), so) < TOL
-    out = torch.zeros_like(s)
-    graph = torch.cuda.CUDAGraph()
-    st = torch.cuda.Stream()
-    st.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(st), torch.cuda.graph(graph, stream=st):
-        forward(v, out, geom)
-    torch.cuda.current_stream().wait_stream(st)
-    out.zero_()
-    graph.replay()
-    torch.cuda.synchronize()
-    assert torch.equal(out, s)
-
-
-@pytest.mark.parametrize("k", [0, 5, 16])
-def test_split_backward_shares_and_graph(cuda_device, monkeypatch, k):
-    """The split backprojection (k sixteenths of the pixel rows on the texture
-    unit, on an internal stream) equals the oracle for every share, adds into
-    the volume, and replays from a CUDA graph like a direct call."""
-    n, nangles = 200, 120
-    g = fan_config(n, nangles)
-    monkeypatch.setenv("CURADON_GB300_ALGO", f"bwd2d=split{k}")
-    geom = FanGeometry(**g, device=cuda_device.index or 0)
-    assert geom.plan.algorithm[1] == "split"
-    monkeypatch.delenv("CURADON_GB300_ALGO")
-    rng = np.random.default_rng(k)
-    sino = torch.as_tensor(rng.uniform(0, 1, geom.sinogram_shape()).astype(np.float32),
-                           device=cuda_device)
-    v0 = torch.as_tensor(rng.uniform(0, 1, (n, n)).astype(np.float32), device=cuda_device)
-    b = v0.clone()
-    backward(sino, b, geom)
-    torch.cuda.synchronize()
-    e = rel_l2((b - v0).cpu().numpy(), oracle.bwd2d(g, sino.cpu().numpy()))
-    assert e < TOL, e
-    out = v0.clone()
-    graph = torch.cuda.CUDAGraph()
-    st = torch.cuda.Stream()
-    st.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(st), torch.cuda.graph(graph, stream=st):
-        backward(sino, out, geom)
-    torch.cuda.current_stream().wait_stream(st)
-    out.copy_(v0)
-    graph.replay()
-    torch.cuda.synchronize()
-    assert torch.equal(out, b)
-
-
-@pytest.mark.parametrize("shape", [3, 4, 5, 14, 24, 25, 26, 27, 28, 37, 38, 48, 68])
+@pytest.mark.parametrize("shape", [27, 48, 68])
 def test_staged_backprojector_shapes(cuda_device, monkeypatch, shape):
-    """Every compiled shape of the staged backprojector (CURADON_GB300_ALGO
-    bwd2d_minb=...: blocks per SM, packed rows, floor by FP32 adds, view-loop
-    unrolling, asynchronous window copies) against the oracle."""
+    """Every compiled variant of the staged backprojector (CURADON_GB300_ALGO
+    bwd2d_minb=...: the default and the autotuner's other candidates)
+    against the oracle."""
     n, nangles = 256, 150
     g = fan_config(n, nangles)
     monkeypatch.setenv("CURADON_GB300_ALGO", f"bwd2d=smem,bwd2d_minb={shape}")
@@ -333,14 +266,12 @@ def test_staged_backprojector_shapes(cuda_device, monkeypatch, shape):
     assert e < TOL
 
 
-@pytest.mark.parametrize("shape", [4, 104, 108, 204, 304, 308, 404, 408, 414, 418, 428, 438,
-                                   439, 440, 441, 442, 443, 444, 447, 448, 449, 450, 451, 453,
-                                   463, 473, 474, 484])
+@pytest.mark.parametrize("shape", [443, 474, 484])
 def test_chunked_forward_shapes(cuda_device, monkeypatch, shape):
     """Every compiled shape of the chunked forward (CURADON_GB300_ALGO
-    fwd2d=cslab<shape>: rows per chunk, bundle width, packed sums, pair reuse,
-    one or two threads per cell) against the oracle, on a wide detector whose
-    bundles hold rays of both stepping classes."""
+    fwd2d=cslab<shape>: the default and the autotuner's other candidates)
+    against the oracle, on a wide detector whose bundles hold rays of both
+    stepping classes."""
     n, nangles, det = 190, 77, 600
     g = fan_config(n, nangles, det)
     monkeypatch.setenv("CURADON_GB300_ALGO", f"fwd2d=cslab{shape}")

@@ -110,3 +110,24 @@ def test_admission_respects_the_memory_budget(cuda_device):
         f.result(timeout=60)
     srv.close()
     assert max(peak) == 1
+
+
+def test_waiting_2d_requests_are_coalesced(cuda_device):
+    """Requests of one 2D geometry and kind that wait together run as one
+    class batch (one batched backprojection for FBP, graph-replayed batched
+    SIRT iterations), with each result equal to the request solved alone."""
+    reqs = ([fan_request("fbp", 160, 120, 20 + k, cuda_device) for k in range(5)] +
+            [fan_request("sirt", 96, 90, 30 + k, cuda_device, iters=6) for k in range(5)])
+    alone = [solve_alone(r, cuda_device.index or 0).cpu() for r in reqs]
+    srv = Server(device=cuda_device.index or 0, slots=1)
+    # hold the only slot busy so that every request is waiting when admission runs
+    blocker = fan_request("sirt", 256, 256, 40, cuda_device, iters=40)
+    fb = srv.submit(blocker)
+    futs = [srv.submit(r) for r in reqs]
+    outs = [f.result(timeout=120) for f in futs]
+    fb.result(timeout=120)
+    srv.close()
+    print(f"batches run: {srv.batches_run} for {len(reqs)} requests")
+    assert srv.batches_run < len(reqs)
+    for i, (out, ref) in enumerate(zip(outs, alone)):
+        assert torch.equal(out, ref), i
