@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--sweep-sizes", default="64,128,256,512,1024,2048",
                    help="image sizes of --workload sweep")
+    p.add_argument("--cone-views", type=int, default=0,
+                   help="views of the cone workloads (default: 360 at 256^3, 720 at 512^3)")
     p.add_argument("--serve-requests", type=int, default=400,
                    help="requests of --workload serve")
     p.add_argument("--serve-rate", type=float, default=200.0,
@@ -75,6 +77,11 @@ def parse():
 
 
 # ------------------------------------------------------------ workloads
+
+# view count of the cone workloads when --cone-views overrides it (smaller
+# profiling captures of the same volume); 0 = the workload's own
+CONE_VIEWS = 0
+
 
 def workload(name: str):
     from curadon_gb300.phantom import cone_config, fan_config, seed_for
@@ -91,6 +98,8 @@ def workload(name: str):
     if name in ("cone256", "cone512"):
         n = int(name[4:])
         nangles, det = (360, 384) if n == 256 else (720, 768)
+        if CONE_VIEWS:
+            nangles = CONE_VIEWS
         g = cone_config(n, nangles, det)
         return dict(kind="cone", name=name, n=n, geom=g, seed=seed_for(2, n),
                     desc=f"3D cone-beam {n}^3 forward+backprojection",
@@ -1146,7 +1155,9 @@ def run_batch(args):
 
 
 def main():
+    global CONE_VIEWS
     args = parse()
+    CONE_VIEWS = args.cone_views
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
