@@ -383,9 +383,9 @@ def roofline_of(wl, ms_fwd, ms_bwd, algos, peaks):
         s_fwd = cone_sample_count(g)
         gather = {"forward": 32, "backward": 16}
         note = (f"gather-bound (L1 load and texture pipes), not HBM-bound: the {nvox * 4 >> 20} "
-                "MiB volume is read once per call and each block's working set (a band of "
-                "detector rows across many views) stays in L2; samples_per_s is the "
-                "efficiency figure")
+                "MiB volume's quad copies are re-read from L2 per sample; from 512^3 the "
+                "resident blocks' working set exceeds L2 (89 % L2 hit) but DRAM runs at a few "
+                "percent of its peak; samples_per_s is the efficiency figure")
     s_bwd = nvox * len(g["angles"])
     b_alg = {"forward": 4 * (nvox + nrays), "backward": 4 * (nrays + 2 * nvox)}
     dom = "forward" if ms_fwd >= ms_bwd else "backward"

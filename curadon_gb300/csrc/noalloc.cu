@@ -120,8 +120,8 @@ extern "C" int cg_backward_2d_static(float *volume, const float *sinogram,
     p.d_sinoP = reinterpret_cast<float2 *>(b + off_sino);
     apply_algo_env(&p, nullptr);
     // Only the register backprojector (0) and the staged one (2) run on this
-    // scratch alone; the texture-unit and split algorithms would allocate
-    // arrays, so an override selecting them falls back to the staged kernel.
+    // scratch alone; the texture-unit algorithm would allocate
+    // arrays, so an override selecting it falls back to the staged kernel.
     if (p.algo_bwd != 0) p.algo_bwd = 2;
 
     cudaStream_t s = (cudaStream_t)stream;
