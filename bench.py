@@ -69,7 +69,7 @@ def parse():
                    help="Poisson arrival rate of --workload serve (per second)")
     p.add_argument("--no-reference-gpu", action="store_true",
                    help="skip the reference's own CUDA operators beside ours (default run)")
-    p.add_argument("--batch-forward", default="texture", choices=["texture", "registers"],
+    p.add_argument("--batch-forward", default="plans", choices=["plans", "texture", "registers"],
                    help="forward algorithm of the batch workload")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="CPU work budget of the cpu_baseline sample")
@@ -987,6 +987,18 @@ def batch_problems(dev, count: int = 64):
     return out
 
 
+def fwd_kernels(algo: str, sizes) -> int:
+    """Kernels of one batched forward: the texture march 1 (plus array
+    copies); the register march 2 (re-layout, rays); each plan's own 1 for
+    the texture problems and 2 (re-layout, bundles) for the chunked ones."""
+    if algo == "texture":
+        return 1
+    if algo == "registers":
+        return 2
+    big = [n * n >= 704 * 704 for n in sizes]
+    return (1 if not all(big) else 0) + (2 if any(big) else 0)
+
+
 def run_batch(args):
     """The batched, differentiable workload: 10 unrolled gradient-descent steps
     x <- x - a grad 1/2 ||A x - y||^2 over all 64 problems, each step through
@@ -1137,7 +1149,8 @@ def run_batch(args):
                                "10 unrolled iterations x - a grad 1/2||Ax - y||^2 through "
                                "torch.autograd over all problems, one iteration graph-captured",
                    "l2": "the working set (0.3-1 GB) exceeds L2", "parallelism": "one GPU"},
-        "gpu_launches": (2 + (1 if proj._fwd.forward_algorithm == "texture" else 2)) * iters * steps,
+        "gpu_launches": (2 + fwd_kernels(proj._fwd.forward_algorithm, [n for _, n, _ in probs]))
+                        * iters * steps,
         "gradient": "drop-in (the backprojector, as the reference's autograd function)",
         "relative_residual_after_10": residual,
         "plain_loop_ops_per_s": plain_value, "speedup_vs_plain_loop": value / plain_value,

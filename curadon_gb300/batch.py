@@ -8,9 +8,12 @@ tensors.  ``forward()`` then projects every volume into its sinogram and
 The buffers stay bound, so both calls can be captured in a CUDA graph
 (``torch.cuda.graph``) and an iteration loop replayed without launch
 overhead.  The forward is the texture-unit ray march (``forward="texture"``,
-default: one array copy per problem, then one launch) or the FP32 register
-march (``forward="registers"``); ``forward="auto"`` times both on the bound
-problems once and keeps the faster (the sinograms' contents are restored
+default: one array copy per problem, then one launch), the FP32 register
+march (``forward="registers"``) or each problem's own plan default
+(``forward="plans"``: the chunked shared-memory forward for problems from
+704^2 pixels, in one re-layout and one bundle launch over all of them, the
+texture march for the others); ``forward="auto"`` times them on the bound
+problems once and keeps the fastest (the sinograms' contents are restored
 afterwards).  The backprojection is the staged one; results equal the
 single-problem operators with those algorithms bit for bit; ``adjoint()``
 adds the matched adjoint (the exact transpose of the register forward).
@@ -34,7 +37,7 @@ __all__ = ["Batch2d", "BatchProjector"]
 
 
 class Batch2d:
-    FORWARD = ("registers", "texture")
+    FORWARD = ("registers", "texture", "plans")
 
     def __init__(self, geoms: Sequence[FanGeometry], volumes: Sequence[torch.Tensor],
                  sinograms: Sequence[torch.Tensor], forward: str = "texture"):
@@ -172,7 +175,7 @@ class BatchProjector:
     register forward that ``matched`` selects.  Both directions are a few
     launches for the whole batch, capturable in a CUDA graph."""
 
-    def __init__(self, geoms: Sequence[FanGeometry], device=None, forward: str = "texture",
+    def __init__(self, geoms: Sequence[FanGeometry], device=None, forward: str = "plans",
                  matched: bool = False):
         dev = torch.device("cuda", 0) if device is None else torch.device(device)
         self.geoms = list(geoms)

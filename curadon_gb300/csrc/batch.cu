@@ -11,8 +11,11 @@
 //
 // The batched forward is the texture-unit ray march (algorithm 1; each
 // problem's volume is copied into its plan's array, then one launch samples
-// all problems through their bindless texture handles) or, selected with
-// cg_batch2d_set_forward, the FP32 register march (algorithm 0); the batched
+// all problems through their bindless texture handles), or, selected with
+// cg_batch2d_set_forward, the FP32 register march (algorithm 0) or each
+// plan's own default (algorithm 2: the chunked shared-memory forward for
+// problems from 704^2 pixels, one re-layout and one bundle launch over all
+// of them, and the texture march for the rest); the batched
 // backprojection is the staged one (algorithm 2); cg_batch2d_adjoint runs
 // the matched adjoint (the exact transpose of the register march) over the
 // same work list.  Each problem uses its own
@@ -28,7 +31,7 @@
 struct cg_batch2d {
     int device = 0;
     int count = 0;
-    int fwd_algo = 1;  // 1 texture unit, 0 registers
+    int fwd_algo = 1;  // 1 texture unit, 0 registers, 2 each plan's own (chunked / texture)
     std::vector<cg::Plan2d *> plans;
     std::vector<cg::Prob2d> probs;  // host copy (the texture forward's copies)
     cg::Prob2d *d_probs = nullptr;
@@ -89,6 +92,7 @@ int cg_batch2d_create(cg_batch2d **batch, cg_plan2d *const *plans, float *const 
         if (int rc = ensure_vol_texture(*plans[i])) return rc;
         q.tex = p.tex_vol, q.arr = p.arr_vol;
         q.quadA = p.d_quadA, q.quadB = p.d_quadB;
+        q.chunked = batch_chunked(p) ? 1 : 0;
         int blocks[kBatchStages];
         batch_blocks(p, blocks);
         for (int st = 0; st < kBatchStages; ++st) {
@@ -97,8 +101,10 @@ int cg_batch2d_create(cg_batch2d **batch, cg_plan2d *const *plans, float *const 
             starts[st * (count + 1) + i + 1] = (int)totals[st];
         }
     }
+    // stages 7..9 hold only the problems of one kind of the "plans" forward
+    // and may be empty; the others have blocks for every problem
     for (long long t : totals)
-        CG_REQUIRE(t > 0 && t < (1ll << 31), "batch too large for one launch");
+        CG_REQUIRE(t < (1ll << 31), "batch too large for one launch");
 
     std::unique_ptr<cg_batch2d> b(new cg_batch2d());
     b->device = plans[0]->device;
@@ -148,6 +154,10 @@ int cg_batch2d_forward(cg_batch2d *batch, void *stream) {
         return launch_batch2d_fwd_tex(batch->d_probs, batch->probs, batch->active,
                                       batch->d_starts + (batch->count + 1), totals[1],
                                       (cudaStream_t)stream);
+    if (batch->fwd_algo == 2)
+        return launch_batch2d_fwd_plans(batch->d_probs, batch->probs, batch->active,
+                                        batch->d_starts, totals, batch->count,
+                                        (cudaStream_t)stream);
     return launch_batch2d(batch->d_probs, batch->d_starts, totals, batch->count, true,
                           (cudaStream_t)stream);
 }
@@ -163,7 +173,7 @@ int cg_batch2d_set_active(cg_batch2d *batch, int active) {
 int cg_batch2d_set_forward(cg_batch2d *batch, int algorithm) {
     clear_error();
     CG_REQUIRE(batch, "batch is NULL");
-    CG_REQUIRE(algorithm == 0 || algorithm == 1, "batched forward algorithm must be 0 or 1");
+    CG_REQUIRE(algorithm >= 0 && algorithm <= 2, "batched forward algorithm must be 0, 1 or 2");
     batch->fwd_algo = algorithm;
     return CG_OK;
 }

@@ -140,6 +140,7 @@ struct Prob2d {
     cudaTextureObject_t tex;  // the plan's volume texture (texture forward)
     cudaArray_t arr;          // and its array
     float4 *quadA, *quadB;    // matched adjoint: the plan's quad accumulators
+    int chunked;              // the batched "plans" forward runs the chunked kernel
 };
 
 // Problem of a batched launch's block b: the last i with start[i] <= b
@@ -153,8 +154,12 @@ __device__ __forceinline__ int batch_problem(const int *__restrict__ start, int 
     return lo;
 }
 // Batched stages: re-layout, forward, sinogram re-layout, backprojection,
-// and the matched adjoint's zeroing, scatter and fold.
-constexpr int kBatchStages = 7;
+// the matched adjoint's zeroing, scatter and fold, and the "plans" forward's
+// absolute-position re-layout and chunked bundles (chunked problems) and
+// texture rays (the others).
+constexpr int kBatchStages = 10;
+// chunked-forward shape the batched "plans" forward compiles
+constexpr int kBatchChunkShape = 484;
 
 struct Plan3d {
     int device = 0;
@@ -213,6 +218,8 @@ struct Plan3d {
     // forward 5: warps of each 8 that sample through the texture unit (4 for
     // volumes of 300^3 voxels and more, set at plan creation)
     int fwd_tex_warps = 3;
+    // forward 4 / 5: blocks per SM the register bound is chosen for (1: no bound)
+    int fwd_minb = 1;
     bool axial = false;  // every backward table's y step is (0, dy, 0)
     // axial backprojection, per view: source -> voxel (0, 0, 0) (3), x step
     // (3), z step (3), y step's v component (1)
@@ -251,6 +258,8 @@ int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s);
 // batches (proj2d.cu): blocks of each stage of one problem, and the launch of
 // one direction over a batch whose starts hold 4 x (count + 1) block starts
 void batch_blocks(const Plan2d &p, int blocks[kBatchStages]);
+// true where the batched "plans" forward runs the plan's chunked shape
+bool batch_chunked(const Plan2d &p);
 int launch_batch2d(const Prob2d *probs, const int *starts, const int totals[kBatchStages],
                    int count, bool forward, cudaStream_t s);
 // the matched adjoint's padded accumulator sizes (float4 elements) and
@@ -259,6 +268,15 @@ size_t adj2d_quad_elems(const Plan2d &p, bool layoutA);
 int ensure_adj2d_quads(Plan2d &p);
 int launch_batch2d_adjoint(const Prob2d *probs, const int *starts,
                            const int totals[kBatchStages], int count, cudaStream_t s);
+// the "plans" forward: texture rays of the problems that are not chunked
+// (stage 9, after their array copies) and the chunked bundles of the others
+// (stages 7 and 8), the first `active` problems
+int launch_batch2d_fwd_plans(const Prob2d *d_probs, const std::vector<Prob2d> &probs,
+                             int active, const int *starts, const int totals[kBatchStages],
+                             int count, cudaStream_t s);
+int launch_batch2d_fwd_tex_stage(const Prob2d *d_probs, const std::vector<Prob2d> &probs,
+                                 int active, const int *starts, int total, bool only_unchunked,
+                                 cudaStream_t s);
 int launch_backward2d(const Plan2d &p, float *vol, cudaStream_t s);
 
 int ensure_plan3d_scratch(Plan3d &p, bool fwd, bool bwd);

@@ -359,20 +359,25 @@ __device__ __forceinline__ unsigned cs_column(float p, int c0, unsigned cmax, fl
 // copy's latency; the kernel then records the timeout and goes on.
 constexpr int kWaitTries = 1 << 22;
 
+// One bundle (bx: cells, by: views, bz: ray class) of the chunked forward;
+// the kernels below run it over a grid (one problem) or a work list (many).
 template <int K, int S, int T, bool PK, bool REUSE = false, int VS = 1, int NG = kCs2G,
           int MB = 0, int MAP = 0, bool ABS = false, bool TMA = false>
-__global__ void __launch_bounds__(T * VS, MB)
-    k_fwd2d_cslab(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
-                  float *__restrict__ sino, const float2 *__restrict__ tsrc,
-                  const float2 *__restrict__ tu0, const float2 *__restrict__ tdu, int W, int H,
-                  int det, int nangles, float sx, float sy, int pa, int pb) {
+__device__ __forceinline__ void cslab_bundle(const float2 *__restrict__ layA,
+                                             const float2 *__restrict__ layB,
+                                             float *__restrict__ sino,
+                                             const float2 *__restrict__ tsrc,
+                                             const float2 *__restrict__ tu0,
+                                             const float2 *__restrict__ tdu, int W, int H, int det,
+                                             int nangles, float sx, float sy, int pa, int pb,
+                                             int bx, int by, int bz) {
     static_assert(S % 2 == 0, "rows of the window buffers must stay 16-byte aligned");
     constexpr int kBuf = (K + 1) * S;               // pairs per buffer
     extern __shared__ __align__(16) float2 cwin[];  // 2 buffers
     __shared__ float s_cor[2 * NG][2];               // column = a + b * row
     __shared__ int s_win[kCs2MaxChunks];             // (first column << 16) | width, or -1
     __shared__ int s_rmin, s_rmax;
-    const bool cls_y = blockIdx.z == 0;
+    const bool cls_y = bz == 0;
     const float2 *lay = cls_y ? layA : layB;
     const int pitch = cls_y ? pa : pb;
     const int qmax = cls_y ? H : W;
@@ -399,7 +404,7 @@ __global__ void __launch_bounds__(T * VS, MB)
                               : (int)((threadIdx.x >> 4) % VS) * GV;
     // bundle view of the thread's ray g
     auto bview = [&](int g) { return MAP == 2 ? gb / GV + g * VS : gb + g; };
-    const int u0 = blockIdx.x * T, v0 = blockIdx.y * NG;
+    const int u0 = bx * T, v0 = by * NG;
     const int u = u0 + cell;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
@@ -646,6 +651,18 @@ __global__ void __launch_bounds__(T * VS, MB)
         }
         sino[(size_t)view * det + u] = out;
     }
+}
+
+template <int K, int S, int T, bool PK, bool REUSE = false, int VS = 1, int NG = kCs2G,
+          int MB = 0, int MAP = 0, bool ABS = false, bool TMA = false>
+__global__ void __launch_bounds__(T * VS, MB)
+    k_fwd2d_cslab(const float2 *__restrict__ layA, const float2 *__restrict__ layB,
+                  float *__restrict__ sino, const float2 *__restrict__ tsrc,
+                  const float2 *__restrict__ tu0, const float2 *__restrict__ tdu, int W, int H,
+                  int det, int nangles, float sx, float sy, int pa, int pb) {
+    cslab_bundle<K, S, T, PK, REUSE, VS, NG, MB, MAP, ABS, TMA>(
+        layA, layB, sino, tsrc, tu0, tdu, W, H, det, nangles, sx, sy, pa, pb, blockIdx.x,
+        blockIdx.y, blockIdx.z);
 }
 
 }  // namespace
@@ -1057,6 +1074,30 @@ __global__ void __launch_bounds__(256)
 }
 
 __global__ void __launch_bounds__(256)
+    k_batch_relayout2d_abs(const Prob2d *__restrict__ probs, const int *__restrict__ start,
+                           int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob2d &q = probs[i];
+    const int local = blockIdx.x - start[i];
+    const int gx = (q.W + 2 * kPad + kTile - 1) / kTile;
+    relayout2d_tile<true>(q.vol, q.W, q.H, q.layA, q.layB, q.pa, q.pb, local % gx, local / gx);
+}
+
+// The chunked forward's default shape (484) over a work list: each block one
+// bundle of one problem, the same code and shared memory as the single launch.
+__global__ void __launch_bounds__(256, 3)
+    k_batch_fwd2d_cslab(const Prob2d *__restrict__ probs, const int *__restrict__ start,
+                        int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob2d &q = probs[i];
+    const int local = blockIdx.x - start[i];
+    const int gx = (q.det + 127) / 128, gy = (q.nangles + 7) / 8;
+    cslab_bundle<16, 256, 128, true, false, 2, 8, 3, 2, true, true>(
+        q.layA, q.layB, q.sino, q.src, q.u0, q.du, q.W, q.H, q.det, q.nangles, q.sx, q.sy, q.pa,
+        q.pb, local % gx, (local / gx) % gy, local / (gx * gy));
+}
+
+__global__ void __launch_bounds__(256)
     k_batch_fwd2d(const Prob2d *__restrict__ probs, const int *__restrict__ start, int count) {
     const int i = batch_problem(start, count, blockIdx.x);
     const Prob2d &q = probs[i];
@@ -1105,6 +1146,35 @@ void batch_blocks(const Plan2d &p, int blocks[kBatchStages]) {
                               1024);
     blocks[5] = ceil_div(p.det, 32) * ceil_div(p.nangles, 8);
     blocks[6] = ceil_div(p.W, 32) * ceil_div(p.H, 8);
+    // "plans" forward: the chunked bundles (with their re-layout) where the
+    // plan's own forward is the chunked shape compiled for batches, else the
+    // texture rays
+    const bool chunked = batch_chunked(p);
+    blocks[7] = chunked ? blocks[0] : 0;
+    blocks[8] = chunked ? ceil_div(p.det, 128) * ceil_div(p.nangles, 8) * 2 : 0;
+    blocks[9] = chunked ? 0 : blocks[1];
+}
+
+bool batch_chunked(const Plan2d &p) {
+    return p.algo_fwd == 4 && p.fwd_chunk_rows == kBatchChunkShape &&
+           std::max(p.pitchA(), p.pitchB()) < 32768;
+}
+
+int launch_batch2d_fwd_plans(const Prob2d *d_probs, const std::vector<Prob2d> &probs,
+                             int active, const int *starts, const int totals[kBatchStages],
+                             int count, cudaStream_t s) {
+    int rc = launch_batch2d_fwd_tex_stage(d_probs, probs, active, starts + 9 * (count + 1),
+                                          totals[9], true, s);
+    if (rc) return rc;
+    if (totals[8] == 0) return CG_OK;
+    k_batch_relayout2d_abs<<<totals[7], dim3(32, 8), 0, s>>>(d_probs, starts + 7 * (count + 1),
+                                                             count);
+    CG_TRY_CUDA(cudaGetLastError());
+    constexpr int smem = 2 * (int)sizeof(float2) * (16 + 1) * 256;
+    if ((rc = ensure_smem_attr((const void *)k_batch_fwd2d_cslab, smem))) return rc;
+    k_batch_fwd2d_cslab<<<totals[8], 256, smem, s>>>(d_probs, starts + 8 * (count + 1), count);
+    CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
 }
 
 int launch_batch2d(const Prob2d *probs, const int *starts, const int totals[kBatchStages],

@@ -296,12 +296,20 @@ int ensure_vol_texture(Plan2d &p) {
 // one launch over the work list (stage-1 starts: 32 x 8 cell-view tiles).
 int launch_batch2d_fwd_tex(const Prob2d *d_probs, const std::vector<Prob2d> &probs, int active,
                            const int *starts, int total, cudaStream_t s) {
+    return launch_batch2d_fwd_tex_stage(d_probs, probs, active, starts, total, false, s);
+}
+
+int launch_batch2d_fwd_tex_stage(const Prob2d *d_probs, const std::vector<Prob2d> &probs,
+                                 int active, const int *starts, int total, bool only_unchunked,
+                                 cudaStream_t s) {
     for (int i = 0; i < active; ++i) {
         const Prob2d &q = probs[i];
+        if (only_unchunked && q.chunked) continue;
         CG_TRY_CUDA(cudaMemcpy2DToArrayAsync(q.arr, 0, 0, q.vol, sizeof(float) * q.W,
                                              sizeof(float) * q.W, q.H, cudaMemcpyDeviceToDevice,
                                              s));
     }
+    if (total == 0) return CG_OK;
     k_batch_fwd2d_tex<<<total, dim3(32, 8), 0, s>>>(d_probs, starts, (int)probs.size());
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;

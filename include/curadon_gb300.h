@@ -305,7 +305,10 @@ int cg_batch2d_adjoint(cg_batch2d *batch, void *stream);
  * resident batch of `count` slots serves however many requests are waiting
  * without being rebuilt. */
 int cg_batch2d_set_active(cg_batch2d *batch, int active);
-/* the batched forward's algorithm: 1 texture unit (default), 0 registers */
+/* the batched forward's algorithm: 1 texture unit (default), 0 registers,
+ * 2 each plan's own default (the chunked shared-memory forward for problems
+ * from 704^2 pixels, the texture unit below; results equal cg_forward_2d on
+ * the plans bit for bit) */
 int cg_batch2d_set_forward(cg_batch2d *batch, int algorithm);
 int cg_batch2d_get_forward(const cg_batch2d *batch, int *algorithm);
 

@@ -101,6 +101,64 @@ def test_batch_graph_replay(cuda_device, algo):
         assert torch.equal(o, d)
 
 
+def test_batch_plans_forward_equals_each_plans_default(cuda_device):
+    """forward="plans": problems from 704^2 pixels through the batched chunked
+    forward (one re-layout and one bundle launch for all of them), the others
+    through the texture march -- each problem's result equal, bit for bit, to
+    its plan's own default forward; also inside a CUDA graph."""
+    rng = np.random.default_rng(12)
+    geoms, vols, sinos = [], [], []
+    for k, n in enumerate([1024, 128, 768, 256, 720, 96]):
+        nangles = int(rng.integers(90, 240))
+        g = fan_config(n, nangles)
+        if k == 2:  # a jittered vector geometry among the big ones
+            v = np.asarray(FanGeometry(**g).to_vec())
+            v[:, 4:] *= g["det_spacing"]
+            v[:, :4] += rng.normal(0, 0.5, (nangles, 4))
+            geom = FanVecGeometry(g["vol_shape"], g["det_shape"], v, device=cuda_device.index or 0)
+        else:
+            geom = FanGeometry(**g, device=cuda_device.index or 0)
+        geoms.append(geom)
+        vols.append(ellipses_2d(n, k, device=cuda_device).contiguous())
+        sinos.append(torch.zeros(geom.sinogram_shape(), device=cuda_device))
+    expect = []
+    for g, v in zip(geoms, vols):
+        p = g._make_plan()
+        assert p.algorithm[0] == ("chunked" if v.numel() >= 704 * 704 else "texture")
+        from curadon_gb300.backend import forward_2d
+
+        s = torch.zeros(g.sinogram_shape(), device=cuda_device)
+        forward_2d(v, s, p)
+        expect.append(s)
+    b = Batch2d(geoms, vols, sinos, forward="plans")
+    assert b.forward_algorithm == "plans"
+    b.forward()
+    torch.cuda.synchronize()
+    for i, (s, e) in enumerate(zip(sinos, expect)):
+        assert torch.equal(s, e), i
+    for s in sinos:
+        s.zero_()
+    graph = torch.cuda.CUDAGraph()
+    st = torch.cuda.Stream()
+    st.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(st), torch.cuda.graph(graph, stream=st):
+        b.forward()
+    torch.cuda.current_stream().wait_stream(st)
+    graph.replay()
+    torch.cuda.synchronize()
+    for i, (s, e) in enumerate(zip(sinos, expect)):
+        assert torch.equal(s, e), i
+    # the first problems only (a resident batch serving fewer requests)
+    for s in sinos:
+        s.zero_()
+    b.set_active(3)
+    b.forward()
+    torch.cuda.synchronize()
+    for i in range(3):
+        assert torch.equal(sinos[i], expect[i]), i
+    assert all(float(s.abs().sum()) == 0.0 for s in sinos[3:])
+
+
 def test_batch_rejects_bad_input(cuda_device):
     g = FanGeometry(**fan_config(64, 30), device=cuda_device.index or 0)
     v = torch.zeros((64, 64), device=cuda_device)
