@@ -125,9 +125,6 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
             if (val == "quad") p3->algo_fwd = 4;
             if (val == "mixed") p3->algo_fwd = 5;
         }
-        if (p3 && key == "fwd3d_minb")
-            for (int k : {1, 7, 8})
-                if (val == std::to_string(k)) p3->fwd_minb = k;
         if (p3 && key == "fwd3d_tex")
             for (int k = 0; k <= 8; ++k)
                 if (val == std::to_string(k)) p3->fwd_tex_warps = k;

@@ -335,8 +335,7 @@ __device__ __forceinline__ Ray3 setup_ray3(const float4 o, const float4 du, cons
 // (the reference's tex3D sampling): the texture path and the L1 load path
 // then work side by side (3 of 8 warps: -8 % at 256^3, -21 % at 512^3
 // against quads alone).
-template <int MINB>
-__global__ void __launch_bounds__(256, MINB)
+__global__ void __launch_bounds__(256)
     k_fwd3d_quad(const float4 *__restrict__ QA, const float4 *__restrict__ QB,
                  float *__restrict__ sino, const float4 *__restrict__ torg,
                  const float4 *__restrict__ tdu, const float4 *__restrict__ tdv,
@@ -759,9 +758,7 @@ int launch_forward3d_quad(Plan3d &p, const float *vol, float *sino, cudaStream_t
         if (rc) return rc;
         tex = p.tex3;
     }
-    auto kernel = p.fwd_minb == 8 ? k_fwd3d_quad<8> : p.fwd_minb == 7 ? k_fwd3d_quad<7>
-                                                                      : k_fwd3d_quad<1>;
-    kernel<<<(unsigned)blocks, 256, 0, s>>>(p.d_volQA, p.d_volQB, sino, p.d_forg, p.d_fdu,
+    k_fwd3d_quad<<<(unsigned)blocks, 256, 0, s>>>(p.d_volQA, p.d_volQB, sino, p.d_forg, p.d_fdu,
                                                   p.d_fdv, p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V,
                                                   p.nangles, utiles, tex, tex_warps, p.exact_t);
     CG_TRY_CUDA(cudaGetLastError());
