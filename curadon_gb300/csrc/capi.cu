@@ -125,6 +125,10 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
             if (val == "quad") p3->algo_fwd = 4;
             if (val == "mixed") p3->algo_fwd = 5;
         }
+        if (p3 && key == "fwd3d_unroll") {
+            if (val == "1") p3->fwd_unroll = 1;
+            if (val == "2") p3->fwd_unroll = 2;
+        }
         if (p3 && key == "fwd3d_tex")
             for (int k = 0; k <= 8; ++k)
                 if (val == std::to_string(k)) p3->fwd_tex_warps = k;

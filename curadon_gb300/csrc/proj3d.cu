@@ -335,6 +335,13 @@ __device__ __forceinline__ Ray3 setup_ray3(const float4 o, const float4 du, cons
 // (the reference's tex3D sampling): the texture path and the L1 load path
 // then work side by side (3 of 8 warps: -8 % at 256^3, -21 % at 512^3
 // against quads alone).
+// UNR = 2: two samples per iteration, all their loads (or texture fetches)
+// issued before either is accumulated, so each warp keeps twice the memory
+// requests in flight; the samples, their order of summation and the march's
+// parameter sequence are those of UNR = 1 (the second sample's loads happen
+// even when it lies past tmax, at an offset clamped into the array, and are
+// then dropped).
+template <int UNR>
 __global__ void __launch_bounds__(256)
     k_fwd3d_quad(const float4 *__restrict__ QA, const float4 *__restrict__ QB,
                  float *__restrict__ sino, const float4 *__restrict__ torg,
@@ -353,11 +360,24 @@ __global__ void __launch_bounds__(256)
     if (warp < tex_warps) {
         // this warp's rays through the texture unit (trilinear, 8-bit weights)
         float acc = 0.f, t = r.tmin;
-        for (int k = 0; k <= r.nsteps + 1; ++k) {
+        const int kend = r.nsteps + 2;
+        for (int k = 0; k < kend; k += UNR) {
             if (!(t <= r.tmax)) break;
-            acc += tex3D<float>(tex, fmaf(r.dx, t, r.sx) + 0.5f, fmaf(r.dy, t, r.sy) + 0.5f,
-                                fmaf(r.dz, t, r.sz) + 0.5f);
-            t = march_next(t, k, r.tmin, r.h, exact_t);
+            const float s0 = tex3D<float>(tex, fmaf(r.dx, t, r.sx) + 0.5f,
+                                          fmaf(r.dy, t, r.sy) + 0.5f, fmaf(r.dz, t, r.sz) + 0.5f);
+            if constexpr (UNR == 2) {
+                const float t1 = march_next(t, k, r.tmin, r.h, exact_t);
+                const float s1 = tex3D<float>(tex, fmaf(r.dx, t1, r.sx) + 0.5f,
+                                              fmaf(r.dy, t1, r.sy) + 0.5f,
+                                              fmaf(r.dz, t1, r.sz) + 0.5f);
+                acc += s0;
+                if (!(k + 1 < kend && t1 <= r.tmax)) break;
+                acc += s1;
+                t = march_next(t1, k + 1, r.tmin, r.h, exact_t);
+            } else {
+                acc += s0;
+                t = march_next(t, k, r.tmin, r.h, exact_t);
+            }
         }
         sino[((size_t)view * V + iv) * U + iu] = acc;
         return;
@@ -375,24 +395,47 @@ __global__ void __launch_bounds__(256)
     // off = (bits_c - base) slice + (bits_b - base) PA + (bits_a - base), mod 2^32
     const unsigned K = base * slice + base * PA + base;
     const float4 *Q1 = Q + slice;
-    float acc = 0.f, t = r.tmin;
-    for (int k = 0; k <= r.nsteps + 1; ++k) {
-        if (!(t <= r.tmax)) break;
+    // one sample at parameter t: its two quads' loads, then its value
+    struct Fetch {
+        float4 q0, q1;
+        float wa, wb, wc;
+    };
+    auto fetch = [&](float t) {
+        Fetch f;
         const float pa = fmaf(da, t, sa), pb = fmaf(r.dy, t, r.sy), pc = fmaf(dc, t, sc);
         const float ta = __fadd_rd(pa, kMagic), tb = __fadd_rd(pb, kMagic),
                     tc = __fadd_rd(pc, kMagic);
-        const float wa = __fadd_rn(pa, -__fadd_rn(ta, -kMagic));
-        const float wb = __fadd_rn(pb, -__fadd_rn(tb, -kMagic));
-        const float wc = __fadd_rn(pc, -__fadd_rn(tc, -kMagic));
+        f.wa = __fadd_rn(pa, -__fadd_rn(ta, -kMagic));
+        f.wb = __fadd_rn(pb, -__fadd_rn(tb, -kMagic));
+        f.wc = __fadd_rn(pc, -__fadd_rn(tc, -kMagic));
         unsigned off = __float_as_uint(tc) * slice + __float_as_uint(tb) * PA +
                        (__float_as_uint(ta) - K);
         off = min(off, maxoff);
-        const float4 q0 = __ldg(Q + off), q1 = __ldg(Q1 + off);
-        const float l0 = fmaf(wa, q0.y, q0.x), g0 = fmaf(wa, q0.w, q0.z);
-        const float l1 = fmaf(wa, q1.y, q1.x), g1 = fmaf(wa, q1.w, q1.z);
-        const float m0 = fmaf(wb, g0, l0), m1 = fmaf(wb, g1, l1);
-        acc += fmaf(wc, m1 - m0, m0);
-        t = march_next(t, k, r.tmin, r.h, exact_t);
+        f.q0 = __ldg(Q + off), f.q1 = __ldg(Q1 + off);
+        return f;
+    };
+    auto value = [](const Fetch &f) {
+        const float l0 = fmaf(f.wa, f.q0.y, f.q0.x), g0 = fmaf(f.wa, f.q0.w, f.q0.z);
+        const float l1 = fmaf(f.wa, f.q1.y, f.q1.x), g1 = fmaf(f.wa, f.q1.w, f.q1.z);
+        const float m0 = fmaf(f.wb, g0, l0), m1 = fmaf(f.wb, g1, l1);
+        return fmaf(f.wc, m1 - m0, m0);
+    };
+    float acc = 0.f, t = r.tmin;
+    const int kend = r.nsteps + 2;
+    for (int k = 0; k < kend; k += UNR) {
+        if (!(t <= r.tmax)) break;
+        const Fetch f0 = fetch(t);
+        if constexpr (UNR == 2) {
+            const float t1 = march_next(t, k, r.tmin, r.h, exact_t);
+            const Fetch f1 = fetch(t1);
+            acc += value(f0);
+            if (!(k + 1 < kend && t1 <= r.tmax)) break;
+            acc += value(f1);
+            t = march_next(t1, k + 1, r.tmin, r.h, exact_t);
+        } else {
+            acc += value(f0);
+            t = march_next(t, k, r.tmin, r.h, exact_t);
+        }
     }
     sino[((size_t)view * V + iv) * U + iu] = acc;
 }
@@ -758,9 +801,10 @@ int launch_forward3d_quad(Plan3d &p, const float *vol, float *sino, cudaStream_t
         if (rc) return rc;
         tex = p.tex3;
     }
-    k_fwd3d_quad<<<(unsigned)blocks, 256, 0, s>>>(p.d_volQA, p.d_volQB, sino, p.d_forg, p.d_fdu,
-                                                  p.d_fdv, p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V,
-                                                  p.nangles, utiles, tex, tex_warps, p.exact_t);
+    auto kernel = p.fwd_unroll == 2 ? k_fwd3d_quad<2> : k_fwd3d_quad<1>;
+    kernel<<<(unsigned)blocks, 256, 0, s>>>(p.d_volQA, p.d_volQB, sino, p.d_forg, p.d_fdu,
+                                            p.d_fdv, p.d_fsrc, p.X, p.Y, p.Z, p.U, p.V,
+                                            p.nangles, utiles, tex, tex_warps, p.exact_t);
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
 }
