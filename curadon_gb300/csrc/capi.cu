@@ -73,6 +73,7 @@ bool listed(const int (&list)[N], int v) {
 // cslab<443 | 474 | 484>; bwd2d = alu | tex | smem; bwd2d_minb = 27 | 48 | 68
 // (staged backprojector variants); adj2d = pair | quad; fwd3d = alu | tex3 |
 // quad | mixed; fwd3d_tex = 0..8 (texture warps of 8 in the mixed forward);
+// fwd3d_unroll = 1 | 2 (samples per iteration of the quad / mixed forward);
 // fwd3d_block = BXxBYxBZ; bwd3d = quad | pair (general kernel on row-pair
 // quads or on 8-byte pairs, its fallback where quads do not fit) | ax8m5
 // (axial runs);

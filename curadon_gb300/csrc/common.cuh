@@ -218,8 +218,9 @@ struct Plan3d {
     // forward 5: warps of each 8 that sample through the texture unit (4 for
     // volumes of 300^3 voxels and more, set at plan creation)
     int fwd_tex_warps = 3;
-    // forward 4 / 5: samples per loop iteration with their loads issued together
-    int fwd_unroll = 1;
+    // forward 4 / 5: samples per loop iteration with their loads issued
+    // together (2, default; 1); the results do not depend on it
+    int fwd_unroll = 2;
     bool axial = false;  // every backward table's y step is (0, dy, 0)
     // axial backprojection, per view: source -> voxel (0, 0, 0) (3), x step
     // (3), z step (3), y step's v component (1)

@@ -337,3 +337,23 @@ def test_fp32_drift_along_rays(cuda_device, monkeypatch, n, nangles, det):
     assert err["exact"][0] <= err["step"][0]
     assert err["exact"][1] <= err["step"][1]
     assert err["exact"][0] < 4e-5 and err["exact"][1] < 1e-4
+
+
+@pytest.mark.parametrize("algo", ["mixed", "quad"])
+def test_forward_two_samples_per_iteration_same_bits(cuda_device, monkeypatch, algo):
+    """The quad / mixed forward takes two samples per loop iteration with both
+    samples' loads in flight (default); the same samples are summed in the
+    same order as one per iteration (CURADON_GB300_ALGO fwd3d_unroll=1), so
+    the sinograms are equal bit for bit, hit/miss included."""
+    shape, nangles, det = (33, 40, 28), 37, 70
+    g = cone_config(shape[0], nangles, det)
+    g["vol_shape"] = shape
+    ph = ellipsoids_3d(shape, 8).numpy()
+    out = []
+    for unroll in ("1", "2"):
+        monkeypatch.setenv("CURADON_GB300_ALGO", f"fwd3d={algo},fwd3d_unroll={unroll}")
+        geom = make(g, cuda_device)
+        geom.plan
+        monkeypatch.delenv("CURADON_GB300_ALGO")
+        out.append(run_fwd(geom, ph, cuda_device))
+    assert np.array_equal(out[0], out[1])
