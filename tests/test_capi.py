@@ -124,3 +124,13 @@ def test_check_maps_codes_to_exceptions(lib):
         _lib.check(_lib.CG_ERR_UNSUPPORTED)
     with pytest.raises(_lib.CuradonError):
         _lib.check(_lib.CG_ERR_CUDA)
+
+
+def test_batch_entry_points_reject_null(lib):
+    """The batch calls check their handle before touching the GPU."""
+    assert lib.cg_batch2d_forward(None, None) == _lib.CG_ERR_INVALID
+    assert lib.cg_batch2d_backward(None, None) == _lib.CG_ERR_INVALID
+    assert lib.cg_batch2d_adjoint(None, None) == _lib.CG_ERR_INVALID
+    assert lib.cg_batch2d_set_active(None, 1) == _lib.CG_ERR_INVALID
+    assert lib.cg_batch2d_set_forward(None, 2) == _lib.CG_ERR_INVALID
+    assert lib.cg_batch2d_destroy(None) == _lib.CG_OK

@@ -28,3 +28,27 @@ def test_memory_estimate_grows_with_the_problem():
     # the volume and sinogram alone are a lower bound
     assert large >= 4 * (1024 * 1024 + 1024 * 1449)
     assert request_bytes(req("sirt", 256)) > request_bytes(req("fbp", 256))
+
+
+def test_coalescing_classes():
+    """2D FBP / SIRT requests below 704^2 pixels coalesce by geometry, kind,
+    iteration count and filter; larger 2D and all 3D requests run alone."""
+    from curadon_gb300.serve import _batchable, _class_key
+
+    small = FanGeometry(**fan_config(256, 90))
+    same = FanGeometry(**fan_config(256, 90))
+    big = FanGeometry(**fan_config(1024, 90))
+    cone = ConeGeometry(**cone_config(32, 20, 48))
+
+    def req(kind, g, iters=20, filt="ram-lak"):
+        return Request(kind, g, torch.zeros(g.sinogram_shape()), iters=iters, filter_name=filt)
+
+    assert _batchable(req("fbp", small)) and _batchable(req("sirt", small))
+    assert not _batchable(req("fbp", big)) and not _batchable(req("cgls", cone))
+    assert not _batchable(req("cgls", small))
+    assert _class_key(req("fbp", small)) == _class_key(req("fbp", same))
+    assert _class_key(req("fbp", small)) != _class_key(req("sirt", small))
+    assert _class_key(req("sirt", small, 20)) != _class_key(req("sirt", small, 10))
+    assert _class_key(req("fbp", small)) != _class_key(req("fbp", small, filt="hann"))
+    # FBP ignores the iteration count
+    assert _class_key(req("fbp", small, 0)) == _class_key(req("fbp", small, 20))
