@@ -173,7 +173,8 @@ class _ClassBatch:
             solver = SirtSolver(self.geoms[0], device, lam=lam)
             self.R, self.C = solver.R, solver.C
             self.graphs: Dict[int, torch.cuda.CUDAGraph] = {}
-        self.bytes = 4 * (self.Y.numel() * 2 + self.X.numel() * (1 if self.kind == "fbp" else 2))
+        # stacked buffers plus each problem's plan scratch, as admission counts it
+        self.bytes = self.capacity * request_bytes(req)
 
     def _sirt_iteration(self, m: int):
         X, S, BP = self.X[:m], self.S[:m], self.BP[:m]
@@ -310,6 +311,13 @@ class Server:
                     return None
                 if self._inflight and torch.cuda.mem_get_info(self.device)[0] < need:
                     return None
+                if key is not None and cb is None:
+                    # a new class batch holds `batch_slots` problems' buffers and
+                    # plans for as long as it stays resident: without room for
+                    # them in the budget the request runs on its own
+                    extra = self.batch_slots * need
+                    if self.resident_bytes() + self.inflight_bytes + extra > self.budget:
+                        key = None
                 items = [(req, fut)]
                 taken = [idx]
                 if key is not None:
@@ -328,6 +336,10 @@ class Server:
                     del self._pending[j]
                 return items, need, key
             return None
+
+    def resident_bytes(self) -> int:
+        """Device bytes held by the resident class batches (an estimate)."""
+        return sum(cb.bytes for cb in self._classes.values())
 
     def _class_batch(self, key, req: Request) -> _ClassBatch:
         cb = self._classes.get(key)
