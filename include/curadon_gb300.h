@@ -20,10 +20,12 @@
  *  - Forward projections overwrite the sinogram (2D: every ray; 3D: every ray
  *    that hits the volume's bounding box, as forward_3d.hpp:74-76 skips the
  *    others).  Backprojections ADD into the volume, as the reference does
- *    (backward_2d.hpp:99, backward_3d.hpp:115-121).
- *  - Plans are immutable after creation except for the forward block shape;
- *    one plan may be used from several threads on different streams, but two
- *    calls on the same plan must not overlap on the GPU (they share scratch).
+ *    (backward_2d.hpp:99, backward_3d.hpp:44-53 and :98-106).
+ *  - A plan's geometry is fixed at creation; its selectors (algorithm,
+ *    kernel shape, forward block shape) may change between calls, not while a
+ *    call on the plan is in flight.  One plan may be used from several threads
+ *    on different streams, but two calls on the same plan must not overlap on
+ *    the GPU (they share the plan's scratch).
  */
 #ifndef CURADON_GB300_H
 #define CURADON_GB300_H
