@@ -857,6 +857,7 @@ def _serve_pass(reqs, rate: float, seed: int = 7, batching: bool = True, count: 
     for f in [srv.submit(r) for r in reqs]:  # warm-up: slot and class-batch residency
         f.result()
     srv.latencies.clear()
+    srv.latencies_by_kind.clear()
     srv.completed, srv.t_first, srv.t_last = 0, None, None
     rng = np.random.default_rng(seed)
     count = count or len(reqs)
@@ -945,7 +946,7 @@ def run_serve(args):
                      "arrival_span_s": st["arrival_span_s"],
                      "wall_s": time.perf_counter() - t0, "solves_per_s": st["solves_per_s"],
                      "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "batches": st["batches"],
-                     "clocks": st["clocks"]}
+                     "latency_by_kind": st["by_kind"], "clocks": st["clocks"]}
     line = {
         "metric": "served solves/s", "value": served["solves_per_s"], "unit": "solves/s",
         "n_gpus": 1, "steps": len(reqs), "warmup": len(reqs),
@@ -958,12 +959,14 @@ def run_serve(args):
                                "CGLS-30 (128^3..256^3, 180..360 views), 8 slots, 2D requests "
                                "below 704^2 pixels coalesced into class batches of up to 16",
                    "parallelism": "one GPU, concurrent streams"},
-        "p50_ms": served["p50_ms"], "p99_ms": served["p99_ms"], "clocks": served["clocks"],
+        "p50_ms": served["p50_ms"], "p99_ms": served["p99_ms"],
+        "latency_by_kind": served["by_kind"], "clocks": served["clocks"],
         "batches": served["batches"],
         "plain_loop_solves_per_s": plain_all,
         "speedup_vs_plain_loop": served["solves_per_s"] / plain_all,
         "below_capacity": {"rate_per_s": sub_rate, "solves_per_s": relaxed["solves_per_s"],
-                           "p50_ms": relaxed["p50_ms"], "p99_ms": relaxed["p99_ms"]},
+                           "p50_ms": relaxed["p50_ms"], "p99_ms": relaxed["p99_ms"],
+                           "latency_by_kind": relaxed["by_kind"]},
         "mix_2d_only": {"requests": len(reqs2d), "rate_per_s": rate_2d,
                         "solves_per_s": served_2d["solves_per_s"],
                         "p50_ms": served_2d["p50_ms"], "p99_ms": served_2d["p99_ms"],

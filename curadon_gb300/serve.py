@@ -21,8 +21,12 @@ elementwise launches over all of them, captured once per batch size as a
 CUDA graph and replayed).  Batched results equal the single-request path bit
 for bit (the same kernels per problem).
 
-Latencies (submission to result on the host) and throughput are kept for
-``stats()`` (p50 / p99 latency, solves per second).
+3D requests, each of which fills the GPU for a long time, may hold at most
+``heavy_slots`` slots (default half), so that 2D requests queued behind them
+keep being admitted, and 2D requests run on high-priority streams, so that
+their blocks start ahead of the 3D requests' as SMs free up.  Latencies
+(submission to result on the host) and throughput are kept for ``stats()``
+(p50 / p99 latency, also per kind; solves per second).
 """
 from __future__ import annotations
 
@@ -102,6 +106,11 @@ def request_bytes(req: Request) -> int:
 class _Slot:
     def __init__(self, device: torch.device, max_resident: int):
         self.stream = torch.cuda.Stream(device)
+        # 2D requests run on a high-priority stream: when a 3D request's long
+        # kernels occupy the GPU, the block scheduler starts the 2D blocks as
+        # SMs free up instead of queueing them behind the 3D work
+        lo, hi = torch.cuda.Stream.priority_range()
+        self.stream_hi = torch.cuda.Stream(device, priority=min(lo, hi))
         self.device = device
         self.resident: "collections.OrderedDict[tuple, object]" = collections.OrderedDict()
         self.max_resident = max_resident
@@ -134,6 +143,11 @@ def _batchable(req: Request) -> bool:
     g = req.geom
     return (req.kind in ("fbp", "sirt") and isinstance(g, FanGeometry)
             and int(g.vol_shape[0]) * int(g.vol_shape[1]) < BATCH_PIXELS)
+
+
+def _heavy(req: Request) -> bool:
+    """3D requests: each fills the GPU on its own for a long time."""
+    return isinstance(req.geom, ConeGeometry)
 
 
 def _class_key(req: Request) -> tuple:
@@ -243,9 +257,14 @@ def solve_alone(req: Request, device=0) -> torch.Tensor:
 class Server:
     def __init__(self, device: int = 0, slots: int = 8, hbm_budget: float = 150e9,
                  max_resident: int = 16, batching: bool = True, batch_slots: int = 16,
-                 max_class_batches: int = 32):
+                 max_class_batches: int = 32, heavy_slots: Optional[int] = None):
         self.device = torch.device("cuda", device)
         torch.cuda.init()
+        # 3D requests (each fills the GPU for a long time) may hold at most
+        # heavy_slots of the slots at once, so the 2D requests behind them in
+        # the queue keep flowing; default: half the slots
+        self.heavy_slots = max(1, slots // 2) if heavy_slots is None else max(1, int(heavy_slots))
+        self.heavy_inflight = 0
         self.batching = bool(batching)
         self.batch_slots = int(batch_slots)
         self.max_class_batches = int(max_class_batches)
@@ -260,6 +279,7 @@ class Server:
         self._cv = threading.Condition()
         self._stop = False
         self.latencies: List[float] = []
+        self.latencies_by_kind: Dict[str, List[float]] = {}
         self.completed = 0
         self.t_first: Optional[float] = None
         self.t_last: Optional[float] = None
@@ -273,7 +293,11 @@ class Server:
         with self._cv:
             if self._stop:
                 raise RuntimeError("server is closed")
-            self._pending.append((req, fut))
+            # what admission needs to know about the request, worked out once
+            # (the geometry key hashes the per-view arrays)
+            meta = (_heavy(req), _class_key(req) if _batchable(req) else None,
+                    request_bytes(req))
+            self._pending.append((req, fut, meta))
             self._cv.notify()
         return fut
 
@@ -287,9 +311,13 @@ class Server:
     def stats(self) -> Dict[str, float]:
         lat = np.asarray(self.latencies) if self.latencies else np.zeros(1)
         span = (self.t_last - self.t_first) if self.completed > 1 else float("nan")
+        by_kind = {k: {"p50_ms": float(np.percentile(v, 50) * 1e3),
+                       "p99_ms": float(np.percentile(v, 99) * 1e3), "count": len(v)}
+                   for k, v in self.latencies_by_kind.items() if v}
         return {"completed": self.completed, "p50_ms": float(np.percentile(lat, 50) * 1e3),
                 "p99_ms": float(np.percentile(lat, 99) * 1e3),
-                "solves_per_s": (self.completed / span) if span and span > 0 else float("nan")}
+                "solves_per_s": (self.completed / span) if span and span > 0 else float("nan"),
+                "by_kind": by_kind}
 
     # ---------------------------------------------------------- GPU thread
     def _next(self):
@@ -301,12 +329,13 @@ class Server:
         with self._cv:
             if not self._pending or not self.free:
                 return None
-            for idx, (req, fut) in enumerate(self._pending):
-                key = _class_key(req) if self.batching and _batchable(req) else None
+            for idx, (req, fut, (heavy, ckey, need)) in enumerate(self._pending):
+                if heavy and self.heavy_inflight >= self.heavy_slots:
+                    continue  # its lane is full; lighter requests behind it may go
+                key = ckey if self.batching else None
                 cb = self._classes.get(key) if key is not None else None
                 if cb is not None and cb.busy:
                     continue  # its class batch is in flight; later requests may go
-                need = request_bytes(req)
                 if self._inflight and self.inflight_bytes + need > self.budget:
                     return None
                 if self._inflight and torch.cuda.mem_get_info(self.device)[0] < need:
@@ -324,9 +353,8 @@ class Server:
                     for j in range(idx + 1, len(self._pending)):
                         if len(items) >= self.batch_slots:
                             break
-                        r2, f2 = self._pending[j]
-                        if _batchable(r2) and _class_key(r2) == key:
-                            n2 = request_bytes(r2)
+                        r2, f2, (_, k2, n2) = self._pending[j]
+                        if k2 == key:
                             if self.inflight_bytes + need + n2 > self.budget:
                                 break
                             items.append((r2, f2))
@@ -362,15 +390,16 @@ class Server:
             items, need, key = nxt
             k = self.free.pop()
             slot = self.slots[k]
+            stream = slot.stream if _heavy(items[0][0]) else slot.stream_hi
             cb = None
             try:
-                with torch.cuda.stream(slot.stream):
+                with torch.cuda.stream(stream):
                     if key is None:
                         outs = [_execute(slot, items[0][0])]
                     else:
                         cb = self._class_batch(key, items[0][0])
                         cb.busy = True
-                        stacked = cb.run([r.sinogram for r, _ in items], slot.stream)
+                        stacked = cb.run([r.sinogram for r, _ in items], stream)
                         outs = list(stacked)
                         self.batches_run += 1
                     hosts = []
@@ -379,7 +408,7 @@ class Server:
                         host.copy_(out, non_blocking=True)
                         hosts.append(host)
                     ev = torch.cuda.Event()
-                    ev.record(slot.stream)
+                    ev.record(stream)
             except Exception as e:  # a bad request fails alone (with its batch)
                 self.free.append(k)
                 if cb is not None:
@@ -388,7 +417,9 @@ class Server:
                     fut.set_exception(e)
                 continue
             self.inflight_bytes += need
-            self._inflight.append((items, k, ev, hosts, need, cb))
+            heavy = _heavy(items[0][0])
+            self.heavy_inflight += heavy
+            self._inflight.append((items, k, ev, hosts, need, cb, heavy))
             progressed = True
         return progressed
 
@@ -396,15 +427,17 @@ class Server:
         progressed = False
         still = []
         for item in self._inflight:
-            items, k, ev, hosts, need, cb = item
+            items, k, ev, hosts, need, cb, heavy = item
             if ev.query():
                 now = time.perf_counter()
                 self.free.append(k)
                 self.inflight_bytes -= need
+                self.heavy_inflight -= heavy
                 if cb is not None:
                     cb.busy = False
                 for (req, fut), host in zip(items, hosts):
                     self.latencies.append(now - req.t_submit)
+                    self.latencies_by_kind.setdefault(req.kind, []).append(now - req.t_submit)
                     self.completed += 1
                     if self.t_first is None or req.t_submit < self.t_first:
                         self.t_first = req.t_submit

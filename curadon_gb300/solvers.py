@@ -29,6 +29,25 @@ def _vol_shape(geom: Geom):
     return tuple(int(v) for v in geom.vol_shape)
 
 
+def _capture(fn, device) -> "torch.cuda.CUDAGraph":
+    """Captures ``fn()`` as a CUDA graph on a side stream that follows the
+    current stream, without synchronising the device (so that a server's
+    other streams keep running while a new solver is captured); capturing
+    does not execute ``fn``'s work."""
+    cur = torch.cuda.current_stream(device)
+    side = torch.cuda.Stream(device)
+    side.wait_stream(cur)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(side):
+        g.capture_begin(capture_error_mode="thread_local")
+        try:
+            fn()
+        finally:
+            g.capture_end()
+    cur.wait_stream(side)
+    return g
+
+
 def _safe_inv(t: torch.Tensor) -> torch.Tensor:
     return torch.where(t > 1e-6, 1.0 / t.clamp_min(1e-6), torch.zeros_like(t))
 
@@ -67,15 +86,8 @@ class SirtSolver:
             self.x.clamp_(min=0.0)
 
     def _capture(self):
-        self._iteration()  # warm-up outside the capture
-        torch.cuda.synchronize(self.x.device)
-        g = torch.cuda.CUDAGraph()
-        s = torch.cuda.Stream(self.x.device)
-        s.wait_stream(torch.cuda.current_stream(self.x.device))
-        with torch.cuda.stream(s), torch.cuda.graph(g, stream=s):
-            self._iteration()
-        torch.cuda.current_stream(self.x.device).wait_stream(s)
-        self._graph = g
+        self._iteration()  # warm-up outside the capture (scratch, texture arrays)
+        self._graph = _capture(self._iteration, self.x.device)
 
     def run(self, y: torch.Tensor, iters: int, x0: Optional[torch.Tensor] = None) -> torch.Tensor:
         if self.use_graph and self._graph is None:
@@ -137,25 +149,16 @@ class CglsSolver:
         self.gamma.copy_(gamma_new)
 
     def _capture(self):
-        g = torch.cuda.CUDAGraph()
-        s = torch.cuda.Stream(self.x.device)
-        s.wait_stream(torch.cuda.current_stream(self.x.device))
-        with torch.cuda.stream(s), torch.cuda.graph(g, stream=s):
-            self._iteration()
-        torch.cuda.current_stream(self.x.device).wait_stream(s)
-        self._graph = g
+        self._graph = _capture(self._iteration, self.x.device)
 
     def run(self, y: torch.Tensor, iters: int, x0: Optional[torch.Tensor] = None) -> torch.Tensor:
         self._start(y, x0)
         if self.use_graph and self._graph is None and iters > 0:
-            # the first iteration runs outside the capture (scratch exists after it)
+            # the first iteration runs outside the capture (scratch exists after
+            # it); capturing does not execute, so the state is unchanged
             self._iteration()
             iters -= 1
-            torch.cuda.synchronize(self.x.device)
-            saved = [t.clone() for t in (self.x, self.p, self.s, self.r, self.q, self.gamma)]
-            self._capture()  # capturing does not execute; state is unchanged
-            for t, v in zip((self.x, self.p, self.s, self.r, self.q, self.gamma), saved):
-                t.copy_(v)
+            self._capture()
         for _ in range(int(iters)):
             if self._graph is not None:
                 self._graph.replay()

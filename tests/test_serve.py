@@ -5,6 +5,8 @@ Each result must be the same alone and in the mix: FBP and SIRT bit for bit
 (deterministic kernels, private per-slot scratch), CGLS within relative L2
 1e-3 (its matched adjoint accumulates with atomics).  The solvers must
 reduce the residual, and CUDA-graph replay must equal direct iterations."""
+import time
+
 import numpy as np
 import pytest
 import torch
@@ -131,3 +133,25 @@ def test_waiting_2d_requests_are_coalesced(cuda_device):
     assert srv.batches_run < len(reqs)
     for i, (out, ref) in enumerate(zip(outs, alone)):
         assert torch.equal(out, ref), i
+
+
+def test_3d_requests_leave_slots_for_2d(cuda_device):
+    """With the 3D lane full (heavy_slots 1), a 2D request submitted after
+    several 3D requests is admitted before the later 3D ones and finishes
+    first; every result still equals the request solved alone."""
+    cones = [cone_request(64, 90, 96, 50 + k, cuda_device, iters=12) for k in range(3)]
+    fan = fan_request("fbp", 128, 90, 60, cuda_device)
+    alone = [solve_alone(r, cuda_device.index or 0).cpu() for r in cones + [fan]]
+    srv = Server(device=cuda_device.index or 0, slots=4, heavy_slots=1)
+    done = {}
+    futs = [srv.submit(r) for r in cones] + [srv.submit(fan)]
+    for i, f in enumerate(futs):
+        f.add_done_callback(lambda _f, i=i: done.setdefault(i, time.perf_counter()))
+    outs = [f.result(timeout=120) for f in futs]
+    srv.close()
+    assert done[3] < done[1] and done[3] < done[2], done
+    for i, (out, ref) in enumerate(zip(outs, alone)):
+        if i < 3:
+            assert rel_l2(out, ref) < 1e-3
+        else:
+            assert torch.equal(out, ref)

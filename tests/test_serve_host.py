@@ -52,3 +52,12 @@ def test_coalescing_classes():
     assert _class_key(req("fbp", small)) != _class_key(req("fbp", small, filt="hann"))
     # FBP ignores the iteration count
     assert _class_key(req("fbp", small, 0)) == _class_key(req("fbp", small, 20))
+
+
+def test_heavy_requests_are_the_3d_ones():
+    from curadon_gb300.serve import _heavy
+
+    fan = FanGeometry(**fan_config(2048, 90))
+    cone = ConeGeometry(**cone_config(32, 20, 48))
+    assert _heavy(Request("cgls", cone, torch.zeros(cone.sinogram_shape())))
+    assert not _heavy(Request("sirt", fan, torch.zeros(fan.sinogram_shape())))
