@@ -23,7 +23,6 @@
 // from different threads -- race on the array and must be ordered by the
 // caller.
 #include <cmath>
-#include <mutex>
 #include <string>
 
 #include "common.cuh"
@@ -35,22 +34,13 @@ namespace {
 constexpr size_t kStaticScratchBytes = size_t(16) << 20;
 __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mutex;
-void *g_scratch_addr[kMaxDevices] = {};
-
-// Device address of g_static_scratch on the current device.
+// Device address of g_static_scratch in the current context, looked up on
+// every call (a lookup allocates nothing, and an address kept from an
+// earlier context would be stale after cudaDeviceReset).
 int static_scratch(void **out) {
-    int dev = 0;
-    CG_TRY_CUDA(cudaGetDevice(&dev));
-    CG_REQUIRE(dev >= 0 && dev < kMaxDevices, "device index beyond the static scratch table");
-    std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        CG_TRY_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
-        g_scratch_addr[dev] = p;
-    }
-    *out = g_scratch_addr[dev];
+    void *p = nullptr;
+    CG_TRY_CUDA(cudaGetSymbolAddress(&p, g_static_scratch));
+    *out = p;
     return CG_OK;
 }
 

@@ -248,12 +248,11 @@ int cg_backward_3d(float *x, const uint64_t vol_shape[3], const float vol_spacin
  * `volume`; all scratch lives in one 16 MiB device array that the library
  * holds on every GPU that loads it.  A call needs at most
  * 8 * nangles * (det_count + 4) + 84 * nangles + 2040 bytes of it; larger
- * problems are rejected with CG_ERR_INVALID.  The first call on a device
- * looks the array's device address up and keeps it for the life of the
- * device's context (make that first call before any stream capture; after a
- * cudaDeviceReset the kept address is stale, so do not call this again in
- * that process).  All calls share the array: calls that overlap on the GPU
- * race and must be ordered by the caller. */
+ * problems are rejected with CG_ERR_INVALID.  Each call looks the array's
+ * device address up in the current context and copies `angles`, `DSO` and
+ * `DSD` from (pageable) host memory with cudaMemcpyAsync on `stream`, so a
+ * call cannot be captured into a CUDA graph.  All calls share the array:
+ * calls that overlap on the GPU race and must be ordered by the caller. */
 int cg_backward_2d_static(float *volume, const float *sinogram, const uint64_t vol_shape[2],
                           const float vol_spacing[2], const float vol_offset[2],
                           uint64_t det_count, float det_spacing, const float *DSO,
