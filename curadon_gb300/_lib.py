@@ -69,6 +69,13 @@ SIGNATURES = [
     ("cg_batch2d_set_active", C.c_int, [C.c_void_p, C.c_int]),
     ("cg_batch2d_set_forward", C.c_int, [C.c_void_p, C.c_int]),
     ("cg_batch2d_get_forward", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    ("cg_batch3d_create", C.c_int,
+     [C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+      C.POINTER(C.c_void_p), C.c_int]),
+    ("cg_batch3d_destroy", C.c_int, [C.c_void_p]),
+    ("cg_batch3d_forward", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("cg_batch3d_backward", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("cg_batch3d_set_active", C.c_int, [C.c_void_p, C.c_int]),
 ]
 
 CG_OK, CG_ERR_INVALID, CG_ERR_CUDA, CG_ERR_NOMEM, CG_ERR_UNSUPPORTED = range(5)

@@ -1,4 +1,4 @@
-"""Many 2D problems per launch (``cg_batch2d_*``).
+"""Many 2D and 3D problems per launch (``cg_batch2d_*``, ``cg_batch3d_*``).
 
 ``Batch2d(geoms, volumes, sinograms)`` binds any number of fan-beam problems
 -- any sizes, circular or vector geometries -- to their float32 CUDA
@@ -18,8 +18,11 @@ afterwards).  The backprojection is the staged one; results equal the
 single-problem operators with those algorithms bit for bit; ``adjoint()``
 adds the matched adjoint (the exact transpose of the register forward).
 ``BatchProjector`` wraps a batch as a differentiable PyTorch function over
-flat buffers.  No counterpart in the reference, which runs one problem per
-call.
+flat buffers.  ``Batch3d`` does the same for cone-beam problems (any volume
+and detector sizes, views and geometries): the quad forward with each
+plan's texture warps and the axial or general backprojection, bit-equal to
+the single-problem operators.  No counterpart in the reference, which runs
+one problem per call.
 """
 from __future__ import annotations
 
@@ -31,9 +34,38 @@ import torch
 
 from ._lib import check, load
 from .backend import _check_tensor, _stream
-from .geometry import FanGeometry
+from .geometry import ConeGeometry, FanGeometry
 
-__all__ = ["Batch2d", "BatchProjector"]
+__all__ = ["Batch2d", "Batch3d", "BatchProjector"]
+
+
+def _bind_plans(geoms, volumes, sinograms, kind, ndim):
+    """The plans of a batch's problems after checking its tensors; a
+    geometry used twice gets a private plan for its second use (each
+    problem needs its own plan scratch)."""
+    if not (len(geoms) == len(volumes) == len(sinograms)) or not geoms:
+        raise ValueError("geoms, volumes and sinograms must be non-empty and of one length")
+    dev = volumes[0].device
+    plans, seen = [], set()
+    for g, v, s in zip(geoms, volumes, sinograms):
+        if not isinstance(g, kind):
+            raise TypeError(f"batches hold {kind.__name__} problems")
+        _check_tensor(v, "volume", ndim)
+        _check_tensor(s, "sinogram", ndim)
+        if v.device != dev or s.device != dev:
+            raise AttributeError("all tensors of a batch must be on one device")
+        if tuple(v.shape) != tuple(int(x) for x in g.vol_shape):
+            raise ValueError(f"volume shape {tuple(v.shape)} != geometry {tuple(g.vol_shape)}")
+        if tuple(s.shape) != tuple(g.sinogram_shape()):
+            raise ValueError(f"sinogram shape {tuple(s.shape)} != {tuple(g.sinogram_shape())}")
+        p = g.plan if id(g) not in seen else g._make_plan()
+        seen.add(id(g))
+        plans.append(p)
+    return plans, dev
+
+
+def _pointers(objs):
+    return (C.c_void_p * len(objs))(*objs)
 
 
 class Batch2d:
@@ -43,33 +75,14 @@ class Batch2d:
                  sinograms: Sequence[torch.Tensor], forward: str = "texture"):
         if forward not in self.FORWARD + ("auto",):
             raise ValueError(f"batched forward must be one of {self.FORWARD + ('auto',)}")
-        if not (len(geoms) == len(volumes) == len(sinograms)) or not geoms:
-            raise ValueError("geoms, volumes and sinograms must be non-empty and of one length")
-        dev = volumes[0].device
-        plans, seen = [], set()
-        for g, v, s in zip(geoms, volumes, sinograms):
-            if not isinstance(g, FanGeometry):
-                raise TypeError("batches hold FanGeometry problems")
-            _check_tensor(v, "volume", 2)
-            _check_tensor(s, "sinogram", 2)
-            if v.device != dev or s.device != dev:
-                raise AttributeError("all tensors of a batch must be on one device")
-            if tuple(v.shape) != tuple(int(x) for x in g.vol_shape):
-                raise ValueError(f"volume shape {tuple(v.shape)} != geometry {tuple(g.vol_shape)}")
-            if tuple(s.shape) != g.sinogram_shape():
-                raise ValueError(f"sinogram shape {tuple(s.shape)} != {g.sinogram_shape()}")
-            # each problem needs its own plan scratch: a geometry used twice
-            # gets a private plan for its second use
-            p = g.plan if id(g) not in seen else g._make_plan()
-            seen.add(id(g))
-            plans.append(p)
+        plans, dev = _bind_plans(geoms, volumes, sinograms, FanGeometry, 2)
         self._L = load()
         n = len(plans)
-        hp = (C.c_void_p * n)(*[p.handle.value for p in plans])
-        vp = (C.c_void_p * n)(*[v.data_ptr() for v in volumes])
-        sp = (C.c_void_p * n)(*[s.data_ptr() for s in sinograms])
         h = C.c_void_p()
-        check(self._L.cg_batch2d_create(C.byref(h), hp, vp, sp, n))
+        check(self._L.cg_batch2d_create(
+            C.byref(h), _pointers([p.handle.value for p in plans]),
+            _pointers([v.data_ptr() for v in volumes]),
+            _pointers([s.data_ptr() for s in sinograms]), n))
         self._h = h
         self._keep = (list(geoms), list(volumes), list(sinograms), plans)
         self.device = dev
@@ -139,6 +152,51 @@ class Batch2d:
         check(self._L.cg_batch2d_adjoint(self._h, _stream(self._keep[1][0])))
 
 
+class Batch3d:
+    """Cone-beam problems bound to their float32 CUDA volumes and projections
+    (``cg_batch3d_*``).  ``forward()`` projects every volume (the quad ray
+    march with each plan's texture warps; as the single-problem forward, it
+    writes only the rays that hit the volume's box) and ``backward()`` adds
+    every backprojection into its volume (axial runs where the geometry
+    allows them, the general kernel otherwise), each over a (problem, tile)
+    work list in a few launches; results equal ``plan.forward`` /
+    ``plan.backward`` bit for bit (plans set to the "registers" or "texture"
+    forward run the "quad" forward here).  Binding allocates each plan's
+    quad copies.  Capturable in a CUDA graph."""
+
+    def __init__(self, geoms: Sequence[ConeGeometry], volumes: Sequence[torch.Tensor],
+                 sinograms: Sequence[torch.Tensor]):
+        plans, dev = _bind_plans(geoms, volumes, sinograms, ConeGeometry, 3)
+        self._L = load()
+        h = C.c_void_p()
+        check(self._L.cg_batch3d_create(
+            C.byref(h), _pointers([p.handle.value for p in plans]),
+            _pointers([v.data_ptr() for v in volumes]),
+            _pointers([s.data_ptr() for s in sinograms]), len(plans)))
+        self._h = h
+        self._keep = (list(geoms), list(volumes), list(sinograms), plans)
+        self.device = dev
+        self.count = len(plans)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._L.cg_batch3d_destroy(h)
+            self._h = None
+
+    def forward(self):
+        """projections_i = A_i volume_i for every problem (on the current stream)."""
+        check(self._L.cg_batch3d_forward(self._h, _stream(self._keep[1][0])))
+
+    def backward(self):
+        """volume_i += A_i^T projections_i for every problem."""
+        check(self._L.cg_batch3d_backward(self._h, _stream(self._keep[1][0])))
+
+    def set_active(self, active: int):
+        """Later calls run problems [0, active) only."""
+        check(self._L.cg_batch3d_set_active(self._h, int(active)))
+
+
 class _BatchProject(torch.autograd.Function):
     """s = A x over a whole batch, x and s flat (every problem's volume, then
     every problem's sinogram, concatenated); the backward is the batched
@@ -147,6 +205,8 @@ class _BatchProject(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, proj):
         proj.X.copy_(x)
+        if proj.cone:
+            proj.S.zero_()  # the 3D forward writes only the rays that hit the box
         proj._fwd.forward()
         ctx.proj = proj
         return proj.S.clone()
@@ -173,13 +233,18 @@ class BatchProjector:
     backprojector, python/standalone/src/curadon/diffable.py:14-38) or, with
     ``matched=True``, the batched matched adjoint, the exact transpose of the
     register forward that ``matched`` selects.  Both directions are a few
-    launches for the whole batch, capturable in a CUDA graph."""
+    launches for the whole batch, capturable in a CUDA graph.  A list of
+    ``ConeGeometry`` problems makes a 3D batch (``Batch3d``; its gradient is
+    the batched backprojection, there is no batched 3D matched adjoint)."""
 
-    def __init__(self, geoms: Sequence[FanGeometry], device=None, forward: str = "plans",
-                 matched: bool = False):
+    def __init__(self, geoms: Sequence[FanGeometry | ConeGeometry], device=None,
+                 forward: str = "plans", matched: bool = False):
         dev = torch.device("cuda", 0) if device is None else torch.device(device)
         self.geoms = list(geoms)
         self.matched = bool(matched)
+        self.cone = bool(self.geoms) and isinstance(self.geoms[0], ConeGeometry)
+        if self.cone and self.matched:
+            raise ValueError("3D batches have no matched adjoint (use matched=False)")
         self.vol_shapes = [tuple(int(v) for v in g.vol_shape) for g in self.geoms]
         self.sino_shapes = [tuple(g.sinogram_shape()) for g in self.geoms]
         nv = [int(np.prod(s)) for s in self.vol_shapes]
@@ -190,9 +255,17 @@ class BatchProjector:
         self.G = torch.zeros_like(self.X)
         self.S = torch.zeros(int(self.sino_offsets[-1]), device=dev)
         self.R = torch.zeros_like(self.S)
-        self._fwd = Batch2d(self.geoms, self.split_volumes(self.X), self.split_sinograms(self.S),
-                            forward="registers" if self.matched else forward)
-        self._bwd = Batch2d(self.geoms, self.split_volumes(self.G), self.split_sinograms(self.R))
+        if self.cone:
+            self._fwd = Batch3d(self.geoms, self.split_volumes(self.X),
+                                self.split_sinograms(self.S))
+            self._bwd = Batch3d(self.geoms, self.split_volumes(self.G),
+                                self.split_sinograms(self.R))
+        else:
+            self._fwd = Batch2d(self.geoms, self.split_volumes(self.X),
+                                self.split_sinograms(self.S),
+                                forward="registers" if self.matched else forward)
+            self._bwd = Batch2d(self.geoms, self.split_volumes(self.G),
+                                self.split_sinograms(self.R))
         self.device = dev
 
     def split_volumes(self, flat: torch.Tensor):

@@ -47,6 +47,26 @@ struct cg_batch2d {
     }
 };
 
+// A 3D batch: the quad forward (with each plan's texture warps) and the
+// backprojection (axial runs where the plan takes them, else the general
+// kernel on row-pair quads) of every problem over one work list.
+struct cg_batch3d {
+    int device = 0;
+    int count = 0;
+    int active = 0;
+    std::vector<cg::Plan3d *> plans;
+    std::vector<cg::Prob3d> probs;
+    cg::Prob3d *d_probs = nullptr;
+    int *d_starts = nullptr;  // kBatch3dStages stages x (count + 1)
+    std::vector<int> starts;
+    float *d_ax = nullptr;  // axial view tables of every problem
+
+    void active_totals(int out[cg::kBatch3dStages]) const {
+        for (int st = 0; st < cg::kBatch3dStages; ++st)
+            out[st] = starts[st * (count + 1) + active];
+    }
+};
+
 using namespace cg;
 
 namespace {
@@ -54,6 +74,16 @@ namespace {
 void free_batch(cg_batch2d *b) {
     if (b->d_probs) cudaFree(b->d_probs);
     if (b->d_starts) cudaFree(b->d_starts);
+}
+
+// floats of a problem's axial view tables (10 per view), rounded up so that
+// every problem's float4 tables start on 16 bytes
+size_t ax_stride(const Plan3d &p) { return ((size_t)p.nangles * 10 + 3) & ~size_t(3); }
+
+void free_batch3d(cg_batch3d *b) {
+    if (b->d_probs) cudaFree(b->d_probs);
+    if (b->d_starts) cudaFree(b->d_starts);
+    if (b->d_ax) cudaFree(b->d_ax);
 }
 
 }  // namespace
@@ -216,6 +246,119 @@ int cg_batch2d_backward(cg_batch2d *batch, void *stream) {
     batch->active_totals(totals);
     return launch_batch2d(batch->d_probs, batch->d_starts, totals, batch->count, false,
                           (cudaStream_t)stream);
+}
+
+int cg_batch3d_create(cg_batch3d **batch, cg_plan3d *const *plans, float *const *volumes,
+                      float *const *sinograms, int count) {
+    clear_error();
+    CG_REQUIRE(batch, "batch output pointer is NULL");
+    *batch = nullptr;
+    CG_REQUIRE(plans && volumes && sinograms, "plan, volume and sinogram lists must be given");
+    CG_REQUIRE(count > 0 && count <= (1 << 20), "count out of range");
+    std::set<const cg_plan3d *> seen;
+    size_t ax_floats = 0;
+    for (int i = 0; i < count; ++i) {
+        CG_REQUIRE(plans[i] && volumes[i] && sinograms[i], "NULL plan or buffer in the batch");
+        CG_REQUIRE(plans[i]->device == plans[0]->device, "all plans of a batch share one device");
+        CG_REQUIRE(seen.insert(plans[i]).second, "a plan appears twice in one batch");
+        ax_floats += ax_stride(*plans[i]);
+    }
+    DeviceGuard guard(plans[0]->device);
+    CG_REQUIRE(guard.ok(), "cannot select the plans' device");
+
+    std::unique_ptr<cg_batch3d> b(new cg_batch3d());
+    b->device = plans[0]->device;
+    b->count = count;
+    b->active = count;
+    b->plans.assign(plans, plans + count);
+    auto fail = [&](cudaError_t e) {
+        free_batch3d(b.get());
+        return set_error(e == cudaErrorMemoryAllocation ? CG_ERR_NOMEM : CG_ERR_CUDA,
+                         std::string("batch set-up: ") + cudaGetErrorString(e));
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&b->d_ax, ax_floats * sizeof(float))) != cudaSuccess) return fail(e);
+    std::vector<Prob3d> probs(count);
+    std::vector<int> starts(kBatch3dStages * (count + 1), 0);
+    long long totals[kBatch3dStages] = {};
+    size_t ax_off = 0;
+    for (int i = 0; i < count; ++i) {
+        int blocks[kBatch3dStages];
+        if (int rc = bind_batch3d_problem(*plans[i], volumes[i], sinograms[i], b->d_ax + ax_off,
+                                          &probs[i], blocks)) {
+            free_batch3d(b.get());
+            return rc;
+        }
+        ax_off += ax_stride(*plans[i]);
+        for (int st = 0; st < kBatch3dStages; ++st) {
+            starts[st * (count + 1) + i] = (int)totals[st];
+            totals[st] += blocks[st];
+            starts[st * (count + 1) + i + 1] = (int)totals[st];
+        }
+    }
+    for (long long t : totals)
+        if (t >= (1ll << 31)) {
+            free_batch3d(b.get());
+            return set_error(CG_ERR_INVALID, "batch too large for one launch");
+        }
+    b->probs = probs;
+    b->starts = starts;
+    if ((e = cudaMalloc(&b->d_probs, sizeof(Prob3d) * count)) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&b->d_starts, sizeof(int) * starts.size())) != cudaSuccess) return fail(e);
+    if ((e = cudaMemcpy(b->d_probs, probs.data(), sizeof(Prob3d) * count,
+                        cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail(e);
+    if ((e = cudaMemcpy(b->d_starts, starts.data(), sizeof(int) * starts.size(),
+                        cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail(e);
+    *batch = b.release();
+    return CG_OK;
+}
+
+int cg_batch3d_destroy(cg_batch3d *batch) {
+    clear_error();
+    if (!batch) return CG_OK;
+    {
+        DeviceGuard guard(batch->device);
+        free_batch3d(batch);
+    }
+    delete batch;
+    return CG_OK;
+}
+
+int cg_batch3d_set_active(cg_batch3d *batch, int active) {
+    clear_error();
+    CG_REQUIRE(batch, "batch is NULL");
+    CG_REQUIRE(active > 0 && active <= batch->count, "active count must be in [1, count]");
+    batch->active = active;
+    return CG_OK;
+}
+
+int cg_batch3d_forward(cg_batch3d *batch, void *stream) {
+    clear_error();
+    CG_REQUIRE(batch, "batch is NULL");
+    DeviceGuard guard(batch->device);
+    CG_REQUIRE(guard.ok(), "cannot select the batch's device");
+    const cudaStream_t s = (cudaStream_t)stream;
+    // the texture warps' volumes into their plans' arrays, then the work list
+    for (int i = 0; i < batch->active; ++i)
+        if (batch->probs[i].tex_warps > 0)
+            if (int rc = upload_volume_texture3(*batch->plans[i], batch->probs[i].vol, s))
+                return rc;
+    int totals[kBatch3dStages];
+    batch->active_totals(totals);
+    return launch_batch3d_forward(batch->d_probs, batch->d_starts, totals, batch->count, s);
+}
+
+int cg_batch3d_backward(cg_batch3d *batch, void *stream) {
+    clear_error();
+    CG_REQUIRE(batch, "batch is NULL");
+    DeviceGuard guard(batch->device);
+    CG_REQUIRE(guard.ok(), "cannot select the batch's device");
+    int totals[kBatch3dStages];
+    batch->active_totals(totals);
+    return launch_batch3d_backward(batch->d_probs, batch->d_starts, totals, batch->count,
+                                   (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -153,6 +153,33 @@ __device__ __forceinline__ int batch_problem(const int *__restrict__ start, int 
     }
     return lo;
 }
+// One problem of a 3D batch as the batched kernels see it (a bound plan's
+// buffers and tables).
+struct Prob3d {
+    float *vol;   // volume: forward input, backprojection accumulator
+    float *sino;  // projections: forward output, backprojection input
+    // forward: the plan's quad copies and tables; texture warps per block
+    float4 *QA, *QB;
+    const float4 *forg, *fdu, *fdv, *fsrc;
+    cudaTextureObject_t tex;
+    int tex_warps, exact_t;
+    int X, Y, Z, U, V, P, utiles;
+    // backprojection: the re-laid projections (quads of rows v, v + 1)
+    float4 *sinoQ;
+    int axial;  // runs along y (k_bwd3d_ax) or the general kernel
+    // axial: per-view tables (p0, p1, p2 as the kernel parameter holds them)
+    // and the constant terms; general: the plan's tables and source
+    const float4 *ax0, *ax1;
+    const float2 *ax2;
+    float num, su, sv;
+    const float4 *borg, *bdx, *bdy, *bdz;
+    float bsx, bsy, bsz, zplane, hu, hv;
+    int tiles_x, tiles_y, tiles_z;
+};
+// 3D batch stages: the two volume quad re-layouts, the forward, the
+// projections' re-layout, the axial and the general backprojection
+constexpr int kBatch3dStages = 6;
+
 // Batched stages: re-layout, forward, sinogram re-layout, backprojection,
 // the matched adjoint's zeroing, scatter and fold, and the "plans" forward's
 // absolute-position re-layout and chunked bundles (chunked problems) and
@@ -305,6 +332,19 @@ int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t
 // texture forward (tex3D, the reference's trilinear sampling)
 int launch_forward3d_tex(Plan3d &p, const float *vol, float *sino, cudaStream_t s);
 int upload_volume_texture3(Plan3d &p, const float *vol, cudaStream_t s);
+// the plan's 3D texture array and object, without a copy
+int ensure_volume_texture3(Plan3d &p);
+
+// 3D batches (proj3d.cu): a plan bound as a batch problem (its quad scratch
+// allocated; `ax` holds 10 floats of device memory per view for the axial
+// tables), each stage's blocks, and the two directions over the first
+// problems whose blocks are the totals
+int bind_batch3d_problem(Plan3d &p, float *vol, float *sino, float *ax, Prob3d *q,
+                         int blocks[kBatch3dStages]);
+int launch_batch3d_forward(const Prob3d *d_probs, const int *starts,
+                           const int totals[kBatch3dStages], int count, cudaStream_t s);
+int launch_batch3d_backward(const Prob3d *d_probs, const int *starts,
+                            const int totals[kBatch3dStages], int count, cudaStream_t s);
 
 // Reads CURADON_GB300_ALGO ("fwd2d=tex,bwd2d=smem,fwd3d=tex2l,...") over the
 // defaults of a new plan.

@@ -13,6 +13,7 @@
 #include <climits>
 
 #include <algorithm>
+#include <vector>
 
 #include "common.cuh"
 
@@ -76,10 +77,9 @@ __global__ void __launch_bounds__(256)
 // and kP3 + 1 above (kQP in all), so the samples of a ray inside the box
 // [-1, N + 1]^3 and their slice c + 1 stay inside the array.
 // QA: slices z, rows y, columns x.
-__global__ void k_relayout3d_qa(const float *__restrict__ vol, int X, int Y, int Z,
-                                float4 *__restrict__ QA) {
+__device__ __forceinline__ void relayout3d_qa_at(const float *__restrict__ vol, int X, int Y,
+                                                 int Z, float4 *__restrict__ QA, long long idx) {
     const int PX = X + kQP, PY = Y + kQP, PZ = Z + kQP;
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)PX * PY * PZ) return;
     const int x = (int)(idx % PX) - kP3;
     const long long r = idx / PX;
@@ -97,13 +97,20 @@ __global__ void k_relayout3d_qa(const float *__restrict__ vol, int X, int Y, int
     QA[idx] = make_float4(v[0][0], b, v[1][0] - v[0][0], (v[1][1] - v[1][0]) - b);
 }
 
+__global__ void k_relayout3d_qa(const float *__restrict__ vol, int X, int Y, int Z,
+                                float4 *__restrict__ QA) {
+    relayout3d_qa_at(vol, X, Y, Z, QA, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // QB: slices x, rows y, columns z; an x <-> z transpose of the rows y, y + 1
 // through shared memory, 32 x 32 (x, z) tiles.
-__global__ void __launch_bounds__(256)
-    k_relayout3d_qb(const float *__restrict__ vol, int X, int Y, int Z, float4 *__restrict__ QB) {
+// One 32 x 32 (z, x) tile (ta, tc) of row b; a block of 32 x 8 threads.
+__device__ __forceinline__ void relayout3d_qb_tile(const float *__restrict__ vol, int X, int Y,
+                                                   int Z, float4 *__restrict__ QB, int ta, int tc,
+                                                   int b) {
     __shared__ float tile[2][33][33];  // [row][z][x]
     const int PX = X + kQP, PY = Y + kQP, PZ = Z + kQP;
-    const int a0 = blockIdx.x * 32, c0 = blockIdx.y * 32, b = blockIdx.z;
+    const int a0 = ta * 32, c0 = tc * 32;
     const int z0 = a0 - kP3, x0 = c0 - kP3, y = b - kP3;
     for (int j = threadIdx.y; j < 33; j += blockDim.y)
         for (int i = 0; i < 2; ++i) {
@@ -122,6 +129,11 @@ __global__ void __launch_bounds__(256)
         const float bb = v01 - v00;
         QB[((size_t)c * PY + b) * PZ + a] = make_float4(v00, bb, v10 - v00, (v11 - v10) - bb);
     }
+}
+
+__global__ void __launch_bounds__(256)
+    k_relayout3d_qb(const float *__restrict__ vol, int X, int Y, int Z, float4 *__restrict__ QB) {
+    relayout3d_qb_tile(vol, X, Y, Z, QB, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 
@@ -145,10 +157,10 @@ __global__ void k_relayout_sino3d(const float *__restrict__ sino, int U, int V, 
 
 // The same layout with rows b and b + 1 in one float4 (pair of row b, pair
 // of row b + 1), so a bilinear sample is one 16-byte load.
-__global__ void k_relayout_sino3d_quad(const float *__restrict__ sino, int U, int V, int nangles,
-                                       float4 *__restrict__ S) {
+__device__ __forceinline__ void relayout_sino3d_quad_at(const float *__restrict__ sino, int U, int V,
+                                                   int nangles, float4 *__restrict__ S,
+                                                   long long idx) {
     const int PU = U + 2 * kP3, PV = V + 2 * kP3;
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)PU * PV * nangles) return;
     const int a = (int)(idx % PU) - kP3;
     const long long r = idx / PU;
@@ -165,14 +177,19 @@ __global__ void k_relayout_sino3d_quad(const float *__restrict__ sino, int U, in
     S[idx] = make_float4(t[0], t[1] - t[0], t[2], t[3] - t[2]);
 }
 
+__global__ void k_relayout_sino3d_quad(const float *__restrict__ sino, int U, int V, int nangles,
+                                       float4 *__restrict__ S) {
+    relayout_sino3d_quad_at(sino, U, V, nangles, S, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // Double-difference quads for the axial backprojector: element (b, a) holds
 // s00, s01 - s00, s10 - s00 and (s11 - s10) - (s01 - s00) of the cells
 // (row b, b + 1) x (column a, a + 1), zero outside the detector, so the
 // bilinear value at fractions (wu, wv) is s00 + wu B + wv (C + wu D).
-__global__ void k_relayout_sino3d_qd(const float *__restrict__ sino, int U, int V, int nangles,
-                                     float4 *__restrict__ S) {
+__device__ __forceinline__ void relayout_sino3d_qd_at(const float *__restrict__ sino, int U, int V,
+                                                   int nangles, float4 *__restrict__ S,
+                                                   long long idx) {
     const int PU = U + 2 * kP3, PV = V + 2 * kP3;
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)PU * PV * nangles) return;
     const int a = (int)(idx % PU) - kP3;
     const long long r = idx / PU;
@@ -187,6 +204,11 @@ __global__ void k_relayout_sino3d_qd(const float *__restrict__ sino, int U, int 
         if (a + 1 >= 0 && a + 1 < U) t[2 * k + 1] = row[a + 1];
     }
     S[idx] = make_float4(t[0], t[1] - t[0], t[2] - t[0], (t[3] - t[2]) - (t[1] - t[0]));
+}
+
+__global__ void k_relayout_sino3d_qd(const float *__restrict__ sino, int U, int V, int nangles,
+                                     float4 *__restrict__ S) {
+    relayout_sino3d_qd_at(sino, U, V, nangles, S, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // ------------------------------------------------------------ forward
@@ -343,14 +365,14 @@ __device__ __forceinline__ Ray3 setup_ray3(const float4 o, const float4 du, cons
 // lies past tmax, at an offset clamped into the array, and are then
 // dropped).  -2 % at 256^3, -0.7 % at 512^3 (the texture warps gain; the
 // quads alone do not change; four fetches per iteration: no better).
+// Block `lin` of the launch order above (the batched forward passes each
+// problem's own block index).
 template <int UNR>
-__global__ void __launch_bounds__(256)
-    k_fwd3d_quad(const float4 *__restrict__ QA, const float4 *__restrict__ QB,
-                 float *__restrict__ sino, const float4 *__restrict__ torg,
-                 const float4 *__restrict__ tdu, const float4 *__restrict__ tdv,
-                 const float4 *__restrict__ tsrc, int X, int Y, int Z, int U, int V, int P,
-                 int utiles, cudaTextureObject_t tex, int tex_warps, bool exact_t) {
-    const int lin = blockIdx.x;
+__device__ __forceinline__ void fwd3d_quad_block(
+    const float4 *__restrict__ QA, const float4 *__restrict__ QB, float *__restrict__ sino,
+    const float4 *__restrict__ torg, const float4 *__restrict__ tdu,
+    const float4 *__restrict__ tdv, const float4 *__restrict__ tsrc, int X, int Y, int Z, int U,
+    int V, int P, int utiles, cudaTextureObject_t tex, int tex_warps, bool exact_t, int lin) {
     const int ut = lin % utiles, rest = lin / utiles;
     const int view = rest % P, band = rest / P;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -449,6 +471,17 @@ __global__ void __launch_bounds__(256)
     sino[((size_t)view * V + iv) * U + iu] = acc;
 }
 
+template <int UNR>
+__global__ void __launch_bounds__(256)
+    k_fwd3d_quad(const float4 *__restrict__ QA, const float4 *__restrict__ QB,
+                 float *__restrict__ sino, const float4 *__restrict__ torg,
+                 const float4 *__restrict__ tdu, const float4 *__restrict__ tdv,
+                 const float4 *__restrict__ tsrc, int X, int Y, int Z, int U, int V, int P,
+                 int utiles, cudaTextureObject_t tex, int tex_warps, bool exact_t) {
+    fwd3d_quad_block<UNR>(QA, QB, sino, torg, tdu, tdv, tsrc, X, Y, Z, U, V, P, utiles, tex,
+                          tex_warps, exact_t, blockIdx.x);
+}
+
 // ------------------------------------------------------------ backward
 
 constexpr int kBZ = 8;         // voxels per thread along z
@@ -469,20 +502,19 @@ struct BwdTab {
 // stepped along z from the run's first voxel -- then a bilinear sample of the
 // difference-encoded pair-packed projection in two 8-byte loads and three
 // FMAs, accumulated in registers; the volume is read and written once.
-template <bool PK, bool MAGIC = false, bool QS = false>
-__global__ void __launch_bounds__(256)
-    k_bwd3d(float *__restrict__ vol, const void *__restrict__ Sv,
-            const float4 *__restrict__ torg, const float4 *__restrict__ tdx,
-            const float4 *__restrict__ tdy, const float4 *__restrict__ tdz, float srcx,
-            float srcy, float srcz, float zplane, float hu, float hv, int X, int Y, int Z, int U,
-            int V, int nangles, int tiles_x, int tiles_y, int tiles_z) {
+template <bool PK, bool MAGIC, bool QS>
+__device__ __forceinline__ void bwd3d_block(
+    float *__restrict__ vol, const void *__restrict__ Sv, const float4 *__restrict__ torg,
+    const float4 *__restrict__ tdx, const float4 *__restrict__ tdy,
+    const float4 *__restrict__ tdz, float srcx, float srcy, float srcz, float zplane, float hu,
+    float hv, int X, int Y, int Z, int U, int V, int nangles, int tiles_x, int tiles_y,
+    int tiles_z, int lin) {
     __shared__ BwdTab stab[kBViews];
     const float2 *S = static_cast<const float2 *>(Sv);
     const float4 *SQ = static_cast<const float4 *>(Sv);  // QS: row-pair quads
     // brick-ordered tile index
     constexpr int BX = 2, BY = 8, BZ = 8;
     const int bricks_x = (tiles_x + BX - 1) / BX, bricks_y = (tiles_y + BY - 1) / BY;
-    const int lin = blockIdx.x;
     const int brick = lin / (BX * BY * BZ), in = lin % (BX * BY * BZ);
     const int bx = brick % bricks_x, by = (brick / bricks_x) % bricks_y,
               bz = brick / (bricks_x * bricks_y);
@@ -611,6 +643,17 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+template <bool PK, bool MAGIC = false, bool QS = false>
+__global__ void __launch_bounds__(256)
+    k_bwd3d(float *__restrict__ vol, const void *__restrict__ Sv,
+            const float4 *__restrict__ torg, const float4 *__restrict__ tdx,
+            const float4 *__restrict__ tdy, const float4 *__restrict__ tdz, float srcx,
+            float srcy, float srcz, float zplane, float hu, float hv, int X, int Y, int Z, int U,
+            int V, int nangles, int tiles_x, int tiles_y, int tiles_z) {
+    bwd3d_block<PK, MAGIC, QS>(vol, Sv, torg, tdx, tdy, tdz, srcx, srcy, srcz, zplane, hu, hv, X,
+                               Y, Z, U, V, nangles, tiles_x, tiles_y, tiles_z, blockIdx.x);
+}
+
 // Views per launch of k_bwd3d_ax: their tables travel as a 30 KB kernel
 // parameter (the limit is 32 KB).
 constexpr int kAxViews = 768;
@@ -637,14 +680,16 @@ struct AxViewParams {
 // write-back path, which the projection loads saturate (-9 % against
 // staging them in shared memory).  Same ray/plane intersection as the
 // reference (backward_3d.hpp:78-94).
-template <int RUN, int MINB>
-__global__ void __launch_bounds__(256, MINB)
-    k_bwd3d_ax(float *__restrict__ vol, const float4 *__restrict__ SQ,
-                const __grid_constant__ AxViewParams tab, int nv, float num, float su, float sv,
-                int X, int Y, int Z, int U, int V, int tiles_x, int tiles_y, int tiles_z) {
+// Block `lin` of the brick order over views [0, nv): tab(j) gives view j's
+// (p0, p1, p2), from the kernel parameter or (batched) from device memory.
+template <int RUN, class Tab>
+__device__ __forceinline__ void bwd3d_ax_block(float *__restrict__ vol,
+                                               const float4 *__restrict__ SQ, const Tab &tab,
+                                               int nv, float num, float su, float sv, int X,
+                                               int Y, int Z, int U, int V, int tiles_x,
+                                               int tiles_y, int tiles_z, int lin) {
     constexpr int BX = 2, BY = 8, BZ = 8;
     const int bricks_x = (tiles_x + BX - 1) / BX, bricks_y = (tiles_y + BY - 1) / BY;
-    const int lin = blockIdx.x;
     const int brick = lin / (BX * BY * BZ), in = lin % (BX * BY * BZ);
     const int bx = brick % bricks_x, by = (brick / bricks_x) % bricks_y,
               bz = brick / (bricks_x * bricks_y);
@@ -671,8 +716,9 @@ __global__ void __launch_bounds__(256, MINB)
 
     const float4 *plane = SQ;
     for (int j = 0; j < nv; ++j, plane += plane_elems) {
-        const float4 p0 = tab.p0[j], p1 = tab.p1[j];
-        const float2 p2 = tab.p2[j];
+        float4 p0, p1;
+        float2 p2;
+        tab(j, p0, p1, p2);
         const float dirx = fmaf(fz, p1.w, fmaf(fx, p1.x, p0.x));
         const float diry = fmaf(fy0, p0.w, fmaf(fz, p2.x, fmaf(fx, p1.y, p0.y)));
         const float dirz = fmaf(fz, p2.y, fmaf(fx, p1.z, p0.z));
@@ -708,6 +754,18 @@ __global__ void __launch_bounds__(256, MINB)
         const int y = y0 + k;
         if (y < Y) vol[((size_t)z * Y + y) * X + x] += acc[k];
     }
+}
+
+template <int RUN, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+    k_bwd3d_ax(float *__restrict__ vol, const float4 *__restrict__ SQ,
+                const __grid_constant__ AxViewParams tab, int nv, float num, float su, float sv,
+                int X, int Y, int Z, int U, int V, int tiles_x, int tiles_y, int tiles_z) {
+    const auto param_tab = [&](int j, float4 &p0, float4 &p1, float2 &p2) {
+        p0 = tab.p0[j], p1 = tab.p1[j], p2 = tab.p2[j];
+    };
+    bwd3d_ax_block<RUN>(vol, SQ, param_tab, nv, num, su, sv, X, Y, Z, U, V, tiles_x, tiles_y,
+                        tiles_z, blockIdx.x);
 }
 
 }  // namespace
@@ -871,6 +929,200 @@ int launch_backward3d(const Plan3d &p, float *vol, const float *sino, cudaStream
         vol, quad ? (const void *)p.d_sinoQ : (const void *)p.d_sinoP, p.d_borg, p.d_bdx,
         p.d_bdy, p.d_bdz, p.bsrc[0], p.bsrc[1], p.bsrc[2], zplane, hu, hv, p.X, p.Y, p.Z, p.U, p.V, p.nangles, tiles_x, tiles_y, tiles_z);
     CG_TRY_CUDA(cudaGetLastError());
+    return CG_OK;
+}
+
+// ------------------------------------------------------------ batches
+
+// Many 3D problems per launch: stage s of problem i owns the blocks
+// [start[i], start[i + 1]) of the stage's launch; each block finds its
+// problem by binary search over the starts and runs the single-problem
+// block code on that problem's buffers with its own block index, so the
+// results are those of the single-problem kernels bit for bit.
+namespace {
+
+__global__ void __launch_bounds__(256)
+    k_batch3d_qa(const Prob3d *__restrict__ probs, const int *__restrict__ start, int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob3d &q = probs[i];
+    relayout3d_qa_at(q.vol, q.X, q.Y, q.Z, q.QA,
+                     (long long)(blockIdx.x - start[i]) * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(256)
+    k_batch3d_qb(const Prob3d *__restrict__ probs, const int *__restrict__ start, int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob3d &q = probs[i];
+    const int lin = blockIdx.x - start[i];
+    const int ga = (q.Z + kQP + 31) / 32, gc = (q.X + kQP + 31) / 32;
+    relayout3d_qb_tile(q.vol, q.X, q.Y, q.Z, q.QB, lin % ga, (lin / ga) % gc, lin / (ga * gc));
+}
+
+__global__ void __launch_bounds__(256, 6)
+    k_batch3d_fwd(const Prob3d *__restrict__ probs, const int *__restrict__ start, int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob3d &q = probs[i];
+    fwd3d_quad_block<2>(q.QA, q.QB, q.sino, q.forg, q.fdu, q.fdv, q.fsrc, q.X, q.Y, q.Z, q.U,
+                        q.V, q.P, q.utiles, q.tex, q.tex_warps, q.exact_t != 0,
+                        blockIdx.x - start[i]);
+}
+
+__global__ void __launch_bounds__(256)
+    k_batch3d_relayout_sino(const Prob3d *__restrict__ probs, const int *__restrict__ start,
+                            int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob3d &q = probs[i];
+    const long long idx = (long long)(blockIdx.x - start[i]) * blockDim.x + threadIdx.x;
+    if (q.axial)
+        relayout_sino3d_qd_at(q.sino, q.U, q.V, q.P, q.sinoQ, idx);
+    else
+        relayout_sino3d_quad_at(q.sino, q.U, q.V, q.P, q.sinoQ, idx);
+}
+
+// The axial backprojection over every view of the problem, kAxViews views
+// at a time with the running sum added into the volume after each (as the
+// single-problem launches do), the view tables read from device memory.
+template <int RUN>
+__global__ void __launch_bounds__(256, 5)
+    k_batch3d_bwd_ax(const Prob3d *__restrict__ probs, const int *__restrict__ start,
+                     int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob3d &q = probs[i];
+    const int lin = blockIdx.x - start[i];
+    const size_t plane = (size_t)(q.U + 2 * kP3) * (q.V + 2 * kP3);
+    for (int c0 = 0; c0 < q.P; c0 += kAxViews) {
+        const int nv = min(kAxViews, q.P - c0);
+        const float4 *a0 = q.ax0 + c0, *a1 = q.ax1 + c0;
+        const float2 *a2 = q.ax2 + c0;
+        const auto tab = [&](int j, float4 &p0, float4 &p1, float2 &p2) {
+            p0 = __ldg(a0 + j), p1 = __ldg(a1 + j), p2 = __ldg(a2 + j);
+        };
+        bwd3d_ax_block<RUN>(q.vol, q.sinoQ + plane * c0, tab, nv, q.num, q.su, q.sv, q.X, q.Y,
+                            q.Z, q.U, q.V, q.tiles_x, q.tiles_y, q.tiles_z, lin);
+    }
+}
+
+__global__ void __launch_bounds__(256, 5)
+    k_batch3d_bwd(const Prob3d *__restrict__ probs, const int *__restrict__ start, int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob3d &q = probs[i];
+    bwd3d_block<true, true, true>(q.vol, q.sinoQ, q.borg, q.bdx, q.bdy, q.bdz, q.bsx, q.bsy,
+                                  q.bsz, q.zplane, q.hu, q.hv, q.X, q.Y, q.Z, q.U, q.V, q.P,
+                                  q.tiles_x, q.tiles_y, q.tiles_z, blockIdx.x - start[i]);
+}
+
+}  // namespace
+
+int bind_batch3d_problem(Plan3d &p, float *vol, float *sino, float *ax, Prob3d *q,
+                         int blocks[kBatch3dStages]) {
+    const size_t n = (size_t)(p.X + kQP) * (p.Y + kQP) * (p.Z + kQP);
+    if (n >= (1ull << 32))
+        return set_error(CG_ERR_INVALID, "volume too large for the batched quad forward");
+    if (!p.d_volQA) {
+        int rc = CG_OK;
+        if (!try_malloc_or_oom((void **)&p.d_volQA, n * sizeof(float4), &rc) ||
+            !try_malloc_or_oom((void **)&p.d_volQB, n * sizeof(float4), &rc)) {
+            if (p.d_volQA) cudaFree(p.d_volQA);
+            p.d_volQA = nullptr;
+            return rc ? rc : set_error(CG_ERR_NOMEM, "no room for a batched problem's quads");
+        }
+    }
+    if (int rc = ensure_plan3d_scratch(p, false, true)) return rc;
+    if (!p.reads_quads())
+        return set_error(CG_ERR_NOMEM, "no room for a batched problem's projection quads");
+    const int tex_warps = p.algo_fwd == 5 ? p.fwd_tex_warps : 0;
+    if (tex_warps > 0)
+        if (int rc = ensure_volume_texture3(p)) return rc;
+
+    Prob3d r{};
+    r.vol = vol, r.sino = sino;
+    r.QA = p.d_volQA, r.QB = p.d_volQB;
+    r.forg = p.d_forg, r.fdu = p.d_fdu, r.fdv = p.d_fdv, r.fsrc = p.d_fsrc;
+    r.tex = tex_warps > 0 ? p.tex3 : 0;
+    r.tex_warps = tex_warps, r.exact_t = p.exact_t ? 1 : 0;
+    r.X = p.X, r.Y = p.Y, r.Z = p.Z, r.U = p.U, r.V = p.V, r.P = p.nangles;
+    r.utiles = ceil_div(p.U, 32);
+    r.sinoQ = p.d_sinoQ;
+    r.axial = p.runs_axial() ? 1 : 0;
+    // the single-problem launchers' constants, in the same FP32 operations
+    const float zplane = p.DSO - p.DSD;
+    const float hu = (float)(p.U / 2), hv = (float)(p.V / 2);
+    if (r.axial) {
+        // per view: p0 = (a0, a1, a2, a9), p1 = (a3, a4, a5, a6), p2 = (a7, a8)
+        const int P = p.nangles;
+        std::vector<float> h((size_t)P * 10);
+        for (int j = 0; j < P; ++j) {
+            const float *a = p.ax_views.data() + (size_t)j * 10;
+            float *p0 = h.data() + (size_t)j * 4, *p1 = h.data() + (size_t)(P + j) * 4;
+            float *p2 = h.data() + (size_t)P * 8 + (size_t)j * 2;
+            p0[0] = a[0], p0[1] = a[1], p0[2] = a[2], p0[3] = a[9];
+            p1[0] = a[3], p1[1] = a[4], p1[2] = a[5], p1[3] = a[6];
+            p2[0] = a[7], p2[1] = a[8];
+        }
+        CG_TRY_CUDA(cudaMemcpy(ax, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+        r.ax0 = reinterpret_cast<const float4 *>(ax);
+        r.ax1 = r.ax0 + P;
+        r.ax2 = reinterpret_cast<const float2 *>(r.ax1 + P);
+        r.num = zplane - p.bsrc[2];
+        r.su = p.bsrc[0] + hu - 0.5f, r.sv = p.bsrc[1] + hv - 0.5f;
+        r.tiles_x = ceil_div(p.X, 32), r.tiles_y = ceil_div(p.Y, 8), r.tiles_z = ceil_div(p.Z, 8);
+    } else {
+        r.borg = p.d_borg, r.bdx = p.d_bdx, r.bdy = p.d_bdy, r.bdz = p.d_bdz;
+        r.bsx = p.bsrc[0], r.bsy = p.bsrc[1], r.bsz = p.bsrc[2];
+        r.zplane = zplane, r.hu = hu, r.hv = hv;
+        r.tiles_x = ceil_div(p.X, 32), r.tiles_y = ceil_div(p.Y, 8), r.tiles_z = ceil_div(p.Z, kBZ);
+    }
+    *q = r;
+
+    const long long bricks = (long long)ceil_div(r.tiles_x, 2) * ceil_div(r.tiles_y, 8) *
+                             ceil_div(r.tiles_z, 8) * 128;
+    const long long b[kBatch3dStages] = {
+        ceil_div((long long)n, 256),
+        (long long)ceil_div(p.Z + kQP, 32) * ceil_div(p.X + kQP, 32) * (p.Y + kQP),
+        (long long)r.utiles * p.nangles * ceil_div(p.V, 8),
+        ceil_div((long long)(p.U + 2 * kP3) * (p.V + 2 * kP3) * p.nangles, 256),
+        r.axial ? bricks : 0,
+        r.axial ? 0 : bricks};
+    for (int st = 0; st < kBatch3dStages; ++st) {
+        if (b[st] >= (1ll << 31)) return set_error(CG_ERR_INVALID, "problem too large for a batch");
+        blocks[st] = (int)b[st];
+    }
+    return CG_OK;
+}
+
+int launch_batch3d_forward(const Prob3d *d_probs, const int *starts,
+                           const int totals[kBatch3dStages], int count, cudaStream_t s) {
+    const int n1 = count + 1;
+    if (totals[0] > 0) {
+        k_batch3d_qa<<<totals[0], 256, 0, s>>>(d_probs, starts, count);
+        CG_TRY_CUDA(cudaGetLastError());
+    }
+    if (totals[1] > 0) {
+        k_batch3d_qb<<<totals[1], dim3(32, 8), 0, s>>>(d_probs, starts + n1, count);
+        CG_TRY_CUDA(cudaGetLastError());
+    }
+    if (totals[2] > 0) {
+        k_batch3d_fwd<<<totals[2], 256, 0, s>>>(d_probs, starts + 2 * n1, count);
+        CG_TRY_CUDA(cudaGetLastError());
+    }
+    return CG_OK;
+}
+
+int launch_batch3d_backward(const Prob3d *d_probs, const int *starts,
+                            const int totals[kBatch3dStages], int count, cudaStream_t s) {
+    const int n1 = count + 1;
+    if (totals[3] > 0) {
+        k_batch3d_relayout_sino<<<totals[3], 256, 0, s>>>(d_probs, starts + 3 * n1, count);
+        CG_TRY_CUDA(cudaGetLastError());
+    }
+    if (totals[4] > 0) {
+        k_batch3d_bwd_ax<8><<<totals[4], 256, 0, s>>>(d_probs, starts + 4 * n1, count);
+        CG_TRY_CUDA(cudaGetLastError());
+    }
+    if (totals[5] > 0) {
+        k_batch3d_bwd<<<totals[5], dim3(32, 8), 0, s>>>(d_probs, starts + 5 * n1, count);
+        CG_TRY_CUDA(cudaGetLastError());
+    }
     return CG_OK;
 }
 

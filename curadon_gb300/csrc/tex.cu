@@ -346,12 +346,17 @@ int launch_backward2d_tex(Plan2d &p, float *vol, const float *sino, cudaStream_t
     return CG_OK;
 }
 
-int upload_volume_texture3(Plan3d &p, const float *vol, cudaStream_t s) {
+int ensure_volume_texture3(Plan3d &p) {
     if (!p.arr3) {
         int rc = alloc_array(&p.arr3, p.X, p.Y, p.Z, cudaArrayDefault);
         if (rc) return rc;
         if ((rc = make_texture(p.arr3, &p.tex3))) return rc;
     }
+    return CG_OK;
+}
+
+int upload_volume_texture3(Plan3d &p, const float *vol, cudaStream_t s) {
+    if (int rc = ensure_volume_texture3(p)) return rc;
     return copy_to_array(p.arr3, vol, p.X, p.Y, p.Z, s);
 }
 

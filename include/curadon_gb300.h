@@ -313,6 +313,31 @@ int cg_batch2d_set_active(cg_batch2d *batch, int active);
 int cg_batch2d_set_forward(cg_batch2d *batch, int algorithm);
 int cg_batch2d_get_forward(const cg_batch2d *batch, int *algorithm);
 
+/* The same for 3D: `count` plans (any volume and detector sizes, views and
+ * geometries, each plan at most once) bound to their device volumes and
+ * projections.  The forward is three launches over the work list (the two
+ * quad re-layouts of every volume, then the quad ray march of every
+ * problem, with each plan's texture warps: algorithm 5 plans first copy
+ * their volume into the plan's array), the backprojection two or three
+ * (the projections' re-layout, then axial runs for the problems whose plan
+ * takes them and the general kernel on row-pair quads for the others).
+ * Results equal cg_forward_3d_plan on plans with forward algorithm 4 or 5
+ * (algorithm 4 for plans set to 0 or 1) and cg_backward_3d_plan bit for
+ * bit; as there, the forward writes only the rays that hit the volume's box
+ * and the backprojection adds into the volumes.  Creation allocates each
+ * plan's quad copies (4 x 16 bytes per padded voxel and per padded
+ * projection cell) and fails with CG_ERR_NOMEM where they do not fit.  No
+ * counterpart in the reference (forward_3d.hpp:97-211 and
+ * backward_3d.hpp:110-178 run one problem per call). */
+typedef struct cg_batch3d cg_batch3d;
+int cg_batch3d_create(cg_batch3d **batch, cg_plan3d *const *plans, float *const *volumes,
+                      float *const *sinograms, int count);
+int cg_batch3d_destroy(cg_batch3d *batch);
+int cg_batch3d_forward(cg_batch3d *batch, void *stream);
+int cg_batch3d_backward(cg_batch3d *batch, void *stream);
+/* later calls run problems [0, active) only, as cg_batch2d_set_active */
+int cg_batch3d_set_active(cg_batch3d *batch, int active);
+
 #ifdef __cplusplus
 }
 #endif
