@@ -56,7 +56,8 @@ def parse():
     p.add_argument("--workload", default="fan2048",
                    help="fan<n> (n-sweep: n x n, n views), cone256 / cone512, serve "
                         "(served reconstruction stream vs the plain loop), batch (64 "
-                        "jittered problems, batched gradient descent vs the plain loop) or "
+                        "jittered problems, batched gradient descent vs the plain loop), "
+                        "batch3d (the same on 24 cone-beam problems) or "
                         "sweep (the 2D n-sweep against the reference's CUDA operators)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--sweep-sizes", default="64,128,256,512,1024,2048",
@@ -1023,85 +1024,71 @@ def fwd_kernels(algo: str, sizes) -> int:
     return (1 if not all(big) else 0) + (2 if any(big) else 0)
 
 
-def run_batch(args):
-    """The batched, differentiable workload: 10 unrolled gradient-descent steps
-    x <- x - a grad 1/2 ||A x - y||^2 over all 64 problems, each step through
-    torch.autograd on the batched projector (one forward and one gradient for
-    the whole batch, a few launches each), one step captured in a CUDA graph
-    and replayed.  ``value`` counts operator calls (two per problem and step)
-    per second.  Beside it: the same steps as a plain loop of single-problem
-    calls through the same autograd functions (one problem per launch), and
-    the reference's own CUDA operators in the same plain loop (its geometry
-    holds no per-view jitter, so it runs the unjittered circular problems of
-    the same sizes: the same work).  ``matched`` repeats the batched steps
-    with the exact gradient (register forward, batched matched adjoint)."""
+def time_batched_gd(proj, Y, iters: int, steps: int, warmup: int):
+    """Times ``steps`` steps of ``iters`` unrolled gradient-descent iterations
+    x <- x - a grad 1/2 ||A x - y||^2 through torch.autograd on a batched
+    projector, one iteration captured in a CUDA graph and replayed (CUDA
+    events around each step); a = 1 / lambda_i per problem, lambda_i the
+    largest eigenvalue of B_i A_i (B the projector's backward operator: the
+    drop-in backprojector is not scaled like A^T) by power iteration
+    (untimed).  Returns (ms per step, relative
+    residual, a)."""
     import torch
 
-    from curadon_gb300 import TorchForward, _build
-    from curadon_gb300.batch import BatchProjector
-
-    _build.build()
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
-    probs = batch_problems(dev)
-    count = len(probs)
-    geoms = [g for g, _, _ in probs]
-    iters = 10
-    steps = max(1, args.steps // 10)  # a step = the 10 unrolled iterations
-
-    def batched(matched: bool):
-        proj = BatchProjector(geoms, dev, forward=args.batch_forward, matched=matched)
-        Y = torch.cat([y.reshape(-1) for _, _, y in probs])
-        # step sizes 1 / ||A_i^T A_i|| by power iteration (set-up, untimed)
-        v = torch.rand_like(proj.X)
-        for _ in range(8):
-            with torch.no_grad():
-                w = proj.adjoint(proj(v))
-            v = torch.cat([(t / t.norm().clamp_min(1e-20)).reshape(-1)
-                           for t in proj.split_volumes(w)])
+    dev = proj.device
+    v = torch.rand_like(proj.X)
+    lam = None
+    for _ in range(10):
+        v = torch.cat([(t / t.norm().clamp_min(1e-20)).reshape(-1)
+                       for t in proj.split_volumes(v)])
         with torch.no_grad():
-            av = proj(v)
-        A = torch.cat([torch.full((int(np.prod(sh)),), 1.0 / float(a_.norm() ** 2), device=dev)
-                       for sh, a_ in zip(proj.vol_shapes, proj.split_sinograms(av))])
-        x = torch.zeros_like(proj.X)
+            v = proj.adjoint(proj(v))
+        lam = [float(t.norm()) for t in proj.split_volumes(v)]
+    A = torch.cat([torch.full((int(np.prod(sh)),), 1.0 / max(l_, 1e-20), device=dev)
+                   for sh, l_ in zip(proj.vol_shapes, lam)])
+    x = torch.zeros_like(proj.X)
 
-        def iteration():
-            xr = x.detach().requires_grad_(True)
-            r = proj(xr) - Y
-            (g,) = torch.autograd.grad(0.5 * (r * r).sum(), xr)
-            x.sub_(A * g)
+    def iteration():
+        xr = x.detach().requires_grad_(True)
+        r = proj(xr) - Y
+        (g,) = torch.autograd.grad(0.5 * (r * r).sum(), xr)
+        x.sub_(A * g)
 
-        for _ in range(max(3, args.warmup)):
-            iteration()
-        torch.cuda.synchronize()
-        graph = torch.cuda.CUDAGraph()
-        cap = torch.cuda.Stream()
-        cap.wait_stream(torch.cuda.current_stream())
-        with torch.cuda.stream(cap), torch.cuda.graph(graph, stream=cap):
-            iteration()
-        torch.cuda.current_stream().wait_stream(cap)
-        for _ in range(max(3, args.warmup)):
+    for _ in range(max(3, warmup)):
+        iteration()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    cap = torch.cuda.Stream()
+    cap.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(cap), torch.cuda.graph(graph, stream=cap):
+        iteration()
+    torch.cuda.current_stream().wait_stream(cap)
+    for _ in range(max(3, warmup)):
+        graph.replay()
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(steps)]
+    for k in range(steps):
+        x.zero_()
+        ev[k][0].record()
+        for _ in range(iters):
             graph.replay()
-        torch.cuda.synchronize()
-        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(steps)]
-        for k in range(steps):
-            x.zero_()
-            ev[k][0].record()
-            for _ in range(iters):
-                graph.replay()
-            ev[k][1].record()
-        torch.cuda.synchronize()
-        ms = sum(a_.elapsed_time(b_) for a_, b_ in ev) / steps
-        with torch.no_grad():
-            res = float(torch.linalg.vector_norm(proj(x) - Y) / torch.linalg.vector_norm(Y))
-        return ms, res, proj, A
+        ev[k][1].record()
+    torch.cuda.synchronize()
+    ms = sum(a_.elapsed_time(b_) for a_, b_ in ev) / steps
+    with torch.no_grad():
+        res = float(torch.linalg.vector_norm(proj(x) - Y) / torch.linalg.vector_norm(Y))
+    return ms, res, A
 
-    batch_ms, residual, proj, A = batched(False)
-    matched_ms, matched_res, _, _ = batched(True)
 
-    # plain loop: the same autograd steps problem by problem (single-problem calls)
-    ys = [y for _, _, y in probs]
-    av = proj.split_volumes(A)
+def time_plain_gd(geoms, ys, av, iters: int):
+    """The same gradient-descent iterations as a plain loop of single-problem
+    calls through the drop-in autograd function (one problem per launch
+    chain); ms for ``iters`` iterations after three warm-up iterations."""
+    import torch
+
+    from curadon_gb300 import TorchForward
+
+    dev = ys[0].device
     xs = [torch.zeros(tuple(int(v) for v in g.vol_shape), device=dev) for g in geoms]
 
     def plain_iteration():
@@ -1122,7 +1109,49 @@ def run_batch(args):
         plain_iteration()
     b_ev.record()
     torch.cuda.synchronize()
-    plain_ms = a_ev.elapsed_time(b_ev)
+    return a_ev.elapsed_time(b_ev)
+
+
+def run_batch(args):
+    """The batched, differentiable workload: 10 unrolled gradient-descent steps
+    x <- x - a grad 1/2 ||A x - y||^2 over all 64 problems, each step through
+    torch.autograd on the batched projector (one forward and one gradient for
+    the whole batch, a few launches each), one step captured in a CUDA graph
+    and replayed.  ``value`` counts operator calls (two per problem and step)
+    per second.  Beside it: the same steps as a plain loop of single-problem
+    calls through the same autograd functions (one problem per launch), and
+    the reference's own CUDA operators in the same plain loop (its geometry
+    holds no per-view jitter, so it runs the unjittered circular problems of
+    the same sizes: the same work).  ``matched`` repeats the batched steps
+    with the exact gradient (register forward, batched matched adjoint)."""
+    import torch
+
+    from curadon_gb300 import _build
+    from curadon_gb300.batch import BatchProjector
+
+    _build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    probs = batch_problems(dev)
+    count = len(probs)
+    geoms = [g for g, _, _ in probs]
+    iters = 10
+    steps = max(1, args.steps // 10)  # a step = the 10 unrolled iterations
+
+    def batched(matched: bool):
+        proj = BatchProjector(geoms, dev, forward=args.batch_forward, matched=matched)
+        Y = torch.cat([y.reshape(-1) for _, _, y in probs])
+        ms, res, A = time_batched_gd(proj, Y, iters, steps, args.warmup)
+        return ms, res, proj, A
+
+    batch_ms, residual, proj, A = batched(False)
+    matched_ms, matched_res, _, _ = batched(True)
+
+    # plain loop: the same autograd steps problem by problem (single-problem calls)
+    ys = [y for _, _, y in probs]
+    av = proj.split_volumes(A)
+    plain_ms = time_plain_gd(geoms, ys, av, iters)
+    a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     # the reference's operators in the same plain loop (circular problems of the same sizes)
     ref, why = reference_ops()
@@ -1191,6 +1220,117 @@ def run_batch(args):
     return line
 
 
+def batch3d_problems(dev, count: int = 24):
+    """The 3D batched workload: ``count`` circular cone-beam problems, n ~
+    U{48, 64, 96, 128} (n^3 volumes), 90..360 views, ceil(1.5 n)^2 cells of
+    1.5, source-isocentre 2n, isocentre-detector n, data y = A x + Poisson
+    noise (I0 = 1e4) from a seeded ellipsoid phantom."""
+    import torch
+
+    from curadon_gb300 import ConeGeometry, forward
+    from curadon_gb300.phantom import cone_config, ellipsoids_3d, seed_for
+
+    rng = np.random.default_rng(seed_for(5, 0))
+    out = []
+    for k in range(count):
+        n = int(rng.choice([48, 64, 96, 128]))
+        nangles = int(rng.integers(90, 361))
+        cfg = cone_config(n, nangles, int(np.ceil(1.5 * n)))
+        geom = ConeGeometry(**cfg, device=dev.index or 0)
+        x = ellipsoids_3d(n, seed_for(5, k + 1), device=dev).contiguous()
+        s = torch.zeros(geom.sinogram_shape(), device=dev)
+        forward(x, s, geom)
+        mu = 2.5 / float(s.max())
+        counts = torch.poisson(1e4 * torch.exp(-mu * s)).clamp_min(1.0)
+        y = -torch.log(counts / 1e4) / mu
+        out.append((geom, cfg, y))
+    return out
+
+
+def run_batch3d(args):
+    """The batched, differentiable workload on 3D problems: 10 unrolled
+    gradient-descent iterations over all problems through torch.autograd on
+    the batched 3D projector (three forward launches and two backprojection
+    launches for the whole batch per iteration), one iteration captured in a
+    CUDA graph; beside it the same iterations as a plain loop of
+    single-problem calls through the drop-in autograd function, and the
+    reference's own CUDA operators in the same plain loop."""
+    import torch
+
+    from curadon_gb300 import _build
+    from curadon_gb300.batch import BatchProjector
+
+    _build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    probs = batch3d_problems(dev)
+    count = len(probs)
+    geoms = [g for g, _, _ in probs]
+    ys = [y for _, _, y in probs]
+    iters = 10
+    steps = max(1, args.steps // 10)
+    proj = BatchProjector(geoms, dev)
+    Y = torch.cat([y.reshape(-1) for y in ys])
+    batch_ms, residual, A = time_batched_gd(proj, Y, iters, steps, args.warmup)
+    av = proj.split_volumes(A)
+    plain_ms = time_plain_gd(geoms, ys, av, iters)
+
+    ref, why = reference_ops()
+    ref_ms = None
+    if ref is not None:
+        rx = [torch.zeros(tuple(int(v) for v in g.vol_shape), device=dev) for g in geoms]
+        rs = [torch.zeros_like(y) for y in ys]
+        rg = [torch.zeros_like(x) for x in rx]
+
+        def ref_iteration():
+            for i, (_, cfg, _) in enumerate(probs):
+                rs[i].zero_()  # the forward writes only the rays that hit the box
+                ref.forward3d(cfg, rx[i].data_ptr(), rs[i].data_ptr())
+                torch.sub(rs[i], ys[i], out=rs[i])
+                rg[i].zero_()
+                ref.backward3d(cfg, rg[i].data_ptr(), rs[i].data_ptr())
+                rx[i].sub_(av[i] * rg[i])
+
+        ref_iteration()
+        torch.cuda.synchronize()
+        a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a_ev.record()
+        for _ in range(iters):
+            ref_iteration()
+        b_ev.record()
+        torch.cuda.synchronize()
+        ref_ms = a_ev.elapsed_time(b_ev)
+
+    ops = 2 * count * iters
+    value = ops / (batch_ms / 1e3)
+    plain_value = ops / (plain_ms / 1e3)
+    sizes = sorted({int(g.vol_shape[0]) for g in geoms})
+    line = {
+        "metric": "fwd/bwd proj ops/s", "value": value, "unit": "ops/s", "n_gpus": 1,
+        "steps": steps, "warmup": max(3, args.warmup), "ms_per_step": batch_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded ellipsoid phantoms, Poisson noise)",
+        "config": {"workload": f"batched differentiable gradient descent: {count} 3D cone-beam "
+                               f"problems, n^3 with n in {sizes}, 90..360 views, ceil(1.5 n)^2 "
+                               "cells, y = Ax + Poisson noise (I0 1e4); a step = 10 unrolled "
+                               "iterations x - a grad 1/2||Ax - y||^2 through torch.autograd "
+                               "over all problems, one iteration graph-captured",
+                   "parallelism": "one GPU"},
+        # per iteration: two quad re-layouts and the forward, the projections'
+        # re-layout and the axial backprojection (circular orbits)
+        "gpu_launches": 5 * iters * steps,
+        "gradient": "drop-in (the backprojector, as the reference's autograd function)",
+        "relative_residual_after_10": residual,
+        "plain_loop_ops_per_s": plain_value, "speedup_vs_plain_loop": value / plain_value,
+    }
+    if ref_ms is not None:
+        line["reference_plain_loop_ops_per_s"] = ops / (ref_ms / 1e3)
+        line["speedup_vs_reference_plain_loop"] = value / (ops / (ref_ms / 1e3))
+    else:
+        line["reference_plain_loop"] = {"unavailable": why}
+    return line
+
+
 def main():
     global CONE_VIEWS
     args = parse()
@@ -1204,6 +1344,8 @@ def main():
         line = run_serve(args) if rank == 0 else None
     elif args.workload == "batch":
         line = run_batch(args) if rank == 0 else None
+    elif args.workload == "batch3d":
+        line = run_batch3d(args) if rank == 0 else None
     elif args.impl == "reference":
         line = run_reference_cpu(args, rank, world)
     elif args.impl == "reference-gpu":
