@@ -75,6 +75,7 @@ SIGNATURES = [
     ("cg_batch3d_destroy", C.c_int, [C.c_void_p]),
     ("cg_batch3d_forward", C.c_int, [C.c_void_p, C.c_void_p]),
     ("cg_batch3d_backward", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("cg_batch3d_adjoint", C.c_int, [C.c_void_p, C.c_void_p]),
     ("cg_batch3d_set_active", C.c_int, [C.c_void_p, C.c_int]),
 ]
 

@@ -21,7 +21,8 @@ adds the matched adjoint (the exact transpose of the register forward).
 flat buffers.  ``Batch3d`` does the same for cone-beam problems (any volume
 and detector sizes, views and geometries): the quad forward with each
 plan's texture warps and the axial or general backprojection, bit-equal to
-the single-problem operators.  No counterpart in the reference, which runs
+the single-problem operators, and the matched adjoint of the quad forward.
+No counterpart in the reference, which runs
 one problem per call.
 """
 from __future__ import annotations
@@ -39,10 +40,11 @@ from .geometry import ConeGeometry, FanGeometry
 __all__ = ["Batch2d", "Batch3d", "BatchProjector"]
 
 
-def _bind_plans(geoms, volumes, sinograms, kind, ndim):
-    """The plans of a batch's problems after checking its tensors; a
-    geometry used twice gets a private plan for its second use (each
-    problem needs its own plan scratch)."""
+def _bind_plans(geoms, volumes, sinograms, kind, ndim, exact=False):
+    """The plans of a batch's problems after checking its tensors (with
+    ``exact``, the geometries' FP32-filtering plans); a geometry used twice
+    gets a private plan for its second use (each problem needs its own plan
+    scratch)."""
     if not (len(geoms) == len(volumes) == len(sinograms)) or not geoms:
         raise ValueError("geoms, volumes and sinograms must be non-empty and of one length")
     dev = volumes[0].device
@@ -58,7 +60,12 @@ def _bind_plans(geoms, volumes, sinograms, kind, ndim):
             raise ValueError(f"volume shape {tuple(v.shape)} != geometry {tuple(g.vol_shape)}")
         if tuple(s.shape) != tuple(g.sinogram_shape()):
             raise ValueError(f"sinogram shape {tuple(s.shape)} != {tuple(g.sinogram_shape())}")
-        p = g.plan if id(g) not in seen else g._make_plan()
+        if id(g) not in seen:
+            p = g.exact_plan if exact else g.plan
+        else:
+            p = g._make_plan()
+            if exact:
+                p.set_algorithm(forward="quad" if ndim == 3 else "registers")
         seen.add(id(g))
         plans.append(p)
     return plans, dev
@@ -161,12 +168,14 @@ class Batch3d:
     allows them, the general kernel otherwise), each over a (problem, tile)
     work list in a few launches; results equal ``plan.forward`` /
     ``plan.backward`` bit for bit (plans set to the "registers" or "texture"
-    forward run the "quad" forward here).  Binding allocates each plan's
-    quad copies.  Capturable in a CUDA graph."""
+    forward run the "quad" forward here).  With ``exact=True`` the batch
+    binds the geometries' FP32-filtering plans (``exact_plan``: the quad
+    forward without texture warps), whose transpose ``adjoint()`` adds.
+    Binding allocates each plan's quad copies.  Capturable in a CUDA graph."""
 
     def __init__(self, geoms: Sequence[ConeGeometry], volumes: Sequence[torch.Tensor],
-                 sinograms: Sequence[torch.Tensor]):
-        plans, dev = _bind_plans(geoms, volumes, sinograms, ConeGeometry, 3)
+                 sinograms: Sequence[torch.Tensor], exact: bool = False):
+        plans, dev = _bind_plans(geoms, volumes, sinograms, ConeGeometry, 3, exact=exact)
         self._L = load()
         h = C.c_void_p()
         check(self._L.cg_batch3d_create(
@@ -195,6 +204,13 @@ class Batch3d:
     def set_active(self, active: int):
         """Later calls run problems [0, active) only."""
         check(self._L.cg_batch3d_set_active(self._h, int(active)))
+
+    def adjoint(self):
+        """volume_i += the matched adjoint of projections_i for every problem
+        (the exact transpose of the quad forward without texture warps; the
+        first call allocates the accumulators, so make it before a graph
+        capture)."""
+        check(self._L.cg_batch3d_adjoint(self._h, _stream(self._keep[1][0])))
 
 
 class _BatchProject(torch.autograd.Function):
@@ -234,8 +250,9 @@ class BatchProjector:
     ``matched=True``, the batched matched adjoint, the exact transpose of the
     register forward that ``matched`` selects.  Both directions are a few
     launches for the whole batch, capturable in a CUDA graph.  A list of
-    ``ConeGeometry`` problems makes a 3D batch (``Batch3d``; its gradient is
-    the batched backprojection, there is no batched 3D matched adjoint)."""
+    ``ConeGeometry`` problems makes a 3D batch (``Batch3d``; with
+    ``matched=True`` the quad forward without texture warps and its batched
+    matched adjoint)."""
 
     def __init__(self, geoms: Sequence[FanGeometry | ConeGeometry], device=None,
                  forward: str = "plans", matched: bool = False):
@@ -243,8 +260,6 @@ class BatchProjector:
         self.geoms = list(geoms)
         self.matched = bool(matched)
         self.cone = bool(self.geoms) and isinstance(self.geoms[0], ConeGeometry)
-        if self.cone and self.matched:
-            raise ValueError("3D batches have no matched adjoint (use matched=False)")
         self.vol_shapes = [tuple(int(v) for v in g.vol_shape) for g in self.geoms]
         self.sino_shapes = [tuple(g.sinogram_shape()) for g in self.geoms]
         nv = [int(np.prod(s)) for s in self.vol_shapes]
@@ -257,9 +272,9 @@ class BatchProjector:
         self.R = torch.zeros_like(self.S)
         if self.cone:
             self._fwd = Batch3d(self.geoms, self.split_volumes(self.X),
-                                self.split_sinograms(self.S))
+                                self.split_sinograms(self.S), exact=self.matched)
             self._bwd = Batch3d(self.geoms, self.split_volumes(self.G),
-                                self.split_sinograms(self.R))
+                                self.split_sinograms(self.R), exact=self.matched)
         else:
             self._fwd = Batch2d(self.geoms, self.split_volumes(self.X),
                                 self.split_sinograms(self.S),

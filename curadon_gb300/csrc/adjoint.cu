@@ -192,27 +192,27 @@ __global__ void k_fold2d(float *__restrict__ vol, const float2 *__restrict__ A,
 // whose lower-slice element coincides at a step (found with
 // __match_any_sync) pass their contributions through shared memory to the
 // lowest such lane, which sums them in lane order and issues one atomic.
-template <bool QUAD, bool BAND = false, bool MERGE = false, bool AGG = false>
-__global__ void __launch_bounds__(256)
-    k_adj3d(void *__restrict__ A, void *__restrict__ B, const float *__restrict__ sino,
-            const float4 *__restrict__ torg, const float4 *__restrict__ tdu,
-            const float4 *__restrict__ tdv, const float4 *__restrict__ tsrc, int X, int Y, int Z,
-            int U, int V, int P, int utiles, bool exact_t) {
-    int iu, iv, view;
-    if constexpr (BAND) {
-        const int lin = blockIdx.x;
-        const int ut = lin % utiles, rest = lin / utiles;
-        view = rest % P;
-        const int band = rest / P;
-        const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-        const int lane = tid & 31, warp = tid >> 5;
-        iu = ut * 32 + (warp & 3) * 8 + (lane & 7);
-        iv = band * 8 + (warp >> 2) * 4 + (lane >> 3);
-    } else {
-        iu = blockIdx.x * blockDim.x + threadIdx.x;
-        iv = blockIdx.y * blockDim.y + threadIdx.y;
-        view = blockIdx.z;
-    }
+// The band-major block `lin`'s cell of this thread.
+__device__ __forceinline__ void adj3d_band_cell(int lin, int utiles, int P, int &iu, int &iv,
+                                                int &view) {
+    const int ut = lin % utiles, rest = lin / utiles;
+    view = rest % P;
+    const int band = rest / P;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    iu = ut * 32 + (warp & 3) * 8 + (lane & 7);
+    iv = band * 8 + (warp >> 2) * 4 + (lane >> 3);
+}
+
+// One ray's scatter (the cell (iu, iv) of `view`).
+template <bool QUAD, bool MERGE, bool AGG>
+__device__ __forceinline__ void adj3d_ray(void *__restrict__ A, void *__restrict__ B,
+                                          const float *__restrict__ sino,
+                                          const float4 *__restrict__ torg,
+                                          const float4 *__restrict__ tdu,
+                                          const float4 *__restrict__ tdv,
+                                          const float4 *__restrict__ tsrc, int X, int Y, int Z,
+                                          int U, int V, bool exact_t, int iu, int iv, int view) {
     if (iu >= U || iv >= V) return;
     const float c = sino[((size_t)view * V + iv) * U + iu];
     if (c == 0.f) return;
@@ -321,6 +321,24 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+template <bool QUAD, bool BAND = false, bool MERGE = false, bool AGG = false>
+__global__ void __launch_bounds__(256)
+    k_adj3d(void *__restrict__ A, void *__restrict__ B, const float *__restrict__ sino,
+            const float4 *__restrict__ torg, const float4 *__restrict__ tdu,
+            const float4 *__restrict__ tdv, const float4 *__restrict__ tsrc, int X, int Y, int Z,
+            int U, int V, int P, int utiles, bool exact_t) {
+    int iu, iv, view;
+    if constexpr (BAND) {
+        adj3d_band_cell(blockIdx.x, utiles, P, iu, iv, view);
+    } else {
+        iu = blockIdx.x * blockDim.x + threadIdx.x;
+        iv = blockIdx.y * blockDim.y + threadIdx.y;
+        view = blockIdx.z;
+    }
+    adj3d_ray<QUAD, MERGE, AGG>(A, B, sino, torg, tdu, tdv, tsrc, X, Y, Z, U, V, exact_t, iu, iv,
+                                view);
+}
+
 // vol[z][y][x] += A[z][y][x].x + A[z][y][x-1].y + B[x][y][z].x + B[x][y][z-1].y
 __global__ void k_fold3d(float *__restrict__ vol, const float2 *__restrict__ A,
                          const float2 *__restrict__ B, int X, int Y, int Z) {
@@ -337,9 +355,10 @@ __global__ void k_fold3d(float *__restrict__ vol, const float2 *__restrict__ A,
 
 // The same fold for the quad accumulators: voxel (a, b) of slice c gathers
 // .x of (a, b), .y of (a - 1, b), .z of (a, b - 1) and .w of (a - 1, b - 1).
-__global__ void k_fold3d_quad(float *__restrict__ vol, const float4 *__restrict__ A,
-                              const float4 *__restrict__ B, int X, int Y, int Z) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void fold3d_quad_at(float *__restrict__ vol,
+                                               const float4 *__restrict__ A,
+                                               const float4 *__restrict__ B, int X, int Y, int Z,
+                                               long long idx) {
     if (idx >= (long long)X * Y * Z) return;
     const int x = (int)(idx % X);
     const int y = (int)((idx / X) % Y);
@@ -350,6 +369,45 @@ __global__ void k_fold3d_quad(float *__restrict__ vol, const float4 *__restrict_
     const float sa = (ra[0].x + ra[-1].y) + (ra[-PX].z + ra[-PX - 1].w);
     const float sb = (rb[0].x + rb[-1].y) + (rb[-PZ].z + rb[-PZ - 1].w);
     vol[idx] += sa + sb;
+}
+
+__global__ void k_fold3d_quad(float *__restrict__ vol, const float4 *__restrict__ A,
+                              const float4 *__restrict__ B, int X, int Y, int Z) {
+    fold3d_quad_at(vol, A, B, X, Y, Z, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// ---- 3D batches: the matched adjoint of every problem over one work list
+// (the quad accumulators zeroed, the merged quad scatter in band-major
+// order, the fold), the transpose partner of the batched quad forward
+// without texture warps.
+
+__global__ void __launch_bounds__(256)
+    k_batch_adj3d_zero(const Prob3d *__restrict__ probs, const int *__restrict__ start,
+                       int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob3d &q = probs[i];
+    const long long idx = (long long)(blockIdx.x - start[i]) * blockDim.x + threadIdx.x;
+    const long long n = (long long)(q.X + 2 * kPad) * (q.Y + 2 * kPad) * (q.Z + 2 * kPad);
+    if (idx < n) q.adjA[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
+    else if (idx < 2 * n) q.adjB[idx - n] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void __launch_bounds__(256)
+    k_batch_adj3d(const Prob3d *__restrict__ probs, const int *__restrict__ start, int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob3d &q = probs[i];
+    int iu, iv, view;
+    adj3d_band_cell(blockIdx.x - start[i], q.utiles, q.P, iu, iv, view);
+    adj3d_ray<true, true, false>(q.adjA, q.adjB, q.sino, q.forg, q.fdu, q.fdv, q.fsrc, q.X, q.Y,
+                                 q.Z, q.U, q.V, q.exact_t != 0, iu, iv, view);
+}
+
+__global__ void __launch_bounds__(256)
+    k_batch_fold3d(const Prob3d *__restrict__ probs, const int *__restrict__ start, int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob3d &q = probs[i];
+    fold3d_quad_at(q.vol, q.adjA, q.adjB, q.X, q.Y, q.Z,
+                   (long long)(blockIdx.x - start[i]) * blockDim.x + threadIdx.x);
 }
 
 }  // namespace
@@ -410,6 +468,37 @@ int launch_adjoint2d(Plan2d &p, float *vol, const float *sino, cudaStream_t s) {
     return CG_OK;
 }
 
+int ensure_adj3d_quads(Plan3d &p) {
+    if (p.d_quadA) return CG_OK;
+    const size_t elems = (size_t)(p.X + 2 * kPad) * (p.Y + 2 * kPad) * (p.Z + 2 * kPad);
+    CG_TRY_CUDA(cudaMalloc(&p.d_quadA, elems * sizeof(float4)));
+    if (cudaMalloc(&p.d_quadB, elems * sizeof(float4)) != cudaSuccess) {
+        (void)cudaGetLastError();
+        cudaFree(p.d_quadA);
+        p.d_quadA = nullptr;
+        return set_error(CG_ERR_NOMEM, "no room for the matched adjoint's accumulators");
+    }
+    return CG_OK;
+}
+
+int launch_batch3d_adjoint(const Prob3d *d_probs, const int *starts,
+                           const int totals[kBatch3dStages], int count, cudaStream_t s) {
+    const int n1 = count + 1;
+    if (totals[6] > 0) {
+        k_batch_adj3d_zero<<<totals[6], 256, 0, s>>>(d_probs, starts + 6 * n1, count);
+        CG_TRY_CUDA(cudaGetLastError());
+    }
+    if (totals[7] > 0) {
+        k_batch_adj3d<<<totals[7], dim3(32, 8), 0, s>>>(d_probs, starts + 7 * n1, count);
+        CG_TRY_CUDA(cudaGetLastError());
+    }
+    if (totals[8] > 0) {
+        k_batch_fold3d<<<totals[8], 256, 0, s>>>(d_probs, starts + 8 * n1, count);
+        CG_TRY_CUDA(cudaGetLastError());
+    }
+    return CG_OK;
+}
+
 int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s) {
     if (p.nangles > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
     const int utiles = ceil_div(p.U, 32);
@@ -426,10 +515,7 @@ int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s) {
     const bool band = (p.adj_band > 0 || (p.adj_band < 0 && !fits)) && bblocks < (1ll << 31);
     dim3 grid = band ? dim3((unsigned)bblocks) : dim3(utiles, ceil_div(p.V, 8), p.nangles);
     if (quad) {
-        if (!p.d_quadA) {
-            CG_TRY_CUDA(cudaMalloc(&p.d_quadA, elems * sizeof(float4)));
-            CG_TRY_CUDA(cudaMalloc(&p.d_quadB, elems * sizeof(float4)));
-        }
+        if (int rc = ensure_adj3d_quads(p)) return rc;
         CG_TRY_CUDA(cudaMemsetAsync(p.d_quadA, 0, elems * sizeof(float4), s));
         CG_TRY_CUDA(cudaMemsetAsync(p.d_quadB, 0, elems * sizeof(float4), s));
         auto kq = p.adj_agg   ? (band ? k_adj3d<true, true, true, true>

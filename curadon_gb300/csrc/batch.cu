@@ -60,6 +60,7 @@ struct cg_batch3d {
     int *d_starts = nullptr;  // kBatch3dStages stages x (count + 1)
     std::vector<int> starts;
     float *d_ax = nullptr;  // axial view tables of every problem
+    bool adjoint_ready = false;  // the plans' quad accumulators are bound
 
     void active_totals(int out[cg::kBatch3dStages]) const {
         for (int st = 0; st < cg::kBatch3dStages; ++st)
@@ -348,6 +349,28 @@ int cg_batch3d_forward(cg_batch3d *batch, void *stream) {
     int totals[kBatch3dStages];
     batch->active_totals(totals);
     return launch_batch3d_forward(batch->d_probs, batch->d_starts, totals, batch->count, s);
+}
+
+int cg_batch3d_adjoint(cg_batch3d *batch, void *stream) {
+    clear_error();
+    CG_REQUIRE(batch, "batch is NULL");
+    DeviceGuard guard(batch->device);
+    CG_REQUIRE(guard.ok(), "cannot select the batch's device");
+    if (!batch->adjoint_ready) {
+        // first call: every plan's quad accumulators, bound into the work list
+        for (int i = 0; i < batch->count; ++i) {
+            if (int rc = ensure_adj3d_quads(*batch->plans[i])) return rc;
+            batch->probs[i].adjA = batch->plans[i]->d_quadA;
+            batch->probs[i].adjB = batch->plans[i]->d_quadB;
+        }
+        CG_TRY_CUDA(cudaMemcpy(batch->d_probs, batch->probs.data(),
+                               sizeof(Prob3d) * batch->count, cudaMemcpyHostToDevice));
+        batch->adjoint_ready = true;
+    }
+    int totals[kBatch3dStages];
+    batch->active_totals(totals);
+    return launch_batch3d_adjoint(batch->d_probs, batch->d_starts, totals, batch->count,
+                                  (cudaStream_t)stream);
 }
 
 int cg_batch3d_backward(cg_batch3d *batch, void *stream) {

@@ -175,10 +175,13 @@ struct Prob3d {
     const float4 *borg, *bdx, *bdy, *bdz;
     float bsx, bsy, bsz, zplane, hu, hv;
     int tiles_x, tiles_y, tiles_z;
+    // matched adjoint: the plan's quad accumulators (bound on first use)
+    float4 *adjA, *adjB;
 };
 // 3D batch stages: the two volume quad re-layouts, the forward, the
-// projections' re-layout, the axial and the general backprojection
-constexpr int kBatch3dStages = 6;
+// projections' re-layout, the axial and the general backprojection, the
+// matched adjoint's zeroing, scatter and fold
+constexpr int kBatch3dStages = 9;
 
 // Batched stages: re-layout, forward, sinogram re-layout, backprojection,
 // the matched adjoint's zeroing, scatter and fold, and the "plans" forward's
@@ -345,6 +348,11 @@ int launch_batch3d_forward(const Prob3d *d_probs, const int *starts,
                            const int totals[kBatch3dStages], int count, cudaStream_t s);
 int launch_batch3d_backward(const Prob3d *d_probs, const int *starts,
                             const int totals[kBatch3dStages], int count, cudaStream_t s);
+// the matched adjoint (adjoint.cu): the plan's quad accumulators (allocated
+// on first use) and the zeroing, scatter and fold stages over a batch
+int ensure_adj3d_quads(Plan3d &p);
+int launch_batch3d_adjoint(const Prob3d *d_probs, const int *starts,
+                           const int totals[kBatch3dStages], int count, cudaStream_t s);
 
 // Reads CURADON_GB300_ALGO ("fwd2d=tex,bwd2d=smem,fwd3d=tex2l,...") over the
 // defaults of a new plan.

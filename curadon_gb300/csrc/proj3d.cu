@@ -1076,13 +1076,17 @@ int bind_batch3d_problem(Plan3d &p, float *vol, float *sino, float *ax, Prob3d *
 
     const long long bricks = (long long)ceil_div(r.tiles_x, 2) * ceil_div(r.tiles_y, 8) *
                              ceil_div(r.tiles_z, 8) * 128;
+    const long long elems = (long long)(p.X + 2 * kP3) * (p.Y + 2 * kP3) * (p.Z + 2 * kP3);
     const long long b[kBatch3dStages] = {
         ceil_div((long long)n, 256),
         (long long)ceil_div(p.Z + kQP, 32) * ceil_div(p.X + kQP, 32) * (p.Y + kQP),
         (long long)r.utiles * p.nangles * ceil_div(p.V, 8),
         ceil_div((long long)(p.U + 2 * kP3) * (p.V + 2 * kP3) * p.nangles, 256),
         r.axial ? bricks : 0,
-        r.axial ? 0 : bricks};
+        r.axial ? 0 : bricks,
+        ceil_div(2 * elems, 256),
+        (long long)r.utiles * p.nangles * ceil_div(p.V, 8),
+        ceil_div((long long)p.X * p.Y * p.Z, 256)};
     for (int st = 0; st < kBatch3dStages; ++st) {
         if (b[st] >= (1ll << 31)) return set_error(CG_ERR_INVALID, "problem too large for a batch");
         blocks[st] = (int)b[st];

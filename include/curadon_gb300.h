@@ -101,20 +101,15 @@ int cg_plan2d_destroy(cg_plan2d *plan);
 int cg_plan2d_get_forward_block(const cg_plan2d *plan, uint64_t *bx, uint64_t *by);
 int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by);
 
-/* Algorithm of each operator of a plan; -1 leaves one unchanged.
+/* Algorithm of each operator of a plan; -1 leaves one unchanged; other
+ * values are rejected with CG_ERR_INVALID.
  *   forward:  0 registers (FP32 filtering of pair-packed copies, gathered
- *               through L1), 1 texture unit, 2 texture unit + registers on
- *               alternate warps, 3 shared-memory row slabs, 4 chunked
- *               shared-memory slabs, 5 chunked slabs beside the texture unit
- *               on a share of the views (an internal stream forked from and
- *               joined back into the caller's)
- *   backward: 0 registers, 1 texture unit, 2 shared-memory detector windows,
- *             3 windows beside the texture unit on a share of the pixel rows
- *             (circular geometry, at most 2048 views)
+ *               through L1), 1 texture unit, 4 chunked shared-memory slabs
+ *   backward: 0 registers, 1 texture unit, 2 shared-memory detector windows
  * The texture unit filters with 8-bit weight fractions, exactly as the
  * reference does; the other algorithms filter in FP32, and cg_adjoint_2d is
- * the transpose of forward algorithms 0, 3 and 4 (exact for 0 and 3; 4 takes
- * the same samples and weights, summed in another order).  A new plan starts
+ * the transpose of forward algorithms 0 and 4 (exact for 0; 4 takes the
+ * same samples and weights, summed in another order).  A new plan starts
  * at the fastest measured combination: forward 4 from 704^2 pixels, else 1;
  * backward 2. */
 int cg_plan2d_set_algorithm(cg_plan2d *plan, int forward, int backward);
@@ -191,10 +186,10 @@ int cg_plan3d_create(cg_plan3d **plan, int device, const uint64_t vol_shape[3],
                      float COR);
 int cg_plan3d_destroy(cg_plan3d *plan);
 
-/* Algorithm of each 3D operator; -1 leaves one unchanged.
+/* Algorithm of each 3D operator; -1 leaves one unchanged; other values are
+ * rejected with CG_ERR_INVALID.
  *   forward:  0 registers (FP32 trilinear from pair-packed copies),
- *             1 texture unit (tex3D), 2 texture unit bilinear per layer +
- *             FP32 lerp across layers, 3 shared-memory slabs (FP32),
+ *             1 texture unit (tex3D),
  *             4 quads (FP32 trilinear, two 16-byte loads per sample),
  *             5 quads with 3 of every 8 warps (4 from 300^3 voxels) on the
  *             texture unit (default)
@@ -202,7 +197,7 @@ int cg_plan3d_destroy(cg_plan3d *plan);
  *             view maps the volume's y axis onto the detector's v axis
  *             (circular orbits without detector tilt; default), else 0.
  * cg_plan3d_get_algorithm reports the backward algorithm that runs.
- * cg_adjoint_3d_plan is the transpose of forward algorithms 0, 3 and 4 (the
+ * cg_adjoint_3d_plan is the transpose of forward algorithms 0 and 4 (the
  * same samples and trilinear weights, up to FP32 rounding). */
 int cg_plan3d_set_algorithm(cg_plan3d *plan, int forward, int backward);
 int cg_plan3d_get_algorithm(const cg_plan3d *plan, int *forward, int *backward);
@@ -335,6 +330,15 @@ int cg_batch3d_create(cg_batch3d **batch, cg_plan3d *const *plans, float *const 
 int cg_batch3d_destroy(cg_batch3d *batch);
 int cg_batch3d_forward(cg_batch3d *batch, void *stream);
 int cg_batch3d_backward(cg_batch3d *batch, void *stream);
+/* volume_i += the matched adjoint (cg_adjoint_3d_plan's operator, the exact
+ * transpose of the quad forward without texture warps) of projections_i for
+ * every problem, as three launches over the work list (zeroing, scatter,
+ * fold); equal to cg_adjoint_3d_plan up to the order of its atomic
+ * additions.  Pairs with a batch of plans on forward algorithm 4.  The first
+ * call allocates the plans' accumulators (make it before any stream
+ * capture).  No counterpart in the reference, whose gradient is its
+ * backprojector (python/standalone/src/curadon/diffable.py:14-38). */
+int cg_batch3d_adjoint(cg_batch3d *batch, void *stream);
 /* later calls run problems [0, active) only, as cg_batch2d_set_active */
 int cg_batch3d_set_active(cg_batch3d *batch, int active);
 

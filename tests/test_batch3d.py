@@ -7,7 +7,8 @@ plan's texture warps, axial or general backprojection) on each problem's
 buffers with the problem's own block index, so results must equal the
 single-problem operators bit for bit; CUDA-graph replay must equal direct
 calls, and the autograd wrapper's gradient must be the batched
-backprojection."""
+backprojection (or, matched, the batched adjoint, which passes the dot
+test)."""
 import numpy as np
 import pytest
 import torch
@@ -162,5 +163,29 @@ def test_batch3d_projector_autograd(cuda_device):
         assert torch.equal(ys, r), k
     for k, (gv, r) in enumerate(zip(proj.split_volumes(x.grad), bw)):
         assert torch.equal(gv, r), k
-    with pytest.raises(ValueError):
-        BatchProjector(geoms, cuda_device, matched=True)
+
+
+def test_batch3d_matched_adjoint(cuda_device):
+    """The batched matched adjoint equals the single-problem one up to the
+    order of its atomic additions and passes the dot test <A x, y> =
+    <x, A^T y> per problem to 1e-5 relative (A the quad forward without
+    texture warps); ``BatchProjector(..., matched=True)``'s gradient is it."""
+    from curadon_gb300 import adjoint
+
+    geoms, vols, _ = mixed_problems(cuda_device, seed=4)
+    gen = torch.Generator(device="cpu").manual_seed(5)
+    ys = [torch.rand(g.sinogram_shape(), generator=gen).to(cuda_device) for g in geoms]
+    proj = BatchProjector(geoms, cuda_device, matched=True)
+    x = torch.cat([v.reshape(-1) for v in vols]).requires_grad_(True)
+    ax = proj(x)
+    w = torch.cat([y.reshape(-1) for y in ys])
+    (ax * w).sum().backward()
+    torch.cuda.synchronize()
+    for k, (g, v, y, a_x, aty) in enumerate(zip(geoms, vols, ys, proj.split_sinograms(ax.detach()),
+                                                 proj.split_volumes(x.grad))):
+        lhs = float((a_x.double() * y.double()).sum())
+        rhs = float((v.double() * aty.double()).sum())
+        assert abs(lhs - rhs) <= 1e-5 * abs(lhs), (k, lhs, rhs)
+        single = adjoint(y, torch.zeros_like(v), g)
+        torch.cuda.synchronize()
+        assert torch.allclose(aty, single, rtol=1e-5, atol=1e-5 * float(single.abs().max())), k

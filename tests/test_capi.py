@@ -138,5 +138,6 @@ def test_batch_entry_points_reject_null(lib):
     assert lib.cg_batch3d_create(C.byref(h), None, None, None, 1) == _lib.CG_ERR_INVALID
     assert lib.cg_batch3d_forward(None, None) == _lib.CG_ERR_INVALID
     assert lib.cg_batch3d_backward(None, None) == _lib.CG_ERR_INVALID
+    assert lib.cg_batch3d_adjoint(None, None) == _lib.CG_ERR_INVALID
     assert lib.cg_batch3d_set_active(None, 1) == _lib.CG_ERR_INVALID
     assert lib.cg_batch3d_destroy(None) == _lib.CG_OK
