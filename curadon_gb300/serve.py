@@ -14,7 +14,8 @@ relative L2 1e-3).
 
 2D FBP and SIRT requests below 704^2 pixels are coalesced: requests of one
 geometry and kind that wait together run as one batch on a resident
-``Batch2d`` of that geometry class (up to ``batch_slots`` problems, one
+``Batch2d`` of that geometry class (built only when two requests of the
+class wait together, reused while it stays resident; up to ``batch_slots`` problems, one
 filter launch and one batched backprojection for FBP; for SIRT each
 iteration is one batched forward, one batched backprojection and three
 elementwise launches over all of them, captured once per batch size as a
@@ -104,7 +105,7 @@ def request_bytes(req: Request) -> int:
 
 
 class _Slot:
-    def __init__(self, device: torch.device, max_resident: int):
+    def __init__(self, device: torch.device, max_resident: int, retire=None):
         self.stream = torch.cuda.Stream(device)
         # 2D requests run on a high-priority stream: when a 3D request's long
         # kernels occupy the GPU, the block scheduler starts the 2D blocks as
@@ -114,6 +115,8 @@ class _Slot:
         self.device = device
         self.resident: "collections.OrderedDict[tuple, object]" = collections.OrderedDict()
         self.max_resident = max_resident
+        # receives the resources the LRU evicts (None: dropped at once)
+        self.retire = retire
 
     def resource(self, kind: str, geom: Geom):
         key = (kind, _geom_key(geom))
@@ -128,7 +131,9 @@ class _Slot:
                 r = (g, None)
             self.resident[key] = r
             while len(self.resident) > self.max_resident:
-                self.resident.popitem(last=False)
+                old = self.resident.popitem(last=False)[1]
+                if self.retire is not None:
+                    self.retire(old)
         else:
             self.resident.move_to_end(key)
         return r
@@ -270,11 +275,21 @@ class Server:
         self.max_class_batches = int(max_class_batches)
         self._classes: "collections.OrderedDict[tuple, _ClassBatch]" = collections.OrderedDict()
         self.batches_run = 0
-        self.slots = [_Slot(self.device, max_resident) for _ in range(slots)]
+        # resources evicted from the slots' and the class batches' caches:
+        # releasing a plan's device memory (cudaFree) synchronises the whole
+        # device, which would stall this thread until every request in flight
+        # finished, so they are released while nothing is in flight, or all
+        # at once when retire_limit of them wait
+        self._graveyard: List[object] = []
+        self.retire_limit = 256
+        self.slots = [_Slot(self.device, max_resident, self._graveyard.append)
+                      for _ in range(slots)]
         self.free = list(range(slots))
         self.budget = float(hbm_budget)
         self.inflight_bytes = 0
         self._pending: "collections.deque[tuple]" = collections.deque()
+        # waiting requests per class key (batchable requests only)
+        self._waiting: "collections.Counter[tuple]" = collections.Counter()
         self._inflight: List[tuple] = []
         self._cv = threading.Condition()
         self._stop = False
@@ -298,6 +313,8 @@ class Server:
             meta = (_heavy(req), _class_key(req) if _batchable(req) else None,
                     request_bytes(req))
             self._pending.append((req, fut, meta))
+            if meta[1] is not None:
+                self._waiting[meta[1]] += 1
             self._cv.notify()
         return fut
 
@@ -342,10 +359,14 @@ class Server:
                     return None
                 if key is not None and cb is None:
                     # a new class batch holds `batch_slots` problems' buffers and
-                    # plans for as long as it stays resident: without room for
-                    # them in the budget the request runs on its own
+                    # plans for as long as it stays resident, and building it
+                    # (a plan per problem) stalls this thread: it is built only
+                    # when another request of the class waits too, and only
+                    # with room for it in the budget; else the request runs on
+                    # its own
                     extra = self.batch_slots * need
-                    if self.resident_bytes() + self.inflight_bytes + extra > self.budget:
+                    if (self._waiting[key] < 2 or
+                            self.resident_bytes() + self.inflight_bytes + extra > self.budget):
                         key = None
                 items = [(req, fut)]
                 taken = [idx]
@@ -361,6 +382,11 @@ class Server:
                             taken.append(j)
                             need += n2
                 for j in reversed(taken):
+                    ck = self._pending[j][2][1]
+                    if ck is not None:
+                        self._waiting[ck] -= 1
+                        if self._waiting[ck] <= 0:
+                            del self._waiting[ck]
                     del self._pending[j]
                 return items, need, key
             return None
@@ -376,7 +402,7 @@ class Server:
             self._classes[key] = cb
             while len(self._classes) > self.max_class_batches:
                 old_key = next(k for k, v in self._classes.items() if not v.busy)
-                del self._classes[old_key]
+                self._graveyard.append(self._classes.pop(old_key))
         else:
             self._classes.move_to_end(key)
         return cb
@@ -454,11 +480,16 @@ class Server:
         while True:
             with self._cv:
                 if self._stop and not self._pending and not self._inflight:
+                    self._graveyard.clear()
                     return
                 if not self._pending and not self._inflight:
+                    self._graveyard.clear()
                     self._cv.wait(timeout=0.05)
                     continue
             admitted = self._admit()
             polled = self._poll()
+            if self._graveyard and (not self._inflight
+                                    or len(self._graveyard) >= self.retire_limit):
+                self._graveyard.clear()
             if not admitted and not polled:
                 time.sleep(50e-6)

@@ -133,6 +133,11 @@ def test_waiting_2d_requests_are_coalesced(cuda_device):
     assert srv.batches_run < len(reqs)
     for i, (out, ref) in enumerate(zip(outs, alone)):
         assert torch.equal(out, ref), i
+    # the blocker waited alone: no class batch (a plan per problem) was built for it
+    from curadon_gb300.serve import _class_key
+
+    assert _class_key(blocker) not in srv._classes
+    assert _class_key(reqs[0]) in srv._classes
 
 
 def test_3d_requests_leave_slots_for_2d(cuda_device):
@@ -155,3 +160,23 @@ def test_3d_requests_leave_slots_for_2d(cuda_device):
             assert rel_l2(out, ref) < 1e-3
         else:
             assert torch.equal(out, ref)
+
+
+def test_evicted_resources_are_released_when_idle(cuda_device):
+    """With one resident geometry per slot every new geometry evicts the last
+    one; evicted plans wait (their release would synchronise the device)
+    until nothing is in flight, and results stay those of the request alone."""
+    reqs = [fan_request("fbp", n, 60, k, cuda_device) for k, n in enumerate((96, 112, 128))]
+    want = [solve_alone(r, cuda_device.index or 0).cpu() for r in reqs]
+    srv = Server(cuda_device.index or 0, slots=1, max_resident=1, batching=False)
+    try:
+        got = [f.result() for f in [srv.submit(r) for r in reqs]]
+        deadline = time.time() + 5.0
+        while srv._graveyard and time.time() < deadline:
+            time.sleep(0.01)
+        assert not srv._graveyard
+        assert len(srv.slots[0].resident) == 1
+    finally:
+        srv.close()
+    for g_, w in zip(got, want):
+        assert torch.equal(g_.cpu(), w)
