@@ -124,6 +124,7 @@ int cg_batch2d_create(cg_batch2d **batch, cg_plan2d *const *plans, float *const 
         q.tex = p.tex_vol, q.arr = p.arr_vol;
         q.quadA = p.d_quadA, q.quadB = p.d_quadB;
         q.chunked = batch_chunked(p) ? 1 : 0;
+        q.bwd_sym = p.bwd_sym;
         int blocks[kBatchStages];
         batch_blocks(p, blocks);
         for (int st = 0; st < kBatchStages; ++st) {

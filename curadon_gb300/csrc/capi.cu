@@ -1,10 +1,12 @@
 // capi.cu -- the extern "C" boundary (include/curadon_gb300.h): argument
 // checking, plan construction and the operator entry points.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
+#include <initializer_list>
 #include <utility>
 #include <vector>
 
@@ -116,6 +118,10 @@ void apply_algo_env(Plan2d *p2, Plan3d *p3) {
         if (p2 && key == "adj2d") {
             if (val == "pair") p2->adj_quad = 0;
             if (val == "quad") p2->adj_quad = 1;
+        }
+        if (p2 && key == "bwd2d_sym") {
+            if (val == "off") p2->bwd_sym_mode = -1;
+            if (val == "on") p2->bwd_sym_mode = 1;
         }
         if (p2 && key == "bwd2d_minb")
             for (int k : kBwdStagedVariants)
@@ -480,6 +486,59 @@ int vec_tables(cg_plan2d &p, const float *vecs, float2 *src, float2 *u0, float2 
 
 }  // namespace
 
+namespace {
+
+// Sets p.bwd_sym where view v + n/4 is view v turned by a quarter turn about
+// the image centre and the image is large enough to gain (+1: it sees pixel (Y, -X) as view v sees (X, Y); -1: it
+// sees (-Y, X)), read off the plan's projective tables: the staged
+// backprojection then evaluates the geometry once for four (pixel, view)
+// pairs.  Needs a square image of an even size whose pixel centres are
+// symmetric about its centre; the tables must agree to 1e-5 of their
+// magnitude (the views' fast sine / cosine differ in the last bits).
+int detect_bwd_symmetry(Plan2d &p) {
+    p.bwd_sym = 0;
+    if (p.vec || p.bwd_sym_mode < 0 || p.W != p.H || (p.W & 1) || p.nangles < 4 ||
+        p.nangles % 4 || p.sx != p.sy || p.ox != p.oy)
+        return CG_OK;
+    // a quarter of the tiles: below three blocks per SM the GPU is not
+    // filled and the per-view kernel is faster (n = 512 / 1024)
+    if (p.bwd_sym_mode == 0 && sym_quadrant_blocks(p.W) < 3 * sm_count()) return CG_OK;
+    const float ex = (float)p.W / 2.0f;
+    const float c0 = (0.f - ex) * p.sx + p.ox + 0.5f;
+    const float c1 = ((float)(p.W - 1) - ex) * p.sx + p.ox + 0.5f;
+    if (std::fabs(c0 + c1) > 1e-6f * std::fabs(c0)) return CG_OK;
+    const int n = p.nangles, q = n / 4;
+    std::vector<float4> t(2 * (size_t)n);
+    CG_TRY_CUDA(cudaMemcpy(t.data(), p.d_bproj, sizeof(float4) * t.size(),
+                           cudaMemcpyDeviceToHost));
+    float sa = 0.f, sb = 0.f;
+    for (int v = 0; v < n; ++v) {
+        sa = std::max({sa, std::fabs(t[v].x), std::fabs(t[v].y)});
+        sb = std::max({sb, std::fabs(t[n + v].x), std::fabs(t[n + v].y)});
+    }
+    constexpr float tol = 1e-5f;
+    for (int dir : {1, -1}) {
+        bool ok = true;
+        for (int v = 0; v < n && ok; ++v) {
+            const int u = (v + q) % n;
+            const float4 a = t[v], a2 = t[u], b = t[n + v], b2 = t[n + u];
+            const float ax = dir > 0 ? a.y : -a.y, ay = dir > 0 ? -a.x : a.x;
+            const float bx = dir > 0 ? b.y : -b.y, by = dir > 0 ? -b.x : b.x;
+            ok = std::fabs(a2.x - ax) <= tol * sa && std::fabs(a2.y - ay) <= tol * sa &&
+                 std::fabs(a2.z - a.z) <= tol * std::fabs(a.z) &&
+                 std::fabs(b2.x - bx) <= tol * sb && std::fabs(b2.y - by) <= tol * sb &&
+                 std::fabs(b2.z - b.z) <= tol * sb;
+        }
+        if (ok) {
+            p.bwd_sym = dir;
+            break;
+        }
+    }
+    return CG_OK;
+}
+
+}  // namespace
+
 int cg_plan2d_create(cg_plan2d **plan, int device, uint32_t vol_prec, const uint64_t vol_shape[2],
                      const float vol_spacing[2], const float vol_offset[2], uint32_t det_prec,
                      uint64_t det_count, float det_spacing, float det_offset, const float *DSO,
@@ -539,6 +598,7 @@ int cg_plan2d_create(cg_plan2d **plan, int device, uint32_t vol_prec, const uint
         cudaError_t e = cudaStreamSynchronize(0);
         if (e != cudaSuccess) return fail(set_error(CG_ERR_CUDA, cudaGetErrorString(e)));
     }
+    if ((rc = detect_bwd_symmetry(*p))) return fail(rc);
     *plan = p.release();
     return CG_OK;
 }

@@ -121,6 +121,15 @@ struct Plan2d {
     // cp.async) or 27 ((t, d) pairs, 32 x 1-pixel warps); the autotuner's
     // candidates
     int bwd_min_blocks = 68;
+    // staged backprojection over the views' quarter-turn symmetry: +1 / -1
+    // when view v + nangles/4 is view v turned by +-90 degrees about the
+    // image centre (checked on the plan's tables at creation), square
+    // centred pixels; 0 otherwise or where disabled
+    int bwd_sym = 0;
+    // CURADON_GB300_ALGO bwd2d_sym=off / on: never, or wherever the geometry
+    // has the symmetry (default: where the first quadrant's tiles give every
+    // SM at least three blocks)
+    int bwd_sym_mode = 0;
 
     // row pitches of layA / layB in pairs, even so every row starts on 16 bytes
     int pitchA() const { return (W + 2 * kPad + 1) & ~1; }
@@ -141,6 +150,7 @@ struct Prob2d {
     cudaArray_t arr;          // and its array
     float4 *quadA, *quadB;    // matched adjoint: the plan's quad accumulators
     int chunked;              // the batched "plans" forward runs the chunked kernel
+    int bwd_sym;              // the plan's quarter-turn symmetry (Plan2d::bwd_sym)
 };
 
 // Problem of a batched launch's block b: the last i with start[i] <= b
@@ -184,10 +194,11 @@ struct Prob3d {
 constexpr int kBatch3dStages = 9;
 
 // Batched stages: re-layout, forward, sinogram re-layout, backprojection,
-// the matched adjoint's zeroing, scatter and fold, and the "plans" forward's
+// the matched adjoint's zeroing, scatter and fold, the "plans" forward's
 // absolute-position re-layout and chunked bundles (chunked problems) and
-// texture rays (the others).
-constexpr int kBatchStages = 10;
+// texture rays (the others), and the backprojection over the quarter-turn
+// symmetry (problems whose plan has it; stage 3 holds the others).
+constexpr int kBatchStages = 11;
 // chunked-forward shape the batched "plans" forward compiles
 constexpr int kBatchChunkShape = 484;
 
@@ -319,6 +330,9 @@ int launch_adjoint2d(Plan2d &p, float *vol, const float *sino, cudaStream_t s);
 int launch_adjoint3d(Plan3d &p, float *vol, const float *sino, cudaStream_t s);
 
 int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s);
+// blocks of the quarter-turn backprojection of a W x W image
+int sym_quadrant_blocks(int W);
+int sm_count();
 // rows: chunk shape (4, 8: rows of 256-cell bundles; 104, 108: 4 or 8 rows
 // of 128-cell bundles)
 int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int rows, int v0 = 0,

@@ -1039,6 +1039,253 @@ __device__ __forceinline__ void bwd2d_smem_tile(float *__restrict__ vol,
     }
 }
 
+// The staged backprojection over the views' quarter-turn symmetry.  When
+// view v + n/4 is view v turned by 90 degrees about the image centre (the
+// same DSO / DSD; a circular orbit whose n views, n divisible by 4, are
+// spaced evenly over a full turn) and the pixels are square and centred,
+// view v + n/4 sees pixel R P = (y, W - 1 - x) exactly as view v sees
+// P = (x, y): the same denominator, weight and detector coordinate.  Each
+// block therefore takes a tile of the image's first quadrant and its three
+// turned copies: per view v and pixel P one projective evaluation (two FMAs,
+// a reciprocal, one FMA, the floor) serves the four (pixel, view) pairs
+// (R^i P, v + i n/4), each of which adds its own view's sample at the same
+// detector coordinate from its own staged window row, so per sample only
+// the shared-memory load and the lerp remain.  The four rows of a view
+// share one window (the turned tile projects to the same interval);
+// kSymViews views per pass, 4 kSymViews rows staged by bulk copies on the
+// block's mbarrier.  DIR = -1: view v + n/4 sees R^-1 P instead.  Every
+// pixel still sums all n views, in the order v + i n/4, v = 0 .. n - 1.
+// NV views per pass, windows of WIN pairs.
+constexpr int kSymR = 4, kSymNV = 16, kSymWin = 80;
+template <int R, int NV, int WIN>
+__device__ __forceinline__ void bwd2d_sym_tile(float *__restrict__ vol,
+                                               const float2 *__restrict__ S,
+                                               const float4 *__restrict__ proj, int W, int det,
+                                               int nangles, float sx, float ox, float ds,
+                                               int dir, int bx, int by) {
+    constexpr int kSymViews = NV;
+    constexpr int kRow = WIN + 2;  // pairs per staged row
+    constexpr int kRows = 4 * kSymViews;
+    static_assert(kRows <= 256, "one thread per staged row");
+    static_assert(kRows % 32 == 0, "warp 0 counts the bulk rows in whole-warp rounds");
+    static_assert(kRow * sizeof(float2) % 16 == 0, "bulk rows are multiples of 16 bytes");
+    __shared__ __align__(16) float2 srow[kRows][kRow];
+    __shared__ float4 sA[kSymViews], sB[kSymViews];
+    __shared__ int sa0[kSymViews];
+    __shared__ int sshift[kRows], sbulk[kRows];
+    __shared__ __align__(8) unsigned long long s_bar;
+    const unsigned bar = (unsigned)__cvta_generic_to_shared(&s_bar);
+    unsigned phase = 0;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int half = W / 2, q = nangles / 4;
+    const int xt = bx * 32, yt = by * (8 * R);
+    const int x = xt + (int)((threadIdx.y & 3) * 8 + (threadIdx.x & 7));
+    const int y0 = yt + (int)((threadIdx.y >> 2) * 4 + (threadIdx.x >> 3));
+    const float ex = (float)W / 2.0f;
+    const float edm = (float)det / 2.0f - 0.5f;
+    const int cq = det / 2;
+    const float edq = edm - (float)cq;
+    const float inv = __fdividef(1.0f, ds);
+    const float X = ((float)x - ex) * sx + ox + 0.5f;
+    float2 Y2[R / 2], acc[4][R / 2];
+#pragma unroll
+    for (int i = 0; i < R / 2; ++i) {
+        Y2[i] = make_float2(((float)(y0 + 16 * i) - ex) * sx + ox + 0.5f,
+                            ((float)(y0 + 16 * i + 8) - ex) * sx + ox + 0.5f);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[k][i] = make_float2(0.f, 0.f);
+    }
+    const int pitch = det + 2 * kPad;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        mbar_fence_init();
+    }
+    // a wait that gives up stops the tile at the next group of views, as in
+    // bwd2d_smem_tile
+    int gave_up = 0;
+    for (int v0 = 0; v0 < nangles; v0 += kSymViews) {
+        const int nv = min(kSymViews, nangles - v0);
+        if (__syncthreads_or(gave_up)) break;
+        if (tid < nv) {
+            const float4 a = proj[v0 + tid], b = proj[nangles + v0 + tid];
+            sA[tid] = a, sB[tid] = b;
+            float lo = FLT_MAX, hi = -FLT_MAX, dmin = FLT_MAX;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float cX = ((float)(xt + (c & 1) * 31) - ex) * sx + ox + 0.5f;
+                const float cY = ((float)(yt + (c >> 1) * (8 * R - 1)) - ex) * sx + ox + 0.5f;
+                const float den = fmaf(a.y, cY, fmaf(a.x, cX, a.z));
+                const float yi = fmaf(b.y, cY, fmaf(b.x, cX, b.z));
+                const float ub = fmaf(__fdividef(1.0f, den), yi, edm);
+                lo = fminf(lo, ub);
+                hi = fmaxf(hi, ub);
+                dmin = fminf(dmin, den);
+            }
+            int a0 = INT_MIN;
+            if (dmin > 0.f && lo >= -1e6f && hi <= 1e6f) {
+                const int l0 = (int)floorf(lo) - 1, l1 = (int)floorf(hi) + 1;
+                if (l1 - l0 + 1 <= WIN) a0 = l0;
+            }
+            sa0[tid] = a0;
+        }
+        __syncthreads();
+        // rows 4 j + i: view (v0 + j + i q) mod n, pairs from a0 (shift 0) or
+        // a0 - 1 (shift 1) so that a bulk copy starts on 16 bytes
+        if (tid < 4 * nv) {
+            const int j = tid >> 2, i = tid & 3;
+            const int a0 = sa0[j];
+            int shift = 0, bulk = 0;
+            if (a0 != INT_MIN) {
+                const long long view = (v0 + j + (long long)i * q) % nangles;
+                const int par = (int)((view * pitch + kPad + a0) & 1);
+                bulk = a0 - par >= -kPad && a0 - par + kRow <= det + kPad;
+                shift = bulk ? par : 0;  // rows copied pair by pair start at a0
+            }
+            sshift[tid] = shift;
+            sbulk[tid] = bulk;
+        }
+        __syncthreads();
+        if (tid < 32) {
+            // every lane takes part in every round (kRows is a multiple of 32)
+            unsigned nb = 0;
+#pragma unroll
+            for (int round = 0; round < kRows / 32; ++round) {
+                const int rr = round * 32 + tid;
+                nb += __popc(__ballot_sync(0xffffffffu, rr < 4 * nv && sbulk[rr]));
+            }
+            if (tid == 0) {
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(bar, nb * (unsigned)(kRow * sizeof(float2)));
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        if (tid < kRows) {
+            const bool mine = tid < 4 * nv && sbulk[tid];
+            if (mine) {
+                const int j = tid >> 2, i = tid & 3;
+                const long long view = (v0 + j + (long long)i * q) % nangles;
+                fence_proxy_async_smem();
+                bulk_copy_g2s((unsigned)__cvta_generic_to_shared(&srow[tid][0]),
+                              S + (size_t)view * pitch + kPad + sa0[j] - sshift[tid],
+                              (unsigned)(kRow * sizeof(float2)), bar);
+            }
+        }
+        // rows whose window reaches past the padded sinogram row: pair by pair,
+        // clamped (shift 0)
+        {
+            const int w = tid >> 5, ln = tid & 31;
+            for (int rr = w; rr < 4 * nv; rr += 8) {
+                const int j = rr >> 2, i = rr & 3;
+                const int a0 = sa0[j];
+                if (a0 == INT_MIN || sbulk[rr]) continue;
+                const long long view = (v0 + j + (long long)i * q) % nangles;
+                for (int e = ln; e < kRow; e += 32) {
+                    const int k = min(max(a0 + e, -kPad), det);
+                    const unsigned d = (unsigned)__cvta_generic_to_shared(&srow[rr][e]);
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d),
+                                 "l"(S + (size_t)view * pitch + kPad + k));
+                }
+            }
+        }
+        asm volatile("cp.async.wait_all;\n" ::);
+        if (mbar_wait(bar, phase, kWaitTries)) phase ^= 1u;
+        else gave_up = 1;
+        __syncthreads();
+#pragma unroll 2
+        for (int j = 0; j < nv; ++j) {
+            const float4 a = sA[j], b = sB[j];
+            const int a0 = sa0[j];
+            const float A = fmaf(a.x, X, a.z), B = fmaf(b.x, X, b.z);
+            const float2 ay = make_float2(a.y, a.y), by = make_float2(b.y, b.y);
+            const float2 A2 = make_float2(A, A), B2 = make_float2(B, B);
+            const float2 e2 = make_float2(edq, edq);
+            if (a0 != INT_MIN) {
+                const float2 *p[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) p[i] = &srow[4 * j + i][sshift[4 * j + i]];
+                const unsigned base = 0x4B400000u + (unsigned)(a0 - cq);
+#pragma unroll
+                for (int r = 0; r < R; r += 2) {
+                    const float2 Yr = Y2[r >> 1];
+                    const float2 den = __ffma2_rn(ay, Yr, A2);
+                    const float2 yi = __ffma2_rn(by, Yr, B2);
+                    const float2 w = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+                    const float2 ub = __ffma2_rn(w, yi, e2);
+                    const float2 M2 = make_float2(12582912.0f, 12582912.0f);
+                    const float2 t = __fadd2_rd(ub, M2);
+                    const unsigned l0 = min(__float_as_uint(t.x) - base, (unsigned)(kRow - 2));
+                    const unsigned l1 = min(__float_as_uint(t.y) - base, (unsigned)(kRow - 2));
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const float2 t0 = p[i][l0], t1 = p[i][l1];
+                        const float2 v = make_float2(fmaf(ub.x, t0.y, t0.x),
+                                                     fmaf(ub.y, t1.y, t1.x));
+                        acc[i][r >> 1] = __ffma2_rn(v, w, acc[i][r >> 1]);
+                    }
+                }
+            } else {
+                // a window wider than kSmWin: the four rows from global memory
+#pragma unroll
+                for (int r = 0; r < R; r += 2) {
+                    const float2 Yr = Y2[r >> 1];
+                    const float2 den = __ffma2_rn(ay, Yr, A2);
+                    const float2 yi = __ffma2_rn(by, Yr, B2);
+                    const float2 w = make_float2(rcp_approx(den.x), rcp_approx(den.y));
+                    const float2 ub = __ffma2_rn(w, yi, e2);
+                    const unsigned c0 = min((unsigned)((int)floorf(ub.x) + cq + kPad),
+                                            (unsigned)(det + kPad));
+                    const unsigned c1 = min((unsigned)((int)floorf(ub.y) + cq + kPad),
+                                            (unsigned)(det + kPad));
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const long long view = (v0 + j + (long long)i * q) % nangles;
+                        const float2 *row = S + (size_t)view * pitch;
+                        const float2 t0 = __ldg(row + c0), t1 = __ldg(row + c1);
+                        const float2 v = make_float2(fmaf(ub.x, t0.y, t0.x),
+                                                     fmaf(ub.y, t1.y, t1.x));
+                        acc[i][r >> 1] = __ffma2_rn(v, w, acc[i][r >> 1]);
+                    }
+                }
+            }
+        }
+    }
+    if (__syncthreads_or(gave_up) && tid == 0) {
+        atomicAdd(&g_wait_timeouts, 1ull);
+        if (gave_up) mbar_wait(bar, phase, kWaitTries);
+    }
+    if (x >= half) return;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int y = y0 + 8 * r;
+        if (y >= half) continue;
+        // pixel R^k P for row i: k = i (DIR +1) or -i mod 4 (DIR -1)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const float v = (r & 1) ? acc[i][r >> 1].y : acc[i][r >> 1].x;
+            const int k = dir > 0 ? i : (4 - i) & 3;
+            int px = x, py = y;
+            if (k == 1) px = y, py = W - 1 - x;
+            else if (k == 2) px = W - 1 - x, py = W - 1 - y;
+            else if (k == 3) px = W - 1 - y, py = x;
+            vol[(size_t)py * W + px] += v * inv;
+        }
+    }
+}
+
+// 4 pixels per thread (32 x 32-pixel tiles of the first quadrant), 16 views
+// per pass (64 rows of 82 pairs, 43 KB): measured fastest of the shapes
+// tried (2 or 4 pixels, 8 or 16 views, windows of 64, 80 or 128 pairs), at
+// n = 1536 / 2048 / 4096 14-16 % below the per-view kernel.
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB)
+    k_bwd2d_sym(float *__restrict__ vol, const float2 *__restrict__ S,
+                const float4 *__restrict__ proj, int W, int det, int nangles, float sx, float ox,
+                float ds, int dir) {
+    bwd2d_sym_tile<kSymR, kSymNV, kSymWin>(vol, S, proj, W, det, nangles, sx, ox, ds, dir,
+                                           blockIdx.x, blockIdx.y);
+}
+
 // MINB: resident blocks per SM the register allocation must allow
 template <int MINB, bool PK, bool MAGIC = false, int VU = 2, bool CPA = false, bool ABS = false,
           bool MAPQ = false, bool BULK = false, int R = kSmRows>
@@ -1130,6 +1377,19 @@ __global__ void __launch_bounds__(256, 4)
                                                            q.oy, q.ds, local % gx, local / gx);
 }
 
+// The quarter-turn symmetric tile of the single-problem default for the
+// problems whose plan has the symmetry (their first quadrant's tiles).
+__global__ void __launch_bounds__(256, 4)
+    k_batch_bwd2d_sym(const Prob2d *__restrict__ probs, const int *__restrict__ start,
+                      int count) {
+    const int i = batch_problem(start, count, blockIdx.x);
+    const Prob2d &q = probs[i];
+    const int local = blockIdx.x - start[i];
+    const int gx = (q.W / 2 + 31) / 32;
+    bwd2d_sym_tile<kSymR, kSymNV, kSymWin>(q.vol, q.sinoP, q.bproj, q.W, q.det, q.nangles, q.sx,
+                                           q.ox, q.ds, q.bwd_sym, local % gx, local / gx);
+}
+
 }  // namespace
 
 // Blocks of each batched stage for one problem (the launch shapes of the
@@ -1138,7 +1398,8 @@ void batch_blocks(const Plan2d &p, int blocks[kBatchStages]) {
     blocks[0] = ceil_div(p.W + 2 * kPad, kTile) * ceil_div(p.H + 2 * kPad, kTile);
     blocks[1] = ceil_div(p.det, 32) * ceil_div(p.nangles, 8);
     blocks[2] = (int)ceil_div((long long)p.pitchS() * p.nangles, 256);
-    blocks[3] = ceil_div(p.W, 32) * ceil_div(p.H, 8 * kSmRows);
+    blocks[3] = p.bwd_sym ? 0 : ceil_div(p.W, 32) * ceil_div(p.H, 8 * kSmRows);
+    blocks[10] = p.bwd_sym ? ceil_div(p.W / 2, 32) * ceil_div(p.W / 2, 8 * kSymR) : 0;
     // matched adjoint: 1024 float4 zeroed per block, one ray per thread in
     // 32 x 8 blocks, one voxel per thread in 32 x 8 blocks
     blocks[4] = (int)ceil_div((long long)(adj2d_quad_elems(p, true) + adj2d_quad_elems(p, false)),
@@ -1186,7 +1447,12 @@ int launch_batch2d(const Prob2d *probs, const int *starts, const int totals[kBat
     } else {
         k_batch_relayout_sino2d<<<totals[2], 256, 0, s>>>(probs, starts + 2 * (count + 1), count);
         CG_TRY_CUDA(cudaGetLastError());
-        k_batch_bwd2d<<<totals[3], tile, 0, s>>>(probs, starts + 3 * (count + 1), count);
+        if (totals[3] > 0)
+            k_batch_bwd2d<<<totals[3], tile, 0, s>>>(probs, starts + 3 * (count + 1), count);
+        CG_TRY_CUDA(cudaGetLastError());
+        if (totals[10] > 0)
+            k_batch_bwd2d_sym<<<totals[10], tile, 0, s>>>(probs, starts + 10 * (count + 1),
+                                                          count);
     }
     CG_TRY_CUDA(cudaGetLastError());
     return CG_OK;
@@ -1236,7 +1502,7 @@ int launch_relayout_sino2d(const Plan2d &p, const float *sino, cudaStream_t s) {
 }
 
 // Streaming multiprocessors of the current device (looked up once per device).
-static int sm_count() {
+int sm_count() {
     static int counts[64] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
@@ -1249,7 +1515,18 @@ static int sm_count() {
     return counts[dev];
 }
 
+int sym_quadrant_blocks(int W) { return ceil_div(W / 2, 32) * ceil_div(W / 2, 8 * kSymR); }
+
 int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s) {
+    if (p.bwd_sym != 0) {
+        // the first quadrant's tiles, each with its three turned copies
+        const int half = p.W / 2;
+        const dim3 grid(ceil_div(half, 32), ceil_div(half, 8 * kSymR));
+        k_bwd2d_sym<4><<<grid, dim3(32, 8), 0, s>>>(vol, p.d_sinoP, p.d_bproj, p.W, p.det,
+                                                 p.nangles, p.sx, p.ox, p.ds, p.bwd_sym);
+        CG_TRY_CUDA(cudaGetLastError());
+        return CG_OK;
+    }
     // tiles of 32 x 64 pixels; an image whose tiles would not give every SM
     // two blocks takes 32 x 16-pixel tiles (two pixels per thread) instead,
     // four times the blocks, the same sums

@@ -315,3 +315,25 @@ def test_batch_unrolled_gradient_descent_graph_equals_eager(cuda_device):
     print(f"graph-replayed vs eager iterates: rel-L2 {e:.2e}; losses {losses[0]:.3e} -> "
           f"{losses[-1]:.3e}")
     assert e <= 1e-4
+
+
+def test_batch_quarter_turn_backprojection(cuda_device, monkeypatch):
+    """Problems whose plans take the quarter-turn backprojection (forced on
+    here for small images) run it in the batch too: equal to the
+    single-problem backprojection bit for bit, beside problems without the
+    symmetry in the same launch."""
+    monkeypatch.setenv("CURADON_GB300_ALGO", "bwd2d_sym=on")
+    geoms, vols, sinos = [], [], []
+    for k, (n, nangles) in enumerate([(128, 128), (256, 360), (130, 90), (192, 200), (96, 64)]):
+        g = FanGeometry(**fan_config(n, nangles), device=cuda_device.index or 0)
+        geoms.append(g)
+        vols.append(ellipses_2d(n, 40 + k, device=cuda_device).contiguous())
+        sinos.append(torch.zeros(g.sinogram_shape(), device=cuda_device))
+    fw, bw = reference_results(geoms, vols, cuda_device)
+    b = Batch2d(geoms, vols, sinos)
+    b.forward()
+    outs = [v.clone() for v in vols]
+    Batch2d(geoms, outs, sinos).backward()
+    torch.cuda.synchronize()
+    for i, (o, r) in enumerate(zip(outs, bw)):
+        assert torch.equal(o, r), i

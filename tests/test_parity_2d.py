@@ -327,7 +327,8 @@ def test_bulk_staged_backprojector_equals_pairwise_staging(cuda_device, monkeypa
     out = {}
     wait_timeouts()
     for variant in (48, 68):
-        monkeypatch.setenv("CURADON_GB300_ALGO", f"bwd2d=smem,bwd2d_minb={variant}")
+        monkeypatch.setenv("CURADON_GB300_ALGO",
+                           f"bwd2d=smem,bwd2d_minb={variant},bwd2d_sym=off")
         geom = FanGeometry(**g, device=cuda_device.index or 0)
         geom.plan
         monkeypatch.delenv("CURADON_GB300_ALGO")
@@ -367,3 +368,66 @@ def test_full_size_backprojection_cross_check(cuda_device):
     print(f"n=2048 staged vs texture bwd rel-L2 {e:.2e} max-abs {max_abs(b1.cpu(), bt.cpu()):.2e}")
     assert e < TOL
     assert rel_l2(b12.cpu(), (2 * b1 - b2).cpu()) < 1e-5
+
+
+def _bwd_with(g, sino, dev, monkeypatch, algo=None):
+    if algo:
+        monkeypatch.setenv("CURADON_GB300_ALGO", algo)
+    geom = FanGeometry(**g, device=dev.index or 0)
+    geom.plan
+    if algo:
+        monkeypatch.delenv("CURADON_GB300_ALGO")
+    v = torch.zeros(tuple(geom.vol_shape), device=dev)
+    backward(torch.as_tensor(sino, device=dev), v, geom)
+    torch.cuda.synchronize()
+    return v.cpu()
+
+
+@pytest.mark.parametrize("n,nangles,reverse", [(64, 360, False), (256, 256, False),
+                                               (1000, 500, False), (512, 512, True),
+                                               (2048, 2048, False)])
+def test_quarter_turn_backprojection(cuda_device, monkeypatch, n, nangles, reverse):
+    """Circular orbits whose views come in quarter turns (n views spaced
+    evenly over a full turn, n divisible by 4) on square centred images take
+    the staged backprojection over the symmetry (one projective evaluation
+    for four (pixel, view) pairs; reversed angles turn the other way): it
+    differs from the per-view evaluation only in the last bits of the views'
+    tables, and matches the oracle."""
+    g = fan_config(n, nangles)
+    if reverse:
+        g["angles"] = np.ascontiguousarray(-g["angles"])
+    rng = np.random.default_rng(n + nangles)
+    sino = rng.uniform(0, 1, (nangles, g["det_shape"])).astype(np.float32)
+    # forced on (by default only images whose first quadrant fills the GPU,
+    # from about 1536^2 pixels, take it)
+    sym = _bwd_with(g, sino, cuda_device, monkeypatch, "bwd2d_sym=on")
+    per_view = _bwd_with(g, sino, cuda_device, monkeypatch, "bwd2d_sym=off")
+    default = _bwd_with(g, sino, cuda_device, monkeypatch)
+    assert torch.equal(default, sym if n >= 2048 else per_view)
+    e = rel_l2(sym, per_view)
+    print(f"n={n} views={nangles}: symmetric vs per-view rel-L2 {e:.2e} "
+          f"max-abs {max_abs(sym, per_view):.2e}")
+    assert not torch.equal(sym, per_view)  # the symmetric kernel ran
+    assert e < 2e-5
+    if n <= 512:
+        eo = rel_l2(sym, oracle.bwd2d(g, sino))
+        print(f"  vs oracle {eo:.2e}")
+        assert eo < TOL
+
+
+@pytest.mark.parametrize("case", ["views", "offset", "rect"])
+def test_no_quarter_turn_without_the_symmetry(cuda_device, monkeypatch, case):
+    """Geometries without the symmetry (views not in quarter turns, an
+    off-centre image, a rectangular image) take the per-view kernel even
+    when the symmetric one is forced on: equal bit for bit with it off."""
+    if case == "views":
+        g = fan_config(128, 90)
+    elif case == "offset":
+        g = dict(fan_config(128, 128), vol_offset=(3.0, -2.0))
+    else:
+        g = dict(fan_config(128, 128), vol_shape=(128, 96))
+    rng = np.random.default_rng(7)
+    sino = rng.uniform(0, 1, (len(g["angles"]), g["det_shape"])).astype(np.float32)
+    a = _bwd_with(g, sino, cuda_device, monkeypatch, "bwd2d_sym=on")
+    b = _bwd_with(g, sino, cuda_device, monkeypatch, "bwd2d_sym=off")
+    assert torch.equal(a, b)
