@@ -41,6 +41,7 @@ KERNELS = {
     ("fan", "forward", "texture"): "k_fwd2d_tex", ("fan", "forward", "chunked"): "k_fwd2d_cslab",
     ("fan", "forward", "registers"): "k_fwd2d", ("fan", "backward", "shared"): "k_bwd2d_smem",
     ("fan", "backward", "registers"): "k_bwd2d", ("fan", "backward", "texture"): "k_bwd2d_tex",
+    ("fan", "backward", "shared, quarter-turn"): "k_bwd2d_sym",
     ("cone", "forward", "texture"): "k_fwd3d_tex3", ("cone", "forward", "registers"): "k_fwd3d",
     ("cone", "forward", "quad"): "k_fwd3d_quad", ("cone", "forward", "mixed"): "k_fwd3d_quad",
     ("cone", "backward", "registers"): "k_bwd3d", ("cone", "backward", "axial"): "k_bwd3d_ax",
@@ -369,6 +370,15 @@ def time_reference_gpu(ref, wl, vol, steps: int, warmup: int, flush, stream):
     return tf, tb, sino
 
 
+def plan_algorithms(geom) -> dict:
+    """The plan's algorithm names; a 2D staged backprojection that runs over
+    the views' quarter-turn symmetry is named so."""
+    algos = dict(zip(("forward", "backward"), geom.plan.algorithm))
+    if algos["backward"] == "shared" and getattr(geom.plan, "quarter_turn", 0):
+        algos["backward"] = "shared, quarter-turn"
+    return algos
+
+
 def roofline_of(wl, ms_fwd, ms_bwd, algos, peaks):
     """Roofline of the dominant operator: compulsory bytes per call over its
     event-timed duration against the measured HBM copy peak, with the
@@ -494,7 +504,7 @@ def run_ours(args, rank, world, local_rank):
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
     except (OSError, ValueError):
         pass
-    algos = dict(zip(("forward", "backward"), geom.plan.algorithm))
+    algos = plan_algorithms(geom)
 
     line = {
         "metric": "fwd/bwd proj ops/s", "value": value, "unit": "ops/s", "n_gpus": world,
@@ -570,7 +580,7 @@ def cone512_comparison(args, dev, flush, stream):
     tf, tb = time_steps(fwd, bwd, steps, warmup, flush, stream)
     raise_on_wait_timeouts()
     mf, mb = sum(tf) / steps, sum(tb) / steps
-    algos = dict(zip(("forward", "backward"), geom.plan.algorithm))
+    algos = plan_algorithms(geom)
     out = {"workload": wl["config"]["workload"], "steps": steps, "warmup": warmup,
            "ms_forward": mf, "ms_backward": mb, "ms_per_step": mf + mb,
            "ops_s": 2e3 / (mf + mb), "algorithms": algos,
@@ -764,7 +774,7 @@ def run_sweep(args):
         wl = workload(f"fan{n}")
         geom, vol, sino, vbp = make_problem(wl, dev)
         row = {"n": n, "views": n, "det": wl["geom"]["det_shape"],
-               "algorithms": dict(zip(("forward", "backward"), geom.plan.algorithm))}
+               "algorithms": plan_algorithms(geom)}
         row["ms_forward"] = timed(lambda: cg.forward(vol, sino, geom))
         row["ms_backward"] = timed(lambda: cg.backward(sino, vbp, geom))
         raise_on_wait_timeouts()

@@ -29,6 +29,7 @@ SIGNATURES = [
     ("cg_plan2d_set_forward_block", C.c_int, [C.c_void_p, C.c_uint64, C.c_uint64]),
     ("cg_plan2d_set_algorithm", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("cg_plan2d_get_algorithm", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("cg_plan2d_get_symmetry", C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     ("cg_plan2d_set_shapes", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("cg_wait_timeouts", C.c_int, [C.POINTER(C.c_ulonglong)]),
     ("cg_plan2d_get_shapes", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),

@@ -153,6 +153,15 @@ class plan_2d:
         check(self._L.cg_plan2d_get_algorithm(self._h, C.byref(f), C.byref(b)))
         return _algo_name(f.value, FORWARD_2D), _algo_name(b.value, BACKWARD_2D)
 
+    @property
+    def quarter_turn(self) -> int:
+        """+1 / -1 where the staged backprojection runs over the views'
+        quarter-turn symmetry (one projective evaluation for four (pixel,
+        view) pairs), else 0."""
+        q = C.c_int()
+        check(self._L.cg_plan2d_get_symmetry(self._h, C.byref(q)))
+        return q.value
+
     def set_algorithm(self, forward=None, backward=None):
         """Selects the algorithms (names from FORWARD_2D / BACKWARD_2D)."""
         check(self._L.cg_plan2d_set_algorithm(

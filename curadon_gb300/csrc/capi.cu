@@ -709,6 +709,13 @@ int cg_plan2d_get_algorithm(const cg_plan2d *plan, int *forward, int *backward) 
     return CG_OK;
 }
 
+int cg_plan2d_get_symmetry(const cg_plan2d *plan, int *quarter_turn) {
+    clear_error();
+    CG_REQUIRE(plan && quarter_turn, "NULL argument");
+    *quarter_turn = plan->bwd_sym;
+    return CG_OK;
+}
+
 int cg_plan2d_set_shapes(cg_plan2d *plan, int forward_shape, int backward_variant) {
     clear_error();
     CG_REQUIRE(plan, "plan is NULL");

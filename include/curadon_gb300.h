@@ -115,6 +115,18 @@ int cg_plan2d_set_forward_block(cg_plan2d *plan, uint64_t bx, uint64_t by);
 int cg_plan2d_set_algorithm(cg_plan2d *plan, int forward, int backward);
 int cg_plan2d_get_algorithm(const cg_plan2d *plan, int *forward, int *backward);
 
+/* Whether the staged backprojection (algorithm 2) of this plan runs over
+ * the views' quarter-turn symmetry: *quarter_turn = +1 / -1 where view
+ * v + nangles/4 is view v turned by +-90 degrees about the image centre
+ * (same DSO / DSD, square image of an even size with centred pixels; found
+ * on the plan's tables at creation) and the image is large enough for its
+ * first quadrant's 32 x 32-pixel tiles to give every SM three blocks, else
+ * 0.  One projective evaluation then serves the four (pixel, view) pairs
+ * the turn relates; results differ from the per-view evaluation only by
+ * the last bits of the views' tables (relative L2 ~3e-6 at n = 2048).
+ * CURADON_GB300_ALGO=bwd2d_sym=off / on overrides the size rule. */
+int cg_plan2d_get_symmetry(const cg_plan2d *plan, int *quarter_turn);
+
 /* Kernel shape of the chunked forward (used by forward algorithms 4 and 5)
  * and variant of the staged backprojector (backward algorithms 2 and 3); -1
  * keeps the current one.  Shapes: 4, 104, 108, 204, 304, 308, 404, 408, 414,
