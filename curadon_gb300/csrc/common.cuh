@@ -333,13 +333,11 @@ int launch_backward2d_smem(const Plan2d &p, float *vol, cudaStream_t s);
 // blocks of the quarter-turn backprojection of a W x W image
 int sym_quadrant_blocks(int W);
 int sm_count();
-// rows: chunk shape (4, 8: rows of 256-cell bundles; 104, 108: 4 or 8 rows
-// of 128-cell bundles)
+// rows: the chunked forward's compiled shape (kFwdChunkShapes: 443, 474,
+// 484); views [v0, v0 + nv), all by default
 int launch_forward2d_cslab(const Plan2d &p, float *sino, cudaStream_t s, int rows, int v0 = 0,
                            int nv = -1);
-int launch_forward2d_tex_views(const Plan2d &p, float *sino, int v0, int nv, cudaStream_t s);
-// Copies the volume into the plan's 2D texture array.
-int load_vol_texture(Plan2d &p, const float *vol, cudaStream_t s);
+// The plan's 2D volume texture array and object (allocated once).
 int ensure_vol_texture(Plan2d &p);
 // the first `active` problems of a batch (the work list's blocks [0, total))
 int launch_batch2d_fwd_tex(const Prob2d *d_probs, const std::vector<Prob2d> &probs, int active,

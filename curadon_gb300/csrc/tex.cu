@@ -270,19 +270,6 @@ int launch_forward2d_tex(Plan2d &p, const float *vol, float *sino, cudaStream_t 
     return CG_OK;
 }
 
-// Views [v0, v0 + nv) from the volume texture already loaded.
-int launch_forward2d_tex_views(const Plan2d &p, float *sino, int v0, int nv, cudaStream_t s) {
-    if (nv <= 0) return CG_OK;
-    dim3 block(p.fwd_bx, p.fwd_by);
-    dim3 grid(ceil_div(p.det, p.fwd_bx), ceil_div(nv, p.fwd_by));
-    if (grid.y > 65535) return set_error(CG_ERR_INVALID, "too many views for one launch");
-    k_fwd2d_tex<<<grid, block, 0, s>>>(p.tex_vol, sino + (size_t)v0 * p.det, p.d_src + v0,
-                                       p.d_u0 + v0, p.d_du + v0, p.W, p.H, p.det, nv, p.sx,
-                                       p.sy);
-    CG_TRY_CUDA(cudaGetLastError());
-    return CG_OK;
-}
-
 int ensure_vol_texture(Plan2d &p) {
     if (!p.arr_vol) {
         int rc = alloc_array(&p.arr_vol, p.W, p.H, 0, cudaArrayDefault);
@@ -312,17 +299,6 @@ int launch_batch2d_fwd_tex_stage(const Prob2d *d_probs, const std::vector<Prob2d
     if (total == 0) return CG_OK;
     k_batch_fwd2d_tex<<<total, dim3(32, 8), 0, s>>>(d_probs, starts, (int)probs.size());
     CG_TRY_CUDA(cudaGetLastError());
-    return CG_OK;
-}
-
-int load_vol_texture(Plan2d &p, const float *vol, cudaStream_t s) {
-    if (!p.arr_vol) {
-        int rc = alloc_array(&p.arr_vol, p.W, p.H, 0, cudaArrayDefault);
-        if (rc) return rc;
-        if ((rc = make_texture(p.arr_vol, &p.tex_vol))) return rc;
-    }
-    CG_TRY_CUDA(cudaMemcpy2DToArrayAsync(p.arr_vol, 0, 0, vol, sizeof(float) * p.W,
-                                         sizeof(float) * p.W, p.H, cudaMemcpyDeviceToDevice, s));
     return CG_OK;
 }
 
