@@ -127,16 +127,16 @@ int cg_plan2d_get_algorithm(const cg_plan2d *plan, int *forward, int *backward);
  * CURADON_GB300_ALGO=bwd2d_sym=off / on overrides the size rule. */
 int cg_plan2d_get_symmetry(const cg_plan2d *plan, int *quarter_turn);
 
-/* Kernel shape of the chunked forward (used by forward algorithms 4 and 5)
- * and variant of the staged backprojector (backward algorithms 2 and 3); -1
- * keeps the current one.  Shapes: 4, 104, 108, 204, 304, 308, 404, 408, 414,
- * 418, 428, 438-444, 447-451, 453, 463, 473, 474, 484 (default); variants: 3, 4,
- * 5, 14, 24-28, 37, 38, 48, 68 (default).  Every shape computes the reference's
- * samples and weights; they differ in rows per chunk, views per bundle,
- * threads per cell, pair layout and register bounds, so the fastest depends
+/* Kernel shape of the chunked forward (forward algorithm 4) and variant of
+ * the staged backprojector (backward algorithm 2); -1 keeps the current one.
+ * Shapes: 443, 474, 484 (default); variants: 27, 48, 68 (default).  Every
+ * shape computes the reference's samples and weights; they differ in rows
+ * per chunk, pair layout, staging and warp layout, so the fastest depends
  * on the geometry (no reference counterpart: the reference has one kernel
- * per direction, forward_2d.hpp:21-79 and backward_2d.hpp:21-100).  Used by
- * the autotuner (curadon_gb300.autotune).  CG_ERR_INVALID for an unknown
+ * per direction, forward_2d.hpp:21-79 and backward_2d.hpp:21-100).  Where
+ * the backprojection runs over the views' quarter-turn symmetry
+ * (cg_plan2d_get_symmetry) the variant has no effect.  Used by the
+ * autotuner (curadon_gb300.autotune).  CG_ERR_INVALID for an unknown
  * shape. */
 int cg_plan2d_set_shapes(cg_plan2d *plan, int forward_shape, int backward_variant);
 int cg_plan2d_get_shapes(const cg_plan2d *plan, int *forward_shape, int *backward_variant);
