@@ -76,6 +76,10 @@ def parse():
                    help="skip the reference's own CUDA operators beside ours (default run)")
     p.add_argument("--batch-forward", default="plans", choices=["plans", "texture", "registers"],
                    help="forward algorithm of the batch workload")
+    p.add_argument("--batch3d-sizes", default="48,64,96,128",
+                   help="volume edges n (n^3 voxels) drawn for --workload batch3d")
+    p.add_argument("--batch3d-count", type=int, default=24,
+                   help="problems of --workload batch3d")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="CPU work budget of the cpu_baseline sample")
     return p.parse_args()
@@ -1230,11 +1234,12 @@ def run_batch(args):
     return line
 
 
-def batch3d_problems(dev, count: int = 24):
+def batch3d_problems(dev, count: int = 24, sizes=(48, 64, 96, 128)):
     """The 3D batched workload: ``count`` circular cone-beam problems, n ~
-    U{48, 64, 96, 128} (n^3 volumes), 90..360 views, ceil(1.5 n)^2 cells of
-    1.5, source-isocentre 2n, isocentre-detector n, data y = A x + Poisson
-    noise (I0 = 1e4) from a seeded ellipsoid phantom."""
+    U{sizes} (n^3 volumes; default 48, 64, 96, 128), 90..360 views,
+    ceil(1.5 n)^2 cells of 1.5, source-isocentre 2n, isocentre-detector n,
+    data y = A x + Poisson noise (I0 = 1e4) from a seeded ellipsoid
+    phantom."""
     import torch
 
     from curadon_gb300 import ConeGeometry, forward
@@ -1243,7 +1248,7 @@ def batch3d_problems(dev, count: int = 24):
     rng = np.random.default_rng(seed_for(5, 0))
     out = []
     for k in range(count):
-        n = int(rng.choice([48, 64, 96, 128]))
+        n = int(rng.choice(list(sizes)))
         nangles = int(rng.integers(90, 361))
         cfg = cone_config(n, nangles, int(np.ceil(1.5 * n)))
         geom = ConeGeometry(**cfg, device=dev.index or 0)
@@ -1273,7 +1278,8 @@ def run_batch3d(args):
     _build.build()
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    probs = batch3d_problems(dev)
+    probs = batch3d_problems(dev, args.batch3d_count,
+                             tuple(int(v) for v in args.batch3d_sizes.split(",")))
     count = len(probs)
     geoms = [g for g, _, _ in probs]
     ys = [y for _, _, y in probs]
